@@ -1,0 +1,173 @@
+"""ctypes access to the reference library's own CPU path (TEST INFRASTRUCTURE).
+
+``oracle/_ref/libref_driver.so`` is built from the reference sources by
+``oracle/Makefile.ref`` where the reference tree exists (it does not exist on
+the GPU host).  Used to pin the oracle restatement and to write the golden
+fixtures under tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_REPO = os.path.dirname(_HERE)
+LIB_PATH = os.path.join(_HERE, "_ref", "libref_driver.so")
+REF_TREE = os.environ.get("DSF_REFERENCE_TREE", "/root/reference")
+
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB_PATH) or os.path.isdir(os.path.join(REF_TREE, "src", "Scattering"))
+
+
+def build(jobs=8):
+    if not os.path.isdir(os.path.join(REF_TREE, "src", "Scattering")):
+        raise RuntimeError("reference tree not present")
+    subprocess.check_call(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={REF_TREE}", f"-j{jobs}"],
+                          cwd=_REPO)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        # one helper of the reference library refers to a symbol outside the
+        # compiled subset; it is never called, so bind lazily
+        _lib = C.CDLL(LIB_PATH, mode=os.RTLD_LAZY)
+    return _lib
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(C.c_void_p)
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(C.c_void_p)
+
+
+def _common(st):
+    cell = np.array(st.cell, dtype=np.float64)
+    ops = ";".join(st.sg.ops_text).encode()
+    adp = st.adp_array()
+    return cell, ops, adp
+
+
+def _outputs(n_hkl, n):
+    return dict(f=np.zeros(2 * n_hkl), d_xyz=np.zeros(3 * n), d_adp=np.zeros(6 * n), d_occ=np.zeros(n))
+
+
+def _pack(out, st, ms):
+    n = st.n_atoms
+    nadp = st.n_adp()
+    d_adp = out["d_adp"].reshape(n, 6)
+    return dict(f=out["f"][0::2] + 1j * out["f"][1::2], d_xyz=out["d_xyz"].reshape(n, 3),
+                d_adp=[d_adp[i, :nadp[i]].copy() for i in range(n)], d_occ=out["d_occ"], ms=ms)
+
+
+def hc(st, n_threads=1):
+    """HansenCoppensStructureFactorCalculator with the "CPU" engine."""
+    keep = []
+
+    def D(a):
+        arr, p = _d(a); keep.append(arr); return p
+
+    def I(a):
+        arr, p = _i(a); keep.append(arr); return p
+
+    cell, ops, adp = _common(st)
+    n = st.n_atoms
+    orb_off, orb_occ, orb_core, sto_off, sto_pow, sto_exp, sto_coeff = [0], [], [], [0], [], [], []
+    def_exp, def_npow, def_pow, anom, zs = [], [], [], [], []
+    for w in st.wfns:
+        for k, o in enumerate(w.orbitals):
+            orb_occ.append(w.occupancy[k])
+            orb_core.append(1 if k in w.core else 0)
+            sto_pow += list(o.powers); sto_exp += list(o.exponents); sto_coeff += list(o.coefficients)
+            sto_off.append(len(sto_pow))
+        orb_off.append(len(orb_occ))
+        def_exp.append(w.def_val_exp)
+        def_npow.append(len(w.def_val_pow))
+        def_pow += list(w.def_val_pow)[:5] + [0] * (5 - min(5, len(w.def_val_pow)))
+        anom += [complex(w.anomalous).real, complex(w.anomalous).imag]
+        zs.append(w.atomic_number)
+    types = st.types
+    out = _outputs(st.n_hkl, n)
+    ms = C.c_double(0)
+    atom_anom = None
+    if st.anomalous is not None:
+        atom_anom = D(np.stack([np.real(st.anomalous), np.imag(st.anomalous)], axis=1).reshape(-1))
+    rc = lib().ref_hc_sf(
+        D(cell), C.c_char_p(ops), C.c_int(n), D(st.xyz.reshape(-1)), I(st.n_adp()), D(adp.reshape(-1)),
+        D(st.occupancy), I(st.multiplicity), I(st.atom_wfn), I(st.atom_type), D(np.asarray(st.lcs).reshape(-1)),
+        C.c_int(len(st.wfns)), I(orb_off), I(orb_occ), I(orb_core), I(sto_off), I(sto_pow), D(sto_exp),
+        D(sto_coeff), D(def_exp), I(def_npow), I(def_pow), D(anom), I(zs),
+        C.c_int(len(types)), I([t.n_l for t in types]), D(np.array([t.plm for t in types]).reshape(-1)),
+        D([t.p_val for t in types]), D([t.kappa for t in types]), D([t.kappa_prime for t in types]),
+        C.c_int(st.n_hkl), I(st.hkl.reshape(-1)), D(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1)),
+        atom_anom, I(st.include_mask().astype(np.int32)), C.c_int(n_threads),
+        D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]), C.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference HC path raised an exception")
+    return _pack(out, st, ms.value)
+
+
+def D_out(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def iam_coefficients(label, table="IT92"):
+    a = np.zeros(5); b = np.zeros(5); c = C.c_double(0); n = C.c_int(0)
+    rc = lib().ref_iam_coefficients(label.encode(), table.encode(), D_out(a), D_out(b), C.byref(c), C.byref(n))
+    if rc != 0:
+        raise KeyError(label)
+    return a[: n.value].copy(), b[: n.value].copy(), c.value
+
+
+def iam(st, labels, table="IT92", n_threads=1):
+    cell, ops, adp = _common(st)
+    n = st.n_atoms
+    out = _outputs(st.n_hkl, n)
+    ms = C.c_double(0)
+    keep = [np.ascontiguousarray(x) for x in (st.xyz.reshape(-1), adp.reshape(-1))]
+    xyz, adpf = keep
+    nadp = st.n_adp(); mult = np.asarray(st.multiplicity, dtype=np.int32); occ = np.ascontiguousarray(st.occupancy)
+    hkl = np.ascontiguousarray(st.hkl.reshape(-1), dtype=np.int32)
+    g = np.ascontiguousarray(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1))
+    rc = lib().ref_iam_sf(D_out(cell), C.c_char_p(ops), C.c_char_p(";".join(labels).encode()),
+                          C.c_char_p(table.encode()), C.c_int(n), D_out(xyz), D_out(nadp), D_out(adpf),
+                          D_out(occ), D_out(mult), C.c_int(st.n_hkl), D_out(hkl), D_out(g), C.c_int(n_threads),
+                          D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]),
+                          C.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference IAM path raised an exception")
+    return _pack(out, st, ms.value)
+
+
+def table(st, keys, values):
+    """keys: (k,3) int Miller indices, values: (k, n_atoms) complex."""
+    cell, ops, adp = _common(st)
+    n = st.n_atoms
+    out = _outputs(st.n_hkl, n)
+    ms = C.c_double(0)
+    xyz = np.ascontiguousarray(st.xyz.reshape(-1)); adpf = np.ascontiguousarray(adp.reshape(-1))
+    nadp = st.n_adp(); mult = np.asarray(st.multiplicity, dtype=np.int32); occ = np.ascontiguousarray(st.occupancy)
+    hkl = np.ascontiguousarray(st.hkl.reshape(-1), dtype=np.int32)
+    g = np.ascontiguousarray(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1))
+    k = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1))
+    v = np.ascontiguousarray(np.stack([np.real(values), np.imag(values)], -1).reshape(-1))
+    rc = lib().ref_table_sf(D_out(cell), C.c_char_p(ops), C.c_int(n), D_out(xyz), D_out(nadp), D_out(adpf),
+                            D_out(occ), D_out(mult), C.c_int(len(keys)), D_out(k), D_out(v), C.c_int(st.n_hkl),
+                            D_out(hkl), D_out(g), D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]),
+                            D_out(out["d_occ"]), C.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference tabulated path raised an exception")
+    return _pack(out, st, ms.value)

@@ -1,0 +1,273 @@
+// Drives the reference library's own CPU structure-factor code for parity
+// pinning.  TEST INFRASTRUCTURE: compiled only by oracle/Makefile.ref
+// together with the reference sources where they lie; used by
+// tests/golden/make_golden.py to write golden fixtures and by the CPU
+// tests to pin the oracle restatement.  Nothing in the shipped library
+// links it.
+//
+// Entry points build the reference's own objects and call:
+//   * HansenCoppensStructureFactorCalculator + setCalculationMode("CPU")
+//     (src/Scattering/HansenCoppensStructureFactorCalculator.cpp:380-508,
+//      engine HansenCoppens_SF_Engine3) -- the HC path;
+//   * AnyScattererStructureFactorCalculator + IamFormFactorCalculationsManager
+//     (the AnyIamCalculator path, src/Scattering/AnyIamCalculator.cpp:49-154);
+//   * AnyScattererStructureFactorCalculator + ConstFormFactorCalculationsManager
+//     (the tabulated path behind TscFileBasedSfCalculator).
+#include "discamb/CrystalStructure/Crystal.h"
+#include "discamb/CrystalStructure/SpaceGroup.h"
+#include "discamb/CrystalStructure/SpaceGroupOperation.h"
+#include "discamb/CrystalStructure/UnitCell.h"
+#include "discamb/HC_Model/HC_ModelParameters.h"
+#include "discamb/Scattering/AnyScattererStructureFactorCalculator.h"
+#include "discamb/Scattering/ConstFormFactorCalculationsManager.h"
+#include "discamb/Scattering/HansenCoppensStructureFactorCalculator.h"
+#include "discamb/Scattering/IamFormFactorCalculationsManager.h"
+#include "discamb/Scattering/NGaussianFormFactorsTable.h"
+
+#include <chrono>
+#include <complex>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+using namespace discamb;
+using std::complex;
+using std::string;
+using std::vector;
+
+namespace {
+
+struct Input {
+    const double *cell;
+    const char *ops;          // ';' separated operation strings
+    int n_atoms;
+    const double *xyz;        // fractional
+    const int *n_adp;
+    const double *adp;        // U_cif / Uiso, 6 per atom
+    const double *occ;
+    const int *mult;
+    const char *atom_types;   // ';' separated element labels (IAM / labels)
+};
+
+Crystal make_crystal(const Input &in)
+{
+    Crystal c;
+    c.unitCell.set(in.cell[0], in.cell[1], in.cell[2], in.cell[3], in.cell[4], in.cell[5]);
+    vector<SpaceGroupOperation> ops;
+    std::stringstream ss(in.ops);
+    string item;
+    while (std::getline(ss, item, ';'))
+        if (!item.empty()) ops.push_back(SpaceGroupOperation(item));
+    c.spaceGroup.set(ops);
+    vector<string> labels;
+    if (in.atom_types) {
+        std::stringstream ls(in.atom_types);
+        while (std::getline(ls, item, ';')) labels.push_back(item);
+    }
+    c.atoms.resize(in.n_atoms);
+    for (int i = 0; i < in.n_atoms; i++) {
+        AtomInCrystal &a = c.atoms[i];
+        a.coordinates = Vector3d(in.xyz[3 * i], in.xyz[3 * i + 1], in.xyz[3 * i + 2]);
+        a.adp.assign(in.adp + 6 * i, in.adp + 6 * i + in.n_adp[i]);
+        a.occupancy = in.occ[i];
+        a.multiplicity = in.mult[i];
+        if (i < (int)labels.size()) { a.type = labels[i]; a.label = labels[i] + std::to_string(i + 1); }
+    }
+    c.adpConvention = structural_parameters_convention::AdpConvention::U_cif;
+    c.xyzCoordinateSystem = structural_parameters_convention::XyzCoordinateSystem::fractional;
+    return c;
+}
+
+void write_out(const vector<complex<double> > &f, const vector<TargetFunctionAtomicParamDerivatives> &d,
+               double *f_out, double *d_xyz, double *d_adp, double *d_occ)
+{
+    for (size_t i = 0; i < f.size(); i++) { f_out[2 * i] = f[i].real(); f_out[2 * i + 1] = f[i].imag(); }
+    for (size_t a = 0; a < d.size(); a++) {
+        for (int j = 0; j < 3; j++) d_xyz[3 * a + j] = d[a].atomic_position_derivatives[j];
+        for (int j = 0; j < 6; j++) d_adp[6 * a + j] = j < (int)d[a].adp_derivatives.size() ? d[a].adp_derivatives[j] : 0.0;
+        d_occ[a] = d[a].occupancy_derivatives;
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+// Hansen-Coppens path through HansenCoppensStructureFactorCalculator ("CPU").
+// Wavefunctions as Slater orbitals: per wfn [orb_off[w], orb_off[w+1]) orbitals,
+// per orbital [sto_off[o], sto_off[o+1]) Slater functions.
+int ref_hc_sf(const double *cell, const char *ops, int n_atoms, const double *xyz, const int *n_adp,
+              const double *adp, const double *occ, const int *mult, const int *atom_wfn,
+              const int *atom_type, const double *lcs,
+              int n_wfn, const int *orb_off, const int *orb_occ, const int *orb_core,
+              const int *sto_off, const int *sto_pow, const double *sto_exp, const double *sto_coeff,
+              const double *def_exp, const int *def_npow, const int *def_pow, const double *wfn_anom,
+              const int *wfn_z,
+              int n_types, const int *type_nl, const double *type_plm, const double *type_pval,
+              const double *type_kappa, const double *type_kappa_p,
+              int n_hkl, const int *hkl, const double *dtdf, const double *atom_anom, const int *include,
+              int n_threads, double *f_out, double *d_xyz, double *d_adp, double *d_occ, double *ms)
+{
+    try {
+        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, nullptr};
+        Crystal crystal = make_crystal(in);
+        HC_ModelParameters p;
+        p.wfn_parameters.resize(n_wfn);
+        for (int w = 0; w < n_wfn; w++) {
+            HC_WfnType &wt = p.wfn_parameters[w];
+            wt.wfnAtomTypeName = "W" + std::to_string(w);
+            wt.atomic_number = wfn_z[w];
+            for (int o = orb_off[w]; o < orb_off[w + 1]; o++) {
+                SlaterTypeAtomicOrbitalRdf orb;
+                for (int s = sto_off[o]; s < sto_off[o + 1]; s++) {
+                    orb.power_r.push_back(sto_pow[s]);
+                    orb.exponents.push_back(sto_exp[s]);
+                    orb.coefficients.push_back(sto_coeff[s]);
+                }
+                int idx = (int)wt.orbitals.size();
+                wt.orbitals.push_back(orb);
+                wt.orbital_occupancy.push_back(orb_occ[o]);
+                if (orb_core[o]) wt.core_orbitals_indices.push_back(idx);
+                else wt.valence_orbitals_indices.push_back(idx);
+            }
+            wt.deformation_valence_exponent = def_exp[w];
+            wt.deformation_valence_power.assign(def_pow + 5 * w, def_pow + 5 * w + def_npow[w]);
+            wt.anomalous_scattering = complex<double>(wfn_anom[2 * w], wfn_anom[2 * w + 1]);
+        }
+        p.type_parameters.resize(n_types);
+        for (int t = 0; t < n_types; t++) {
+            HC_AtomTypeParameters &tp = p.type_parameters[t];
+            tp.p_lm.resize(type_nl[t]);
+            for (int l = 0; l < type_nl[t]; l++)
+                tp.p_lm[l].assign(type_plm + 25 * t + l * l, type_plm + 25 * t + l * l + 2 * l + 1);
+            tp.p_val = type_pval[t];
+            tp.kappa_spherical_valence = type_kappa[t];
+            tp.kappa_deformation_valence = type_kappa_p[t];
+        }
+        p.atom_to_wfn_map.assign(atom_wfn, atom_wfn + n_atoms);
+        p.atom_to_type_map.assign(atom_type, atom_type + n_atoms);
+        vector<Matrix3d> lcsm(n_atoms);
+        for (int a = 0; a < n_atoms; a++)
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) lcsm[a](i, j) = lcs[9 * a + 3 * i + j];
+        HansenCoppensStructureFactorCalculator calc(crystal, p);
+        calc.setCalculationMode("CPU");
+        calc.setN_Threads(n_threads);
+        if (atom_anom) {
+            vector<complex<double> > an(n_atoms);
+            for (int a = 0; a < n_atoms; a++) an[a] = complex<double>(atom_anom[2 * a], atom_anom[2 * a + 1]);
+            calc.set_anomalous_dispersion_per_atom(an);
+        }
+        vector<Vector3i> h(n_hkl);
+        vector<complex<double> > g(n_hkl), f;
+        for (int i = 0; i < n_hkl; i++) {
+            h[i] = Vector3i(hkl[3 * i], hkl[3 * i + 1], hkl[3 * i + 2]);
+            g[i] = complex<double>(dtdf[2 * i], dtdf[2 * i + 1]);
+        }
+        vector<bool> inc(n_atoms, true);
+        if (include) for (int a = 0; a < n_atoms; a++) inc[a] = include[a] != 0;
+        vector<TargetFunctionAtomicParamDerivatives> d;
+        auto t0 = std::chrono::steady_clock::now();
+        calc.calculateStructureFactorsAndDerivatives(crystal.atoms, lcsm, h, f, d, g, inc);
+        auto t1 = std::chrono::steady_clock::now();
+        if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        write_out(f, d, f_out, d_xyz, d_adp, d_occ);
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+// Gaussian coefficients the reference's IAM table holds for a label.
+int ref_iam_coefficients(const char *label, const char *table, double *a, double *b, double *c, int *n)
+{
+    try {
+        if (!n_gaussian_form_factors_table::hasFormFactor(label, table)) return 1;
+        NGaussianFormFactor ff = n_gaussian_form_factors_table::getFormFactor(label, table);
+        vector<double> va, vb;
+        ff.get_parameters(va, vb, *c);
+        *n = (int)va.size();
+        for (int i = 0; i < *n && i < 5; i++) { a[i] = va[i]; b[i] = vb[i]; }
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+// IAM path of AnyIamCalculator: AnyScatterer engine over all operations with
+// n-Gaussian form factors from the named table.
+int ref_iam_sf(const double *cell, const char *ops, const char *labels, const char *table, int n_atoms,
+               const double *xyz, const int *n_adp, const double *adp, const double *occ, const int *mult,
+               int n_hkl, const int *hkl, const double *dtdf, int n_threads,
+               double *f_out, double *d_xyz, double *d_adp, double *d_occ, double *ms)
+{
+    try {
+        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, labels};
+        Crystal crystal = make_crystal(in);
+        AnyScattererStructureFactorCalculator calc(crystal);
+        std::shared_ptr<AtomicFormFactorCalculationsManager> mgr =
+            std::make_shared<IamFormFactorCalculationsManager>(crystal, string(table));
+        calc.setAtomicFormfactorManager(mgr);
+        vector<Vector3i> h(n_hkl);
+        vector<complex<double> > g(n_hkl), f;
+        for (int i = 0; i < n_hkl; i++) {
+            h[i] = Vector3i(hkl[3 * i], hkl[3 * i + 1], hkl[3 * i + 2]);
+            g[i] = complex<double>(dtdf[2 * i], dtdf[2 * i + 1]);
+        }
+        vector<bool> inc(n_atoms, true);
+        vector<TargetFunctionAtomicParamDerivatives> d;
+        auto t0 = std::chrono::steady_clock::now();
+        calc.calculateStructureFactorsAndDerivatives(h, f, d, g, inc);
+        auto t1 = std::chrono::steady_clock::now();
+        if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        write_out(f, d, f_out, d_xyz, d_adp, d_occ);
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+// Tabulated path: AnyScatterer engine + ConstFormFactorCalculationsManager with a
+// map from Miller index to the per-atom complex form factors.
+int ref_table_sf(const double *cell, const char *ops, int n_atoms, const double *xyz, const int *n_adp,
+                 const double *adp, const double *occ, const int *mult,
+                 int n_keys, const int *keys, const double *values /* [n_keys][n_atoms][2] */,
+                 int n_hkl, const int *hkl, const double *dtdf,
+                 double *f_out, double *d_xyz, double *d_adp, double *d_occ, double *ms)
+{
+    try {
+        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, nullptr};
+        Crystal crystal = make_crystal(in);
+        std::map<Vector3i, vector<complex<double> > > table;
+        for (int k = 0; k < n_keys; k++) {
+            vector<complex<double> > v(n_atoms);
+            for (int a = 0; a < n_atoms; a++)
+                v[a] = complex<double>(values[2 * ((size_t)k * n_atoms + a)], values[2 * ((size_t)k * n_atoms + a) + 1]);
+            table[Vector3i(keys[3 * k], keys[3 * k + 1], keys[3 * k + 2])] = v;
+        }
+        AnyScattererStructureFactorCalculator calc(crystal);
+        std::shared_ptr<AtomicFormFactorCalculationsManager> mgr =
+            std::make_shared<ConstFormFactorCalculationsManager>(crystal.unitCell, table);
+        calc.setAtomicFormfactorManager(mgr);
+        vector<Vector3i> h(n_hkl);
+        vector<complex<double> > g(n_hkl), f;
+        for (int i = 0; i < n_hkl; i++) {
+            h[i] = Vector3i(hkl[3 * i], hkl[3 * i + 1], hkl[3 * i + 2]);
+            g[i] = complex<double>(dtdf[2 * i], dtdf[2 * i + 1]);
+        }
+        vector<bool> inc(n_atoms, true);
+        vector<TargetFunctionAtomicParamDerivatives> d;
+        auto t0 = std::chrono::steady_clock::now();
+        calc.calculateStructureFactorsAndDerivatives(h, f, d, g, inc);
+        auto t1 = std::chrono::steady_clock::now();
+        if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        write_out(f, d, f_out, d_xyz, d_adp, d_occ);
+        return 0;
+    } catch (...) {
+        return 1;
+    }
+}
+
+} // extern "C"
