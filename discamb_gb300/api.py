@@ -1,0 +1,396 @@
+"""Python binding of the dsf_gb300 C ABI (include/dsf_gb300.h).
+
+``Engine`` owns one GPU and a stream; ``HcCalculator``, ``IamCalculator`` and
+``TabulatedCalculator`` mirror the reference calculators behind
+``SfCalculator::calculateStructureFactorsAndDerivatives``
+(include/discamb/Scattering/SfCalculator.h:45-67):
+
+* ``HcCalculator`` ~ HansenCoppensStructureFactorCalculator
+  (include/discamb/Scattering/HansenCoppensStructureFactorCalculator.h:42-165);
+* ``IamCalculator`` ~ AnyIamCalculator (src/Scattering/AnyIamCalculator.cpp);
+* ``TabulatedCalculator`` ~ TscFileBasedSfCalculator
+  (src/Scattering/TscFileBasedSfCalculator.cpp).
+
+``calculate_structure_factors_and_derivatives`` takes the atoms' current
+parameters, dT/dF per reflection and the inclusion mask, and returns F and
+the derivatives in the crystal's conventions; errors raise ``DsfError`` with
+the engine's message (the reference throws discamb::Exception).  The
+library must be built (``discamb_gb300.build.build()``); there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .build import LIB
+from .model import density_terms
+
+_P = C.POINTER
+
+DSF_FP64 = 0
+DSF_FP32_BULK = 1
+DSF_D_XYZ, DSF_D_ADP, DSF_D_OCC, DSF_D_MULTIPOLE = 1, 2, 4, 8
+_ADP = {"U_cif": 0, "U_cart": 1, "U_star": 2}
+_XYZ = {"fractional": 0, "cartesian": 1}
+
+
+class DsfError(RuntimeError):
+    pass
+
+
+class _Sym(C.Structure):
+    _fields_ = [("cell", C.c_double * 6), ("n_symops", C.c_int), ("symop_rotation", _P(C.c_int)),
+                ("symop_translation", _P(C.c_double)), ("centrosymmetric", C.c_int),
+                ("inversion_translation", C.c_double * 3), ("centering", C.c_char), ("obverse", C.c_int),
+                ("n_symops_total", C.c_int)]
+
+
+class _Hc(C.Structure):
+    _fields_ = [("n_wfn", C.c_int), ("core_offset", _P(C.c_int)), ("core_coeff", _P(C.c_double)),
+                ("core_exp", _P(C.c_double)), ("core_pow", _P(C.c_int)), ("val_offset", _P(C.c_int)),
+                ("val_coeff", _P(C.c_double)), ("val_exp", _P(C.c_double)), ("val_pow", _P(C.c_int)),
+                ("def_val_exp", _P(C.c_double)), ("def_val_npow", _P(C.c_int)), ("def_val_pow", _P(C.c_int)),
+                ("anomalous", _P(C.c_double)), ("n_types", C.c_int), ("type_nl", _P(C.c_int)),
+                ("type_plm", _P(C.c_double)), ("type_pval", _P(C.c_double)), ("type_kappa", _P(C.c_double)),
+                ("type_kappa_prime", _P(C.c_double))]
+
+
+class _Iam(C.Structure):
+    _fields_ = [("n_types", C.c_int), ("n_gauss", _P(C.c_int)), ("a", _P(C.c_double)), ("b", _P(C.c_double)),
+                ("c", _P(C.c_double))]
+
+
+class _Atoms(C.Structure):
+    _fields_ = [("n_atoms", C.c_int), ("atom_wfn", _P(C.c_int)), ("atom_type", _P(C.c_int)),
+                ("adp_components", _P(C.c_int)), ("lcs", _P(C.c_double)), ("multiplicity", _P(C.c_double)),
+                ("anomalous", _P(C.c_double)), ("xyz_convention", C.c_int), ("adp_convention", C.c_int)]
+
+
+class _Out(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in
+                ("f", "d_xyz", "d_adp", "d_occ", "d_pval", "d_plm", "d_kappa", "d_kappa_prime")]
+
+
+_lib = None
+
+
+def library():
+    """Loads libdsf_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise DsfError(f"CUDA engine library not built: {LIB} (run discamb_gb300.build.build())")
+        _lib = C.CDLL(LIB)
+        L = _lib
+        L.dsf_engine_create.argtypes = [C.c_int, _P(C.c_void_p)]
+        L.dsf_engine_destroy.argtypes = [C.c_void_p]
+        L.dsf_last_error.argtypes = [C.c_void_p]
+        L.dsf_last_error.restype = C.c_char_p
+        L.dsf_structure_create_hc.argtypes = [C.c_void_p, _P(_Sym), _P(_Hc), _P(_Atoms), _P(C.c_void_p)]
+        L.dsf_structure_create_iam.argtypes = [C.c_void_p, _P(_Sym), _P(_Iam), _P(_Atoms), _P(C.c_void_p)]
+        L.dsf_structure_create_tabulated.argtypes = [C.c_void_p, _P(_Sym), _P(_Atoms), C.c_int, _P(C.c_int),
+                                                     _P(C.c_double), C.c_int, _P(C.c_void_p)]
+        L.dsf_structure_destroy.argtypes = [C.c_void_p]
+        L.dsf_structure_set_hkl.argtypes = [C.c_void_p, C.c_int, _P(C.c_int)]
+        L.dsf_structure_update_atoms.argtypes = [C.c_void_p, _P(C.c_double), _P(C.c_double), _P(C.c_double)]
+        L.dsf_structure_update_types.argtypes = [C.c_void_p, _P(C.c_double), _P(C.c_double), _P(C.c_double),
+                                                 _P(C.c_double)]
+        L.dsf_structure_set_lcs.argtypes = [C.c_void_p, _P(C.c_double)]
+        L.dsf_structure_device_bytes.argtypes = [C.c_void_p]
+        L.dsf_structure_device_bytes.restype = C.c_int64
+        L.dsf_calculate.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), _P(C.c_int), _P(_Out)]
+        L.dsf_calculate_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, _P(_Out), C.c_void_p]
+        L.dsf_last_launch_count.argtypes = [C.c_void_p]
+    return _lib
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_P(C.c_double))
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(_P(C.c_int))
+
+
+class Engine:
+    """One GPU + stream (dsf_engine)."""
+
+    def __init__(self, device=0):
+        self.lib = library()
+        self.h = C.c_void_p()
+        rc = self.lib.dsf_engine_create(int(device), C.byref(self.h))
+        if rc != 0:
+            raise DsfError(f"dsf_engine_create failed with status {rc}")
+
+    def check(self, rc, what):
+        if rc != 0:
+            msg = self.lib.dsf_last_error(self.h)
+            raise DsfError(f"{what}: status {rc}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if self.h:
+            self.lib.dsf_engine_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def symmetry_desc(st, representation="engine"):
+    """dsf_symmetry of a Structure: 'engine' = subset + inversion flag (the
+    HansenCoppens CPU engine), 'all' = all operations modulo centering
+    (the generic AnyScatterer engine)."""
+    sg = st.sg
+    keep = []
+    if representation == "engine":
+        rot, tr = sg.subset_rot, sg.subset_trans
+        centro = sg.centrosymmetric
+    else:
+        # all operations, one per centering coset
+        cv = {tuple(t) for r, t in zip(sg.rot, sg.trans12) if np.array_equal(r, np.eye(3, dtype=np.int64))}
+        chosen, seen = [], set()
+        for r, t in zip(sg.rot, sg.trans12):
+            key = (r.tobytes(), tuple(t))
+            if key in seen:
+                continue
+            chosen.append((r, t))
+            for c in cv:
+                seen.add((r.tobytes(), tuple((np.array(t) + np.array(c)) % 12)))
+        rot = np.array([r for r, _ in chosen])
+        tr = np.array([t for _, t in chosen], dtype=np.float64) / 12.0
+        centro = False
+    s = _Sym()
+    for k in range(6):
+        s.cell[k] = st.cell[k]
+    s.n_symops = len(rot)
+    a, s.symop_rotation = _i(np.asarray(rot).reshape(-1)); keep.append(a)
+    b, s.symop_translation = _d(np.asarray(tr).reshape(-1)); keep.append(b)
+    s.centrosymmetric = int(centro)
+    for k in range(3):
+        s.inversion_translation[k] = float(sg.inversion_translation[k]) if centro else 0.0
+    s.centering = sg.centering.encode()
+    s.obverse = int(sg.obverse)
+    s.n_symops_total = sg.n_total
+    return s, keep
+
+
+def _atoms_desc(st, lcs=True):
+    keep = []
+    a = _Atoms()
+    a.n_atoms = st.n_atoms
+    x, a.atom_wfn = _i(st.atom_wfn); keep.append(x)
+    x, a.atom_type = _i(st.atom_type); keep.append(x)
+    x, a.adp_components = _i(st.n_adp()); keep.append(x)
+    if lcs:
+        x, a.lcs = _d(np.asarray(st.lcs).reshape(-1)); keep.append(x)
+    x, a.multiplicity = _d(np.asarray(st.multiplicity, dtype=np.float64)); keep.append(x)
+    if st.anomalous is not None:
+        x, a.anomalous = _d(np.stack([np.real(st.anomalous), np.imag(st.anomalous)], 1).reshape(-1)); keep.append(x)
+    a.xyz_convention = _XYZ[st.xyz_convention]
+    a.adp_convention = _ADP[st.adp_convention]
+    return a, keep
+
+
+def _hc_desc(st):
+    keep = []
+    m = _Hc()
+    core_off, val_off = [0], [0]
+    cc, ce, cp, vc, ve, vp, dexp, dnp, dpw, an = [], [], [], [], [], [], [], [], [], []
+    for w in st.wfns:
+        c, e, p = density_terms(w, "core"); cc += list(c); ce += list(e); cp += list(p); core_off.append(len(cc))
+        c, e, p = density_terms(w, "valence"); vc += list(c); ve += list(e); vp += list(p); val_off.append(len(vc))
+        dexp.append(w.def_val_exp); dnp.append(min(5, len(w.def_val_pow)))
+        dpw += list(w.def_val_pow)[:5] + [0] * (5 - min(5, len(w.def_val_pow)))
+        an += [complex(w.anomalous).real, complex(w.anomalous).imag]
+    m.n_wfn = len(st.wfns)
+    for name, arr, kind in [("core_offset", core_off, "i"), ("core_coeff", cc + [0.0], "d"), ("core_exp", ce + [1.0], "d"),
+                            ("core_pow", cp + [0], "i"), ("val_offset", val_off, "i"), ("val_coeff", vc + [0.0], "d"),
+                            ("val_exp", ve + [1.0], "d"), ("val_pow", vp + [0], "i"), ("def_val_exp", dexp, "d"),
+                            ("def_val_npow", dnp, "i"), ("def_val_pow", dpw, "i"), ("anomalous", an, "d")]:
+        x, p = (_i if kind == "i" else _d)(arr)
+        keep.append(x)
+        setattr(m, name, p)
+    types = st.types
+    m.n_types = len(types)
+    for name, arr, kind in [("type_nl", [t.n_l for t in types], "i"),
+                            ("type_plm", np.array([t.plm for t in types]).reshape(-1), "d"),
+                            ("type_pval", [t.p_val for t in types], "d"), ("type_kappa", [t.kappa for t in types], "d"),
+                            ("type_kappa_prime", [t.kappa_prime for t in types], "d")]:
+        x, p = (_i if kind == "i" else _d)(arr)
+        keep.append(x)
+        setattr(m, name, p)
+    return m, keep
+
+
+class _Calculator:
+    model = "hc"
+
+    def __init__(self, engine: Engine, st):
+        self.engine = engine
+        self.lib = engine.lib
+        self.st = st
+        self.h = C.c_void_p()
+        self.n_atoms = st.n_atoms
+        self.n_hkl = 0
+
+    def set_hkl(self, hkl):
+        hkl = np.ascontiguousarray(hkl, dtype=np.int32)
+        x, p = _i(hkl.reshape(-1))
+        self.engine.check(self.lib.dsf_structure_set_hkl(self.h, len(hkl), p), "set_hkl")
+        self.n_hkl = len(hkl)
+
+    def update_atoms(self, xyz, adp, occupancy):
+        adp6 = np.zeros((self.n_atoms, 6))
+        if isinstance(adp, np.ndarray) and adp.shape == (self.n_atoms, 6):
+            adp6 = adp
+        else:
+            for i, a in enumerate(adp):
+                adp6[i, :len(a)] = a
+        x1, p1 = _d(np.asarray(xyz).reshape(-1))
+        x2, p2 = _d(adp6.reshape(-1))
+        x3, p3 = _d(occupancy)
+        self.engine.check(self.lib.dsf_structure_update_atoms(self.h, p1, p2, p3), "update_atoms")
+
+    def calculate(self, dtdf, precision=DSF_FP64, derivatives=("xyz", "adp", "occ"), multipoles=False,
+                  include=None):
+        """F and dT/dparam in the crystal's conventions (host buffers)."""
+        n, m = self.n_atoms, self.n_hkl
+        flags = (DSF_D_XYZ if "xyz" in derivatives else 0) | (DSF_D_ADP if "adp" in derivatives else 0) | \
+                (DSF_D_OCC if "occ" in derivatives else 0) | (DSF_D_MULTIPOLE if multipoles else 0)
+        g = np.ascontiguousarray(np.stack([np.real(dtdf), np.imag(dtdf)], 1).reshape(-1), dtype=np.float64)
+        f = np.zeros(2 * m)
+        dx, da, do = np.zeros(3 * n), np.zeros(6 * n), np.zeros(n)
+        dpv, dplm, dk, dkp = np.zeros(n), np.zeros(25 * n), np.zeros(n), np.zeros(n)
+        o = _Out()
+        o.f = f.ctypes.data
+        o.d_xyz, o.d_adp, o.d_occ = dx.ctypes.data, da.ctypes.data, do.ctypes.data
+        if multipoles:
+            o.d_pval, o.d_plm, o.d_kappa, o.d_kappa_prime = dpv.ctypes.data, dplm.ctypes.data, dk.ctypes.data, dkp.ctypes.data
+        inc = None
+        if include is not None:
+            incarr, inc = _i(np.asarray(include, dtype=np.int32))
+        self.engine.check(self.lib.dsf_calculate(self.h, int(precision), flags, g.ctypes.data_as(_P(C.c_double)),
+                                                 inc, C.byref(o)), "calculate")
+        nadp = self.st.n_adp()
+        da = da.reshape(n, 6)
+        out = dict(f=f[0::2] + 1j * f[1::2], d_xyz=dx.reshape(n, 3), d_adp=[da[i, :nadp[i]] for i in range(n)],
+                   d_occ=do)
+        if multipoles:
+            out.update(d_pval=dpv, d_plm=dplm.reshape(n, 25), d_kappa=dk, d_kappa_p=dkp)
+        return out
+
+    def calculate_structure_factors_and_derivatives(self, xyz, adp, occupancy, hkl, dtdf, include=None,
+                                                    precision=DSF_FP64, multipoles=False):
+        """Reference-style call: atoms + hkl + dT/dF -> F and derivatives.
+        The reflection set stays resident while it does not change."""
+        hkl = np.asarray(hkl, dtype=np.int32)
+        cached = getattr(self, "_hkl_cache", None)
+        if cached is None or cached.shape != hkl.shape or not np.array_equal(cached, hkl):
+            self.set_hkl(hkl)
+            self._hkl_cache = hkl.copy()
+        self.update_atoms(xyz, adp, occupancy)
+        return self.calculate(dtdf, precision=precision, multipoles=multipoles, include=include)
+
+    def device_bytes(self):
+        return self.lib.dsf_structure_device_bytes(self.h)
+
+    def last_launch_count(self):
+        return self.lib.dsf_last_launch_count(self.h)
+
+    def close(self):
+        if self.h:
+            self.lib.dsf_structure_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class HcCalculator(_Calculator):
+    """Hansen-Coppens structure factors; symmetry as the HC CPU engine
+    (subset + inversion + centering multipliers) by default."""
+
+    def __init__(self, engine, st, representation="engine"):
+        super().__init__(engine, st)
+        sym, k1 = symmetry_desc(st, representation)
+        model, k2 = _hc_desc(st)
+        atoms, k3 = _atoms_desc(st)
+        engine.check(self.lib.dsf_structure_create_hc(engine.h, C.byref(sym), C.byref(model), C.byref(atoms),
+                                                      C.byref(self.h)), "create_hc")
+        self.set_hkl(st.hkl)
+        self.update_atoms(st.xyz, st.adp, st.occupancy)
+
+    def update_types(self, plm=None, pval=None, kappa=None, kappa_prime=None):
+        ps = [None if v is None else _d(np.asarray(v).reshape(-1)) for v in (plm, pval, kappa, kappa_prime)]
+        args = [None if p is None else p[1] for p in ps]
+        self.engine.check(self.lib.dsf_structure_update_types(self.h, *args), "update_types")
+
+    def set_lcs(self, lcs):
+        x, p = _d(np.asarray(lcs).reshape(-1))
+        self.engine.check(self.lib.dsf_structure_set_lcs(self.h, p), "set_lcs")
+
+
+class IamCalculator(_Calculator):
+    """IAM with per-type n-Gaussian form factors; all operations modulo
+    centering (the AnyScatterer engine's representation)."""
+
+    def __init__(self, engine, st, iam):
+        super().__init__(engine, st)
+        sym, k1 = symmetry_desc(st, "all")
+        m = _Iam()
+        m.n_types = len(iam["c"])
+        keep = []
+        for name, arr, kind in [("n_gauss", iam["ngauss"], "i"), ("a", np.asarray(iam["a"]).reshape(-1), "d"),
+                                ("b", np.asarray(iam["b"]).reshape(-1), "d"), ("c", iam["c"], "d")]:
+            x, p = (_i if kind == "i" else _d)(arr)
+            keep.append(x)
+            setattr(m, name, p)
+        atoms, k3 = _atoms_desc(st, lcs=False)
+        engine.check(self.lib.dsf_structure_create_iam(engine.h, C.byref(sym), C.byref(m), C.byref(atoms),
+                                                       C.byref(self.h)), "create_iam")
+        self.set_hkl(st.hkl)
+        self.update_atoms(st.xyz, st.adp, st.occupancy)
+
+
+class TabulatedCalculator(_Calculator):
+    """Tabulated complex form factors per (reflection, operation, atom) over
+    all operations modulo centering."""
+
+    def __init__(self, engine, st, table, fp32_table=False):
+        super().__init__(engine, st)
+        sym, k1 = symmetry_desc(st, "all")
+        atoms, k3 = _atoms_desc(st, lcs=False)
+        t = np.asarray(table)
+        tt = np.ascontiguousarray(np.stack([t.real, t.imag], -1).reshape(-1), dtype=np.float64)
+        x, p = _i(np.asarray(st.hkl).reshape(-1))
+        engine.check(self.lib.dsf_structure_create_tabulated(engine.h, C.byref(sym), C.byref(atoms), len(st.hkl), p,
+                                                             tt.ctypes.data_as(_P(C.c_double)), int(fp32_table),
+                                                             C.byref(self.h)), "create_tabulated")
+        self.n_hkl = len(st.hkl)
+        self.update_atoms(st.xyz, st.adp, st.occupancy)
+
+
+def all_ops_mod_centering(sg):
+    """(rot, trans) of all operations modulo lattice centering, in the
+    order symmetry_desc(..., 'all') passes them to the engine."""
+    cv = {tuple(t) for r, t in zip(sg.rot, sg.trans12) if np.array_equal(r, np.eye(3, dtype=np.int64))}
+    chosen, seen = [], set()
+    for r, t in zip(sg.rot, sg.trans12):
+        key = (r.tobytes(), tuple(t))
+        if key in seen:
+            continue
+        chosen.append((r, t))
+        for c in cv:
+            seen.add((r.tobytes(), tuple((np.array(t) + np.array(c)) % 12)))
+    return np.array([r for r, _ in chosen]), np.array([t for _, t in chosen], dtype=np.float64) / 12.0

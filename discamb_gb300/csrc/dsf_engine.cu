@@ -1,0 +1,1196 @@
+// Host side of the dsf_gb300 C ABI: resident structures, host preparation
+// (atom tiling by type, symmetry in integer form, convention matrices,
+// global-frame multipole populations) and the per-call launch sequence
+//   adjoint weights -> fused SF+adjoint kernel -> F / derivative epilogues.
+//
+// Host restatements of the reference's set-up steps:
+//   HansenCoppensStructureFactorCalculator::setModel / prepareDataForEngine_part
+//     (src/Scattering/HansenCoppensStructureFactorCalculator.cpp:157-290, 897-990)
+//   HansenCoppens_SF_Engine3::pre_hkl_loop_sf_calc (src/Scattering/HansenCoppens_SF_Engine3.cpp:195-256)
+//   HansenCoppens_SF_Engine3::calculateGlobalCoordinatesPlm (same file :594-654): here the rotation
+//     of each P_l block into the global frame is obtained by sampling the local-frame angular
+//     function at fixed directions and fitting global-frame harmonics (exact for degree-l
+//     harmonic polynomials; no Wigner recursion)
+//   scattering_utilities::centeringSfMultipliers (src/Scattering/scattering_utilities.cpp:103-170)
+//   HansenCoppensStructureFactorCalculator::convertDerivatives (same file :634-664)
+#include "../../include/dsf_gb300.h"
+#include "dsf_device.cuh"
+#include "dsf_math.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+namespace dsf {
+cudaError_t launch_sf_grad(const DevStructure &S, const CallBuffers &C, bool fp64, bool mp, int hkl_chunk, int ht,
+                           cudaStream_t st);
+size_t sf_grad_smem_bytes(bool fp64, int ht, int n_sym);
+}  // namespace dsf
+
+using namespace dsf;
+
+struct dsf_engine {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int n_sm = 0;
+    size_t max_smem = 0;
+    std::string err;
+};
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t alloc(size_t n)
+    {
+        if (n <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+struct Status {
+    int code = DSF_OK;
+    std::string msg;
+};
+
+#define DSF_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t _e = (call);                                                                    \
+        if (_e != cudaSuccess) {                                                                    \
+            return fail(e, _e == cudaErrorMemoryAllocation ? DSF_ERR_MEMORY : DSF_ERR_CUDA,         \
+                        std::string(#call) + ": " + cudaGetErrorString(_e));                        \
+        }                                                                                           \
+    } while (0)
+
+int fail(dsf_engine *e, int code, const std::string &msg)
+{
+    if (e) e->err = msg;
+    return code;
+}
+
+void mat3_mul(const double *a, const double *b, double *c)
+{
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double s = 0;
+            for (int k = 0; k < 3; k++) s += a[3 * i + k] * b[3 * k + j];
+            c[3 * i + j] = s;
+        }
+}
+
+bool mat_inverse(const double *a, double *inv, int n)
+{
+    std::vector<double> m(a, a + n * n), r(n * n, 0.0);
+    for (int i = 0; i < n; i++) r[i * n + i] = 1.0;
+    for (int c = 0; c < n; c++) {
+        int p = c;
+        for (int i = c + 1; i < n; i++)
+            if (std::fabs(m[i * n + c]) > std::fabs(m[p * n + c])) p = i;
+        if (std::fabs(m[p * n + c]) < 1e-300) return false;
+        if (p != c)
+            for (int j = 0; j < n; j++) { std::swap(m[p * n + j], m[c * n + j]); std::swap(r[p * n + j], r[c * n + j]); }
+        const double d = 1.0 / m[c * n + c];
+        for (int j = 0; j < n; j++) { m[c * n + j] *= d; r[c * n + j] *= d; }
+        for (int i = 0; i < n; i++) {
+            if (i == c) continue;
+            const double f = m[i * n + c];
+            if (f == 0.0) continue;
+            for (int j = 0; j < n; j++) { m[i * n + j] -= f * m[c * n + j]; r[i * n + j] -= f * r[c * n + j]; }
+        }
+    }
+    std::copy(r.begin(), r.end(), inv);
+    return true;
+}
+
+// UnitCell::calculateTransformationMatrices (src/CrystalStructure/UnitCell.cpp:183-212)
+void cell_matrices(const double *cell, double *M, double *Minv, double *B)
+{
+    const double f = DSF_PI / 180.0;
+    const double ca = std::cos(cell[3] * f), cb = std::cos(cell[4] * f), cg = std::cos(cell[5] * f),
+                 sg = std::sin(cell[5] * f);
+    const double phi = std::sqrt(1 - ca * ca - cb * cb - cg * cg + 2 * ca * cb * cg);
+    const double a = cell[0], b = cell[1], c = cell[2];
+    double m[9] = {a, b * cg, c * cb, 0, b * sg, (c / sg) * (ca - cb * cg), 0, 0, c * phi / sg};
+    std::copy(m, m + 9, M);
+    mat_inverse(M, Minv, 3);
+    // B = M^{-T}: columns are a*, b*, c*
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) B[3 * i + j] = Minv[3 * j + i];
+}
+
+// U (symmetric 3x3) -> Voigt param vector helpers; A6 maps U_param -> U*_param for U* = A U A^T
+void adp_param_map(const double *A, double *A6)
+{
+    static const int I[6] = {0, 1, 2, 0, 0, 1}, J[6] = {0, 1, 2, 1, 2, 2};
+    for (int p = 0; p < 6; p++)       // output param (i,j)
+        for (int q = 0; q < 6; q++) { // input param (k,l), symmetric
+            const int i = I[p], j = J[p], k = I[q], l = J[q];
+            double v = A[3 * i + k] * A[3 * j + l];
+            if (k != l) v += A[3 * i + l] * A[3 * j + k];
+            A6[6 * p + q] = v;
+        }
+}
+
+}  // namespace
+
+struct dsf_structure {
+    dsf_engine *eng = nullptr;
+    int model = MODEL_HC;
+    int n_atoms = 0, n_hkl = 0, n_sym = 0, n_types = 0, n_wfn = 0, n_tiles = 0;
+    int xyz_conv = 0, adp_conv = 0;
+    double M[9], Minv[9], B[9];
+    double A6[36];  // beta_param (without 2 pi^2) = A6 U_param
+    int centro_mode = 0;  // 0 none, 1 inversion at origin, 2 shifted
+    int t_inv24[3] = {0, 0, 0};
+    char centering = 'P';
+    int obverse = 1;
+    int n_total = 1;
+    std::vector<int> sym_rot, sym_t24;
+    std::vector<int> perm;  // sorted -> original
+    std::vector<int> tile_begin, tile_ntypes, tile_types;
+    // host model copies
+    std::vector<int> atom_type, atom_wfn, adpk;
+    std::vector<double> mult_w, anom, lcs;
+    std::vector<int> type_nl, type_wfn;
+    std::vector<double> type_plm, type_pval, type_kappa, type_kappa_p;
+    std::vector<TypeRadial> trad;
+    std::vector<double> tcoeff, texp;
+    std::vector<int> tpow;
+    std::vector<double> dmat;  // [n_atoms][165] D_l blocks (sorted order)
+    // device
+    DevBuf d_sym_rot, d_sym_t24, d_tile_begin, d_tile_ntypes, d_tile_types, d_atom_ltype, d_atom_adpk,
+        d_active, d_xq, d_xlo, d_xd, d_adp_f, d_adp_d, d_w_f, d_w_d, d_anom_f, d_anom_d, d_pg_f, d_pg_d, d_types,
+        d_tcoeff, d_texp, d_tpow, d_hkl, d_h2, d_hmult, d_cinv, d_table_f, d_table_d, d_perm, d_multw, d_dmat,
+        d_raw, d_dtdf, d_gw_d, d_gw_f, d_facc, d_gacc, d_out, d_plm_lmax;
+    std::vector<uint8_t> active_host;
+    bool have_hkl = false, have_atoms = false;
+    int last_launches = 0;
+    DevStructure dev{};
+};
+
+namespace {
+
+// ------------------------------------------------------------------------
+// small kernels: per-call adjoint weights, epilogues, atom conversion
+// ------------------------------------------------------------------------
+
+// g = conj(dT/dF) * centering multiplier; effective weight of the
+// centrosymmetric forms: 2 Re g (inversion at origin), g + conj(g c_inv) (shifted)
+__global__ void gw_kernel(int n, const double2 *dtdf, const double *mult, const double2 *cinv, int centro,
+                          double2 *gw_d, float2 *gw_f)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double m = mult[i];
+    double gre = dtdf[i].x * m, gim = -dtdf[i].y * m;
+    if (centro == 1) {
+        gre = 2.0 * gre;
+        gim = 0.0;
+    } else if (centro == 2) {
+        const double2 c = cinv[i];
+        const double pre = gre * c.x - gim * c.y, pim = gre * c.y + gim * c.x;
+        gre = gre + pre;
+        gim = gim - pim;
+    }
+    gw_d[i] = make_double2(gre, gim);
+    gw_f[i] = make_float2((float)gre, (float)gim);
+}
+
+__global__ void f_epilogue_kernel(int n, const double2 *facc, const double *mult, const double2 *cinv, int centro,
+                                  double *f_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 F = facc[i];
+    if (centro == 1) {
+        F.x = 2.0 * F.x;
+        F.y = 0.0;
+    } else if (centro == 2) {
+        const double2 c = cinv[i];
+        // F + c conj(F)
+        const double re = F.x + (c.x * F.x + c.y * F.y);
+        const double im = F.y + (c.y * F.x - c.x * F.y);
+        F.x = re;
+        F.y = im;
+    }
+    f_out[2 * i] = F.x * mult[i];
+    f_out[2 * i + 1] = F.y * mult[i];
+}
+
+struct GradParams {
+    int n_atoms;
+    int xyz_conv;   // 0 frac, 1 cart
+    double Minv[9];
+    double A6[36];  // beta = 2 pi^2 A6 U
+    int want_xyz, want_adp, want_occ, want_mp;
+};
+
+__global__ void grad_epilogue_kernel(GradParams P, const double *g_acc, const int *perm, const int *adpk,
+                                     const double *w, const double *mult_w, const double *dmat,
+                                     const int *plm_lmax, double *d_xyz,
+                                     double *d_adp, double *d_occ, double *d_pval, double *d_plm, double *d_kappa,
+                                     double *d_kappa_p)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= P.n_atoms) return;
+    const int o = perm[a];
+    const double *G = g_acc + (size_t)a * kNch;
+    const double wa = w[a];
+    const double two_pi = 2.0 * DSF_PI, two_pi2 = 2.0 * DSF_PI * DSF_PI;
+    if (P.want_xyz && d_xyz) {
+        double gf[3];
+        for (int j = 0; j < 3; j++) gf[j] = two_pi * wa * G[CH_XYZ + j];
+        if (P.xyz_conv == 1) {
+            for (int j = 0; j < 3; j++)
+                d_xyz[3 * o + j] = gf[0] * P.Minv[0 * 3 + j] + gf[1] * P.Minv[1 * 3 + j] + gf[2] * P.Minv[2 * 3 + j];
+        } else {
+            for (int j = 0; j < 3; j++) d_xyz[3 * o + j] = gf[j];
+        }
+    }
+    if (P.want_adp && d_adp) {
+        const int k = adpk[a];
+        for (int j = 0; j < 6; j++) d_adp[6 * o + j] = 0.0;
+        if (k == 1) d_adp[6 * o] = two_pi2 * wa * G[CH_ADP];
+        if (k == 6)
+            for (int q = 0; q < 6; q++) {
+                double s = 0;
+                for (int p = 0; p < 6; p++) s += P.A6[6 * p + q] * G[CH_ADP + p];
+                d_adp[6 * o + q] = two_pi2 * wa * s;
+            }
+    }
+    if (P.want_occ && d_occ) d_occ[o] = mult_w[a] * G[CH_OCC];
+    if (P.want_mp) {
+        if (d_pval) d_pval[o] = wa * G[CH_PV];
+        if (d_kappa) d_kappa[o] = wa * G[CH_KAPPA];
+        if (d_kappa_p) d_kappa_p[o] = wa * G[CH_KAPPA_P];
+        if (d_plm) {
+            const double *D = dmat + (size_t)a * 165;
+            int off = 0;
+            for (int l = 0; l <= 4; l++) {
+                const int n = 2 * l + 1;
+                for (int i = 0; i < n; i++) {
+                    double s = 0;
+                    for (int j = 0; j < n; j++) s += D[off + i * n + j] * G[CH_PLM + l * l + j];
+                    d_plm[25 * o + l * l + i] = l <= plm_lmax[a] ? wa * s : 0.0;
+                }
+                off += n * n;
+            }
+        }
+    }
+}
+
+struct AtomParams {
+    int n_atoms;
+    int xyz_conv;
+    double Minv[9];
+    double A6[36];
+};
+
+// raw atoms (original order: xyz[3], adp[6], occ) -> kernel representation (sorted order)
+__global__ void atom_convert_kernel(AtomParams P, const double *raw, const int *perm, const int *adpk,
+                                    const double *mult_w, uint32_t *xq, float *xlo, double *xd, float *adp_f,
+                                    double *adp_d, float *w_f, double *w_d)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= P.n_atoms) return;
+    const int o = perm[a];
+    const double *r = raw + (size_t)o * 10;
+    double x[3] = {r[0], r[1], r[2]};
+    if (P.xyz_conv == 1) {
+        double f[3];
+        for (int i = 0; i < 3; i++) f[i] = P.Minv[3 * i] * x[0] + P.Minv[3 * i + 1] * x[1] + P.Minv[3 * i + 2] * x[2];
+        for (int i = 0; i < 3; i++) x[i] = f[i];
+    }
+    for (int i = 0; i < 3; i++) {
+        xd[3 * a + i] = x[i];
+        const double xr = x[i] - floor(x[i]);
+        const double q = rint(xr * 4294967296.0);
+        xlo[3 * a + i] = (float)(xr - q * (1.0 / 4294967296.0));
+        xq[3 * a + i] = (uint32_t)(unsigned long long)q;  // 2^32 wraps to 0
+    }
+    const double two_pi2 = 2.0 * DSF_PI * DSF_PI;
+    const int k = adpk[a];
+    for (int i = 0; i < 6; i++) {
+        adp_d[6 * a + i] = 0.0;
+        adp_f[6 * a + i] = 0.0f;
+    }
+    if (k == 1) {
+        adp_d[6 * a] = two_pi2 * r[3];
+        adp_f[6 * a] = (float)(two_pi2 * r[3]);
+    } else if (k == 6) {
+        for (int p = 0; p < 6; p++) {
+            double s = 0;
+            for (int q = 0; q < 6; q++) s += P.A6[6 * p + q] * r[3 + q];
+            adp_d[6 * a + p] = two_pi2 * s;
+            adp_f[6 * a + p] = (float)(two_pi2 * s);
+        }
+    }
+    const double wt = r[9] * mult_w[a];
+    w_d[a] = wt;
+    w_f[a] = (float)wt;
+}
+
+// ------------------------------------------------------------------------
+// host helpers
+// ------------------------------------------------------------------------
+
+int sym_from_desc(dsf_engine *e, dsf_structure *s, const dsf_symmetry *sym)
+{
+    if (!sym || sym->n_symops < 1 || sym->n_symops > kMaxSym)
+        return fail(e, DSF_ERR_ARGUMENT, "n_symops must be in 1..48");
+    for (int i = 0; i < 3; i++)
+        if (!(sym->cell[i] > 0)) return fail(e, DSF_ERR_ARGUMENT, "cell lengths must be positive");
+    cell_matrices(sym->cell, s->M, s->Minv, s->B);
+    s->n_sym = sym->n_symops;
+    s->sym_rot.assign(sym->symop_rotation, sym->symop_rotation + 9 * s->n_sym);
+    s->sym_t24.resize(3 * s->n_sym);
+    for (int i = 0; i < 3 * s->n_sym; i++) {
+        const double t = sym->symop_translation[i] * 24.0;
+        const double r = std::rint(t);
+        if (std::fabs(t - r) > 1e-6) return fail(e, DSF_ERR_ARGUMENT, "symmetry translations must be multiples of 1/24");
+        int v = (int)r % 24;
+        if (v < 0) v += 24;
+        s->sym_t24[i] = v;
+    }
+    s->centro_mode = 0;
+    if (sym->centrosymmetric) {
+        bool origin = true;
+        for (int i = 0; i < 3; i++) {
+            const double t = sym->inversion_translation[i] * 24.0;
+            const double r = std::rint(t);
+            if (std::fabs(t - r) > 1e-6) return fail(e, DSF_ERR_ARGUMENT, "inversion translation must be a multiple of 1/24");
+            int v = (int)r % 24;
+            if (v < 0) v += 24;
+            s->t_inv24[i] = v;
+            if (v != 0) origin = false;
+        }
+        s->centro_mode = origin ? 1 : 2;
+    }
+    s->centering = sym->centering ? sym->centering : 'P';
+    s->obverse = sym->obverse;
+    s->n_total = sym->n_symops_total > 0 ? sym->n_symops_total : s->n_sym;
+    const char c = (char)toupper(s->centering);
+    if (!strchr("PABCIFR", c)) return fail(e, DSF_ERR_ARGUMENT, "unsupported lattice centering");
+    s->centering = c;
+    return DSF_OK;
+}
+
+double centering_multiplier(char c, int obverse, int h, int k, int l)
+{
+    switch (c) {
+    case 'P': return 1.0;
+    case 'R': return (std::abs(obverse ? (-h + k + l) : (h - k + l)) % 3 == 0) ? 3.0 : 0.0;
+    case 'F': {
+        const int a = std::abs(h % 2), b = std::abs(k % 2), d = std::abs(l % 2);
+        return (a == b && a == d) ? 4.0 : 0.0;
+    }
+    case 'I': return ((h + k + l) % 2 == 0) ? 2.0 : 0.0;
+    case 'A': return ((k + l) % 2 == 0) ? 2.0 : 0.0;
+    case 'B': return ((h + l) % 2 == 0) ? 2.0 : 0.0;
+    case 'C': return ((h + k) % 2 == 0) ? 2.0 : 0.0;
+    }
+    return 1.0;
+}
+
+// fixed sampling directions and the least-squares fit matrices for the
+// global-frame rotation of P_lm (per l: pinv (2l+1) x K)
+struct RotationFit {
+    static constexpr int K = 40;
+    double u[K][3];
+    std::vector<double> pinv[5];
+    RotationFit()
+    {
+        const double ga = DSF_PI * (3.0 - std::sqrt(5.0));
+        for (int k = 0; k < K; k++) {
+            const double z = 1.0 - (2.0 * k + 1.0) / K;
+            const double r = std::sqrt(1.0 - z * z);
+            u[k][0] = r * std::cos(ga * k);
+            u[k][1] = r * std::sin(ga * k);
+            u[k][2] = z;
+        }
+        for (int l = 0; l <= 4; l++) {
+            const int n = 2 * l + 1;
+            std::vector<double> A(K * n), AtA(n * n, 0.0), inv(n * n);
+            for (int k = 0; k < K; k++) {
+                double v[25];
+                harmonic_polys<double>(u[k][0], u[k][1], u[k][2], v);
+                for (int m = 0; m < n; m++) A[k * n + m] = v[l * l + m] * kDensityNormHost[l * l + m];
+            }
+            for (int i = 0; i < n; i++)
+                for (int j = 0; j < n; j++)
+                    for (int k = 0; k < K; k++) AtA[i * n + j] += A[k * n + i] * A[k * n + j];
+            mat_inverse(AtA.data(), inv.data(), n);
+            pinv[l].assign(n * K, 0.0);
+            for (int i = 0; i < n; i++)
+                for (int k = 0; k < K; k++) {
+                    double s = 0;
+                    for (int j = 0; j < n; j++) s += inv[i * n + j] * A[k * n + j];
+                    pinv[l][i * K + k] = s;
+                }
+        }
+    }
+};
+
+const RotationFit &rotation_fit()
+{
+    static RotationFit f;
+    return f;
+}
+
+// D_l with d_l(L^T u) = D_l d_l(u); stored row-major per l (165 doubles)
+void rotation_blocks(const double *L, double *D)
+{
+    const RotationFit &F = rotation_fit();
+    const int K = RotationFit::K;
+    std::vector<double> Bk(K * 25);
+    for (int k = 0; k < K; k++) {
+        double v[3];
+        for (int j = 0; j < 3; j++) v[j] = L[0 + j] * F.u[k][0] + L[3 + j] * F.u[k][1] + L[6 + j] * F.u[k][2];
+        double p[25];
+        harmonic_polys<double>(v[0], v[1], v[2], p);
+        for (int q = 0; q < 25; q++) Bk[k * 25 + q] = p[q] * kDensityNormHost[q];
+    }
+    int off = 0;
+    for (int l = 0; l <= 4; l++) {
+        const int n = 2 * l + 1;
+        // D^T = pinv * B_l  ->  D[i][j] = (pinv B)[j][i]
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                double s = 0;
+                for (int k = 0; k < K; k++) s += F.pinv[l][j * K + k] * Bk[k * 25 + l * l + i];
+                D[off + i * n + j] = s;
+            }
+        off += n * n;
+    }
+}
+
+template <typename T>
+int upload(dsf_engine *e, DevBuf &b, const T *src, size_t n)
+{
+    DSF_CUDA(b.alloc(sizeof(T) * std::max<size_t>(n, 1)));
+    if (n) DSF_CUDA(cudaMemcpyAsync(b.p, src, sizeof(T) * n, cudaMemcpyHostToDevice, e->stream));
+    return DSF_OK;
+}
+
+int compute_global_plm(dsf_structure *s)
+{
+    dsf_engine *e = s->eng;
+    const int n = s->n_atoms;
+    std::vector<double> pg(25 * (size_t)n, 0.0);
+    std::vector<float> pgf(25 * (size_t)n, 0.0f);
+    s->dmat.assign(165 * (size_t)n, 0.0);
+    for (int a = 0; a < n; a++) {
+        const int o = s->perm[a];
+        const int t = s->atom_type[o];
+        double *D = s->dmat.data() + 165 * (size_t)a;
+        rotation_blocks(s->lcs.data() + 9 * (size_t)o, D);
+        const int lmax = s->trad[t].lmax_used;
+        int off = 0;
+        for (int l = 0; l <= 4; l++) {
+            const int nl = 2 * l + 1;
+            if (l <= lmax) {
+                const double *P = s->type_plm.data() + 25 * (size_t)t + l * l;
+                for (int j = 0; j < nl; j++) {
+                    double v = 0;
+                    for (int i = 0; i < nl; i++) v += D[off + i * nl + j] * P[i];  // P_glob = D^T P
+                    pg[25 * (size_t)a + l * l + j] = v;
+                    pgf[25 * (size_t)a + l * l + j] = (float)v;
+                }
+            }
+            off += nl * nl;
+        }
+    }
+    std::vector<int> lmx(n);
+    for (int a = 0; a < n; a++) {
+        const int t = s->atom_type[s->perm[a]];
+        lmx[a] = std::min(std::min(s->type_nl[t] - 1, s->trad[t].n_def - 1), 4);
+    }
+    int rc;
+    if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return rc;
+    if ((rc = upload(e, s->d_pg_d, pg.data(), pg.size()))) return rc;
+    if ((rc = upload(e, s->d_pg_f, pgf.data(), pgf.size()))) return rc;
+    if ((rc = upload(e, s->d_dmat, s->dmat.data(), s->dmat.size()))) return rc;
+    return DSF_OK;
+}
+
+// pre_hkl_loop_sf_calc: l used in the sum and the deformation normalisation
+int build_type_radial(dsf_structure *s, const dsf_hc_model *m)
+{
+    dsf_engine *e = s->eng;
+    const int nT = s->n_types;
+    s->trad.assign(nT, TypeRadial{});
+    for (int t = 0; t < nT; t++) {
+        TypeRadial &r = s->trad[t];
+        r.pv = s->type_pval[t];
+        r.kappa = s->type_kappa[t];
+        r.kappa_p = s->type_kappa_p[t];
+        const int w = s->type_wfn[t];
+        if (m) {
+            r.zeta = m->def_val_exp[w];
+            r.n_def = std::min(5, m->def_val_npow[w]);
+            for (int l = 0; l < 5; l++) {
+                r.npow[l] = l < r.n_def ? m->def_val_pow[5 * w + l] : 0;
+                if (l < r.n_def) {
+                    if (r.npow[l] < l || r.npow[l] > 8)
+                        return fail(e, DSF_ERR_ARGUMENT, "deformation-valence r power n_l must satisfy l <= n_l <= 8");
+                    double nrm = std::pow(r.zeta, r.npow[l] + 3);
+                    for (int q = 2; q <= r.npow[l] + 2; q++) nrm /= q;
+                    r.norm[l] = nrm;
+                }
+            }
+            r.core_begin = m->core_offset[w];
+            r.core_end = m->core_offset[w + 1];
+            int lp = -1;
+            for (int l = 0; l < s->type_nl[t] && l <= 4; l++)
+                for (int q = 0; q < 2 * l + 1; q++)
+                    if (s->type_plm[25 * (size_t)t + l * l + q] != 0.0) lp = l;
+            r.lmax_used = std::min(lp, std::min(4, r.n_def - 1));
+        } else {
+            r.lmax_used = -1;
+        }
+    }
+    return DSF_OK;
+}
+
+int build_tiles(dsf_structure *s, bool by_type)
+{
+    const int n = s->n_atoms;
+    s->perm.resize(n);
+    std::iota(s->perm.begin(), s->perm.end(), 0);
+    if (by_type)
+        std::stable_sort(s->perm.begin(), s->perm.end(), [&](int x, int y) {
+            if (s->atom_type[x] != s->atom_type[y]) return s->atom_type[x] < s->atom_type[y];
+            return s->adpk[x] < s->adpk[y];
+        });
+    s->tile_begin.clear();
+    s->tile_ntypes.clear();
+    s->tile_types.clear();
+    std::vector<int> ltype(n);
+    int a = 0;
+    while (a < n) {
+        s->tile_begin.push_back(a);
+        std::vector<int> types;
+        int cnt = 0;
+        while (a < n && cnt < kTileAtoms) {
+            const int t = by_type ? s->atom_type[s->perm[a]] : 0;
+            auto it = std::find(types.begin(), types.end(), t);
+            int li;
+            if (it == types.end()) {
+                if ((int)types.size() == kMaxTileTypes) break;
+                types.push_back(t);
+                li = (int)types.size() - 1;
+            } else {
+                li = (int)(it - types.begin());
+            }
+            ltype[a] = li;
+            a++;
+            cnt++;
+        }
+        s->tile_ntypes.push_back((int)types.size());
+        for (int i = 0; i < kMaxTileTypes; i++) s->tile_types.push_back(i < (int)types.size() ? types[i] : 0);
+    }
+    s->tile_begin.push_back(n);
+    s->n_tiles = (int)s->tile_ntypes.size();
+    dsf_engine *e = s->eng;
+    int rc;
+    std::vector<int> adpk_sorted(n);
+    std::vector<double> mw_sorted(n);
+    std::vector<double> an_d(2 * (size_t)n);
+    std::vector<float> an_f(2 * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        const int o = s->perm[i];
+        adpk_sorted[i] = s->adpk[o];
+        mw_sorted[i] = s->mult_w[o];
+        an_d[2 * i] = s->anom[2 * o];
+        an_d[2 * i + 1] = s->anom[2 * o + 1];
+        an_f[2 * i] = (float)an_d[2 * i];
+        an_f[2 * i + 1] = (float)an_d[2 * i + 1];
+    }
+    if ((rc = upload(e, s->d_tile_begin, s->tile_begin.data(), s->tile_begin.size()))) return rc;
+    if ((rc = upload(e, s->d_tile_ntypes, s->tile_ntypes.data(), s->tile_ntypes.size()))) return rc;
+    if ((rc = upload(e, s->d_tile_types, s->tile_types.data(), s->tile_types.size()))) return rc;
+    if ((rc = upload(e, s->d_atom_ltype, ltype.data(), ltype.size()))) return rc;
+    if ((rc = upload(e, s->d_atom_adpk, adpk_sorted.data(), adpk_sorted.size()))) return rc;
+    if ((rc = upload(e, s->d_perm, s->perm.data(), s->perm.size()))) return rc;
+    if ((rc = upload(e, s->d_multw, mw_sorted.data(), mw_sorted.size()))) return rc;
+    if ((rc = upload(e, s->d_anom_d, an_d.data(), an_d.size()))) return rc;
+    if ((rc = upload(e, s->d_anom_f, an_f.data(), an_f.size()))) return rc;
+    s->active_host.assign(n, 1);
+    if ((rc = upload(e, s->d_active, s->active_host.data(), s->active_host.size()))) return rc;
+    // per-atom buffers
+    DSF_CUDA(s->d_xq.alloc(12 * (size_t)n));
+    DSF_CUDA(s->d_xlo.alloc(12 * (size_t)n));
+    DSF_CUDA(s->d_xd.alloc(24 * (size_t)n));
+    DSF_CUDA(s->d_adp_f.alloc(24 * (size_t)n));
+    DSF_CUDA(s->d_adp_d.alloc(48 * (size_t)n));
+    DSF_CUDA(s->d_w_f.alloc(4 * (size_t)n));
+    DSF_CUDA(s->d_w_d.alloc(8 * (size_t)n));
+    DSF_CUDA(s->d_raw.alloc(80 * (size_t)n));
+    DSF_CUDA(s->d_gacc.alloc(sizeof(double) * kNch * (size_t)n));
+    return DSF_OK;
+}
+
+void refresh_dev(dsf_structure *s)
+{
+    DevStructure &d = s->dev;
+    d.model = s->model;
+    d.n_atoms = s->n_atoms;
+    d.n_hkl = s->n_hkl;
+    d.n_sym = s->n_sym;
+    d.n_tiles = s->n_tiles;
+    d.n_types = s->n_types;
+    std::copy(s->B, s->B + 9, d.B);
+    d.sym_rot = s->d_sym_rot.as<int>();
+    d.sym_t24 = s->d_sym_t24.as<int>();
+    d.tile_begin = s->d_tile_begin.as<int>();
+    d.tile_ntypes = s->d_tile_ntypes.as<int>();
+    d.tile_types = s->d_tile_types.as<int>();
+    d.atom_ltype = s->d_atom_ltype.as<int>();
+    d.atom_adpk = s->d_atom_adpk.as<int>();
+    d.atom_active = s->d_active.as<uint8_t>();
+    d.atom_xq = s->d_xq.as<uint32_t>();
+    d.atom_xlo = s->d_xlo.as<float>();
+    d.atom_xd = s->d_xd.as<double>();
+    d.atom_adp_f = s->d_adp_f.as<float>();
+    d.atom_adp_d = s->d_adp_d.as<double>();
+    d.atom_w_f = s->d_w_f.as<float>();
+    d.atom_w_d = s->d_w_d.as<double>();
+    d.atom_anom_f = s->d_anom_f.as<float2>();
+    d.atom_anom_d = s->d_anom_d.as<double2>();
+    d.atom_pg_f = s->d_pg_f.as<float>();
+    d.atom_pg_d = s->d_pg_d.as<double>();
+    d.types = s->d_types.as<TypeRadial>();
+    d.term_coeff = s->d_tcoeff.as<double>();
+    d.term_exp = s->d_texp.as<double>();
+    d.term_pow = s->d_tpow.as<int>();
+    d.hkl = s->d_hkl.as<int4>();
+    d.h2 = s->d_h2.as<double>();
+    d.table_f = s->d_table_f.as<float2>();
+    d.table_d = s->d_table_d.as<double2>();
+    d.atom_orig = s->d_perm.as<int>();
+    d.atom_plm_lmax = s->d_plm_lmax.as<int>();
+}
+
+int common_atoms(dsf_engine *e, dsf_structure *s, const dsf_atoms *at)
+{
+    if (!at || at->n_atoms < 1) return fail(e, DSF_ERR_ARGUMENT, "structure needs at least one atom");
+    const int n = at->n_atoms;
+    s->n_atoms = n;
+    s->xyz_conv = at->xyz_convention;
+    s->adp_conv = at->adp_convention;
+    if (s->xyz_conv < 0 || s->xyz_conv > 1) return fail(e, DSF_ERR_ARGUMENT, "bad xyz convention");
+    if (s->adp_conv < 0 || s->adp_conv > 2) return fail(e, DSF_ERR_ARGUMENT, "bad ADP convention");
+    s->adpk.resize(n);
+    s->mult_w.resize(n);
+    s->anom.assign(2 * (size_t)n, 0.0);
+    s->atom_type.assign(n, 0);
+    s->atom_wfn.assign(n, 0);
+    for (int i = 0; i < n; i++) {
+        const int k = at->adp_components ? at->adp_components[i] : 1;
+        if (k != 0 && k != 1 && k != 6) return fail(e, DSF_ERR_ARGUMENT, "adp_components must be 0, 1 or 6");
+        s->adpk[i] = k;
+        s->mult_w[i] = (at->multiplicity ? at->multiplicity[i] : (double)s->n_total) / (double)s->n_total;
+        if (at->atom_type) s->atom_type[i] = at->atom_type[i];
+        if (at->atom_wfn) s->atom_wfn[i] = at->atom_wfn[i];
+        if (at->anomalous) {
+            s->anom[2 * i] = at->anomalous[2 * i];
+            s->anom[2 * i + 1] = at->anomalous[2 * i + 1];
+        }
+    }
+    // U_param -> U*_param (the kernel's beta basis without 2 pi^2)
+    double A[9];
+    const double lam[3] = {std::sqrt(s->B[0] * s->B[0] + s->B[3] * s->B[3] + s->B[6] * s->B[6]),
+                           std::sqrt(s->B[1] * s->B[1] + s->B[4] * s->B[4] + s->B[7] * s->B[7]),
+                           std::sqrt(s->B[2] * s->B[2] + s->B[5] * s->B[5] + s->B[8] * s->B[8])};
+    if (s->adp_conv == DSF_ADP_U_CIF) {
+        for (int i = 0; i < 9; i++) A[i] = 0;
+        for (int i = 0; i < 3; i++) A[4 * i] = lam[i];
+    } else if (s->adp_conv == DSF_ADP_U_CART) {
+        std::copy(s->Minv, s->Minv + 9, A);  // U* = M^-1 U_cart M^-T
+    } else {
+        for (int i = 0; i < 9; i++) A[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    }
+    adp_param_map(A, s->A6);
+    return DSF_OK;
+}
+
+int finish_create(dsf_engine *e, dsf_structure *s)
+{
+    int rc;
+    if ((rc = upload(e, s->d_sym_rot, s->sym_rot.data(), s->sym_rot.size()))) return rc;
+    if ((rc = upload(e, s->d_sym_t24, s->sym_t24.data(), s->sym_t24.size()))) return rc;
+    if ((rc = upload(e, s->d_types, s->trad.data(), s->trad.size()))) return rc;
+    refresh_dev(s);
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    return DSF_OK;
+}
+
+}  // namespace
+
+// ==========================================================================
+// C ABI
+// ==========================================================================
+extern "C" {
+
+int dsf_abi_version(void) { return DSF_ABI_VERSION; }
+
+int dsf_engine_create(int device, dsf_engine **out)
+{
+    if (!out) return DSF_ERR_ARGUMENT;
+    *out = nullptr;
+    dsf_engine *e = new dsf_engine();
+    e->device = device;
+    cudaError_t ce = cudaSetDevice(device);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        delete e;
+        return DSF_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, device);
+    int smem = 0;
+    cudaDeviceGetAttribute(&smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    e->max_smem = (size_t)smem;
+    *out = e;
+    return DSF_OK;
+}
+
+int dsf_engine_destroy(dsf_engine *e)
+{
+    if (!e) return DSF_ERR_ARGUMENT;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return DSF_OK;
+}
+
+const char *dsf_last_error(const dsf_engine *e) { return e ? e->err.c_str() : "null engine"; }
+
+static int create_common(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms, int model,
+                         dsf_structure **out, dsf_structure **sp)
+{
+    if (!e || !out) return DSF_ERR_ARGUMENT;
+    *out = nullptr;
+    cudaSetDevice(e->device);
+    dsf_structure *s = new dsf_structure();
+    s->eng = e;
+    s->model = model;
+    int rc = sym_from_desc(e, s, sym);
+    if (!rc) rc = common_atoms(e, s, atoms);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *sp = s;
+    return DSF_OK;
+}
+
+int dsf_structure_create_hc(dsf_engine *e, const dsf_symmetry *sym, const dsf_hc_model *m, const dsf_atoms *atoms,
+                            dsf_structure **out)
+{
+    dsf_structure *s = nullptr;
+    int rc = create_common(e, sym, atoms, MODEL_HC, out, &s);
+    if (rc) return rc;
+    auto bail = [&](int code) { delete s; return code; };
+    if (!m || m->n_wfn < 1 || m->n_types < 1) return bail(fail(e, DSF_ERR_ARGUMENT, "HC model needs wavefunctions and types"));
+    if (!atoms->lcs) return bail(fail(e, DSF_ERR_ARGUMENT, "HC model needs local coordinate systems"));
+    s->n_wfn = m->n_wfn;
+    s->n_types = m->n_types;
+    for (int i = 0; i < s->n_atoms; i++) {
+        if (s->atom_type[i] < 0 || s->atom_type[i] >= m->n_types) return bail(fail(e, DSF_ERR_ARGUMENT, "atom type index out of range"));
+        if (s->atom_wfn[i] < 0 || s->atom_wfn[i] >= m->n_wfn) return bail(fail(e, DSF_ERR_ARGUMENT, "atom wavefunction index out of range"));
+        if (!atoms->anomalous) {
+            s->anom[2 * i] = m->anomalous ? m->anomalous[2 * s->atom_wfn[i]] : 0.0;
+            s->anom[2 * i + 1] = m->anomalous ? m->anomalous[2 * s->atom_wfn[i] + 1] : 0.0;
+        }
+    }
+    s->lcs.assign(atoms->lcs, atoms->lcs + 9 * (size_t)s->n_atoms);
+    s->type_nl.assign(m->type_nl, m->type_nl + m->n_types);
+    s->type_plm.assign(m->type_plm, m->type_plm + 25 * (size_t)m->n_types);
+    s->type_pval.assign(m->type_pval, m->type_pval + m->n_types);
+    s->type_kappa.assign(m->type_kappa, m->type_kappa + m->n_types);
+    s->type_kappa_p.assign(m->type_kappa_prime, m->type_kappa_prime + m->n_types);
+    // type -> wavefunction: that of the atoms using the type (unused types keep wavefunction 0)
+    s->type_wfn.assign(m->n_types, 0);
+    for (int i = 0; i < s->n_atoms; i++) s->type_wfn[s->atom_type[i]] = s->atom_wfn[i];
+    // concatenated density terms: core of all wfns then valence of all wfns
+    const int ncore = m->core_offset[m->n_wfn], nval = m->val_offset[m->n_wfn];
+    s->tcoeff.clear(); s->texp.clear(); s->tpow.clear();
+    for (int q = 0; q < ncore; q++) { s->tcoeff.push_back(m->core_coeff[q]); s->texp.push_back(m->core_exp[q]); s->tpow.push_back(m->core_pow[q]); }
+    for (int q = 0; q < nval; q++) { s->tcoeff.push_back(m->val_coeff[q]); s->texp.push_back(m->val_exp[q]); s->tpow.push_back(m->val_pow[q]); }
+    for (size_t q = 0; q < s->tpow.size(); q++)
+        if (s->tpow[q] < 0 || s->tpow[q] > 8) return bail(fail(e, DSF_ERR_ARGUMENT, "density term r powers must be in 0..8"));
+    if ((rc = build_type_radial(s, m))) return bail(rc);
+    // val ranges point behind the core terms
+    for (int t = 0; t < s->n_types; t++) {
+        const int w = s->type_wfn[t];
+        s->trad[t].val_begin = ncore + m->val_offset[w];
+        s->trad[t].val_end = ncore + m->val_offset[w + 1];
+    }
+    if ((rc = upload(e, s->d_tcoeff, s->tcoeff.data(), s->tcoeff.size()))) return bail(rc);
+    if ((rc = upload(e, s->d_texp, s->texp.data(), s->texp.size()))) return bail(rc);
+    if ((rc = upload(e, s->d_tpow, s->tpow.data(), s->tpow.size()))) return bail(rc);
+    if ((rc = build_tiles(s, true))) return bail(rc);
+    if ((rc = compute_global_plm(s))) return bail(rc);
+    if ((rc = finish_create(e, s))) return bail(rc);
+    *out = s;
+    return DSF_OK;
+}
+
+int dsf_structure_create_iam(dsf_engine *e, const dsf_symmetry *sym, const dsf_iam_model *m, const dsf_atoms *atoms,
+                             dsf_structure **out)
+{
+    dsf_structure *s = nullptr;
+    int rc = create_common(e, sym, atoms, MODEL_IAM, out, &s);
+    if (rc) return rc;
+    auto bail = [&](int code) { delete s; return code; };
+    if (!m || m->n_types < 1) return bail(fail(e, DSF_ERR_ARGUMENT, "IAM model needs types"));
+    s->n_types = m->n_types;
+    s->trad.assign(m->n_types, TypeRadial{});
+    for (int t = 0; t < m->n_types; t++) {
+        TypeRadial &r = s->trad[t];
+        r.lmax_used = -1;
+        r.iam_n = m->n_gauss[t];
+        if (r.iam_n < 0 || r.iam_n > 5) return bail(fail(e, DSF_ERR_ARGUMENT, "at most 5 Gaussians per IAM type"));
+        for (int q = 0; q < r.iam_n; q++) { r.iam_a[q] = m->a[5 * t + q]; r.iam_b[q] = m->b[5 * t + q]; }
+        r.iam_c = m->c[t];
+    }
+    for (int i = 0; i < s->n_atoms; i++)
+        if (s->atom_type[i] < 0 || s->atom_type[i] >= m->n_types) return bail(fail(e, DSF_ERR_ARGUMENT, "atom type index out of range"));
+    if ((rc = build_tiles(s, true))) return bail(rc);
+    std::vector<double> z(25 * (size_t)s->n_atoms, 0.0);
+    std::vector<float> zf(25 * (size_t)s->n_atoms, 0.0f);
+    if ((rc = upload(e, s->d_pg_d, z.data(), z.size()))) return bail(rc);
+    if ((rc = upload(e, s->d_pg_f, zf.data(), zf.size()))) return bail(rc);
+    s->dmat.assign(165 * (size_t)s->n_atoms, 0.0);
+    if ((rc = upload(e, s->d_dmat, s->dmat.data(), s->dmat.size()))) return bail(rc);
+    {
+        std::vector<int> lmx(s->n_atoms, -1);
+        if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return bail(rc);
+    }
+    if ((rc = finish_create(e, s))) return bail(rc);
+    *out = s;
+    return DSF_OK;
+}
+
+int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl);
+
+int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms, int n_hkl,
+                                   const int *hkl, const double *table, int table_fp32, dsf_structure **out)
+{
+    dsf_structure *s = nullptr;
+    int rc = create_common(e, sym, atoms, MODEL_TABLE, out, &s);
+    if (rc) return rc;
+    auto bail = [&](int code) { delete s; return code; };
+    if (!table || n_hkl < 1) return bail(fail(e, DSF_ERR_ARGUMENT, "tabulated model needs a table and reflections"));
+    s->n_types = 1;
+    s->trad.assign(1, TypeRadial{});
+    s->trad[0].lmax_used = -1;
+    if ((rc = build_tiles(s, false))) return bail(rc);
+    std::vector<double> z(25 * (size_t)s->n_atoms, 0.0);
+    std::vector<float> zf(25 * (size_t)s->n_atoms, 0.0f);
+    if ((rc = upload(e, s->d_pg_d, z.data(), z.size()))) return bail(rc);
+    if ((rc = upload(e, s->d_pg_f, zf.data(), zf.size()))) return bail(rc);
+    s->dmat.assign(165 * (size_t)s->n_atoms, 0.0);
+    if ((rc = upload(e, s->d_dmat, s->dmat.data(), s->dmat.size()))) return bail(rc);
+    {
+        std::vector<int> lmx(s->n_atoms, -1);
+        if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return bail(rc);
+    }
+    const size_t nel = (size_t)n_hkl * s->n_sym * s->n_atoms;
+    if (table_fp32) {
+        std::vector<float> tf(2 * nel);
+        for (size_t i = 0; i < 2 * nel; i++) tf[i] = (float)table[i];
+        if ((rc = upload(e, s->d_table_f, tf.data(), tf.size()))) return bail(rc);
+    } else {
+        if ((rc = upload(e, s->d_table_d, table, 2 * nel))) return bail(rc);
+        std::vector<float> tf(2 * nel);
+        for (size_t i = 0; i < 2 * nel; i++) tf[i] = (float)table[i];
+        if ((rc = upload(e, s->d_table_f, tf.data(), tf.size()))) return bail(rc);
+    }
+    if ((rc = finish_create(e, s))) return bail(rc);
+    if ((rc = dsf_structure_set_hkl(s, n_hkl, hkl))) return bail(rc);
+    *out = s;
+    return DSF_OK;
+}
+
+int dsf_structure_destroy(dsf_structure *s)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    cudaSetDevice(s->eng->device);
+    cudaStreamSynchronize(s->eng->stream);
+    DevBuf *bufs[] = {&s->d_sym_rot, &s->d_sym_t24, &s->d_tile_begin, &s->d_tile_ntypes, &s->d_tile_types,
+                      &s->d_atom_ltype, &s->d_atom_adpk, &s->d_active, &s->d_xq, &s->d_xlo, &s->d_xd, &s->d_adp_f,
+                      &s->d_adp_d, &s->d_w_f, &s->d_w_d, &s->d_anom_f, &s->d_anom_d, &s->d_pg_f, &s->d_pg_d,
+                      &s->d_types, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_hkl, &s->d_h2, &s->d_hmult,
+                      &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw, &s->d_dmat, &s->d_raw,
+                      &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc, &s->d_out, &s->d_plm_lmax};
+    for (DevBuf *b : bufs) b->release();
+    delete s;
+    return DSF_OK;
+}
+
+int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (n_hkl < 1 || !hkl) return fail(e, DSF_ERR_ARGUMENT, "need at least one reflection");
+    if (s->model == MODEL_TABLE && s->have_hkl && n_hkl != s->n_hkl)
+        return fail(e, DSF_ERR_ARGUMENT, "tabulated structures keep the reflection set of their table");
+    cudaSetDevice(e->device);
+    std::vector<int4> h4(n_hkl);
+    std::vector<double> h2(n_hkl), mult(n_hkl), cinv(2 * (size_t)n_hkl);
+    for (int i = 0; i < n_hkl; i++) {
+        const int h = hkl[3 * i], k = hkl[3 * i + 1], l = hkl[3 * i + 2];
+        h4[i] = make_int4(h, k, l, 0);
+        double c[3];
+        for (int j = 0; j < 3; j++) c[j] = s->B[3 * j] * h + s->B[3 * j + 1] * k + s->B[3 * j + 2] * l;
+        h2[i] = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
+        mult[i] = centering_multiplier(s->centering, s->obverse, h, k, l);
+        int r = (h * s->t_inv24[0] + k * s->t_inv24[1] + l * s->t_inv24[2]) % 24;
+        if (r < 0) r += 24;
+        cinv[2 * i] = std::cos(2.0 * DSF_PI * r / 24.0);
+        cinv[2 * i + 1] = std::sin(2.0 * DSF_PI * r / 24.0);
+        if (r % 6 == 0) {  // exact values at quarter turns
+            const int q = r / 6;
+            cinv[2 * i] = q == 0 ? 1.0 : q == 2 ? -1.0 : 0.0;
+            cinv[2 * i + 1] = q == 1 ? 1.0 : q == 3 ? -1.0 : 0.0;
+        }
+    }
+    int rc;
+    if ((rc = upload(e, s->d_hkl, h4.data(), h4.size()))) return rc;
+    if ((rc = upload(e, s->d_h2, h2.data(), h2.size()))) return rc;
+    if ((rc = upload(e, s->d_hmult, mult.data(), mult.size()))) return rc;
+    if ((rc = upload(e, s->d_cinv, cinv.data(), cinv.size()))) return rc;
+    DSF_CUDA(s->d_dtdf.alloc(16 * (size_t)n_hkl));
+    DSF_CUDA(s->d_gw_d.alloc(16 * (size_t)n_hkl));
+    DSF_CUDA(s->d_gw_f.alloc(8 * (size_t)n_hkl));
+    DSF_CUDA(s->d_facc.alloc(16 * (size_t)n_hkl));
+    s->n_hkl = n_hkl;
+    s->have_hkl = true;
+    refresh_dev(s);
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    return DSF_OK;
+}
+
+int dsf_structure_update_atoms(dsf_structure *s, const double *xyz, const double *adp, const double *occ)
+{
+    if (!s || !xyz || !occ) return s ? fail(s->eng, DSF_ERR_ARGUMENT, "xyz and occupancy are required") : DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    cudaSetDevice(e->device);
+    const int n = s->n_atoms;
+    std::vector<double> raw(10 * (size_t)n, 0.0);
+    for (int i = 0; i < n; i++) {
+        for (int j = 0; j < 3; j++) {
+            raw[10 * i + j] = xyz[3 * i + j];
+            if (!std::isfinite(xyz[3 * i + j])) return fail(e, DSF_ERR_ARGUMENT, "non-finite coordinate");
+        }
+        if (adp)
+            for (int j = 0; j < s->adpk[i]; j++) raw[10 * i + 3 + j] = adp[6 * i + j];
+        raw[10 * i + 9] = occ[i];
+    }
+    DSF_CUDA(cudaMemcpyAsync(s->d_raw.p, raw.data(), raw.size() * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    AtomParams P;
+    P.n_atoms = n;
+    P.xyz_conv = s->xyz_conv;
+    std::copy(s->Minv, s->Minv + 9, P.Minv);
+    std::copy(s->A6, s->A6 + 36, P.A6);
+    atom_convert_kernel<<<(n + 127) / 128, 128, 0, e->stream>>>(
+        P, s->d_raw.as<double>(), s->d_perm.as<int>(), s->d_atom_adpk.as<int>(), s->d_multw.as<double>(),
+        s->d_xq.as<uint32_t>(), s->d_xlo.as<float>(), s->d_xd.as<double>(), s->d_adp_f.as<float>(),
+        s->d_adp_d.as<double>(), s->d_w_f.as<float>(), s->d_w_d.as<double>());
+    DSF_CUDA(cudaGetLastError());
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    s->have_atoms = true;
+    return DSF_OK;
+}
+
+int dsf_structure_update_types(dsf_structure *s, const double *plm, const double *pval, const double *kappa,
+                               const double *kappa_p)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (s->model != MODEL_HC) return fail(e, DSF_ERR_STATE, "multipole parameters exist only for HC structures");
+    cudaSetDevice(e->device);
+    const int nT = s->n_types;
+    if (plm) s->type_plm.assign(plm, plm + 25 * (size_t)nT);
+    if (pval) s->type_pval.assign(pval, pval + nT);
+    if (kappa) s->type_kappa.assign(kappa, kappa + nT);
+    if (kappa_p) s->type_kappa_p.assign(kappa_p, kappa_p + nT);
+    for (int t = 0; t < nT; t++) {
+        TypeRadial &r = s->trad[t];
+        r.pv = s->type_pval[t];
+        r.kappa = s->type_kappa[t];
+        r.kappa_p = s->type_kappa_p[t];
+        int lp = -1;
+        for (int l = 0; l < s->type_nl[t] && l <= 4; l++)
+            for (int q = 0; q < 2 * l + 1; q++)
+                if (s->type_plm[25 * (size_t)t + l * l + q] != 0.0) lp = l;
+        r.lmax_used = std::min(lp, std::min(4, r.n_def - 1));
+    }
+    int rc;
+    if ((rc = upload(e, s->d_types, s->trad.data(), s->trad.size()))) return rc;
+    if (plm && (rc = compute_global_plm(s))) return rc;
+    refresh_dev(s);
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    return DSF_OK;
+}
+
+int dsf_structure_set_lcs(dsf_structure *s, const double *lcs)
+{
+    if (!s || !lcs) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (s->model != MODEL_HC) return fail(e, DSF_ERR_STATE, "local coordinate systems exist only for HC structures");
+    cudaSetDevice(e->device);
+    s->lcs.assign(lcs, lcs + 9 * (size_t)s->n_atoms);
+    int rc = compute_global_plm(s);
+    if (rc) return rc;
+    refresh_dev(s);
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    return DSF_OK;
+}
+
+int64_t dsf_structure_device_bytes(const dsf_structure *s)
+{
+    if (!s) return 0;
+    const DevBuf *bufs[] = {&s->d_sym_rot, &s->d_sym_t24, &s->d_tile_begin, &s->d_tile_ntypes, &s->d_tile_types,
+                            &s->d_atom_ltype, &s->d_atom_adpk, &s->d_active, &s->d_xq, &s->d_xlo, &s->d_xd,
+                            &s->d_adp_f, &s->d_adp_d, &s->d_w_f, &s->d_w_d, &s->d_anom_f, &s->d_anom_d, &s->d_pg_f,
+                            &s->d_pg_d, &s->d_types, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_hkl, &s->d_h2,
+                            &s->d_hmult, &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw,
+                            &s->d_dmat, &s->d_raw, &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc,
+                            &s->d_out, &s->d_plm_lmax};
+    int64_t b = 0;
+    for (const DevBuf *p : bufs) b += (int64_t)p->bytes;
+    return b;
+}
+
+int dsf_last_launch_count(const dsf_structure *s) { return s ? s->last_launches : 0; }
+
+int dsf_calculate_device(dsf_structure *s, int precision, int flags, const double *dtdf_device,
+                         const dsf_outputs *out, void *stream)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (!s->have_hkl) return fail(e, DSF_ERR_STATE, "no reflections set");
+    if (!s->have_atoms) return fail(e, DSF_ERR_STATE, "atomic parameters not uploaded");
+    if (!out || !out->f || !dtdf_device) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
+    if (precision != DSF_FP64 && precision != DSF_FP32_BULK) return fail(e, DSF_ERR_ARGUMENT, "unknown precision");
+    cudaSetDevice(e->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    const bool fp64 = precision == DSF_FP64;
+    const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
+    const int n_hkl = s->n_hkl, n = s->n_atoms;
+    int launches = 0;
+    gw_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, reinterpret_cast<const double2 *>(dtdf_device),
+                                                   s->d_hmult.as<double>(), s->d_cinv.as<double2>(), s->centro_mode,
+                                                   s->d_gw_d.as<double2>(), s->d_gw_f.as<float2>());
+    launches++;
+    DSF_CUDA(cudaGetLastError());
+    DSF_CUDA(cudaMemsetAsync(s->d_facc.p, 0, 16 * (size_t)n_hkl, st));
+    DSF_CUDA(cudaMemsetAsync(s->d_gacc.p, 0, sizeof(double) * kNch * (size_t)n, st));
+    // launch shape: reflections per sub-tile from the shared-memory budget,
+    // reflection chunks so the grid covers the SMs several times
+    int ht = kMaxHT;
+    while (ht > 2 && sf_grad_smem_bytes(fp64, ht, s->n_sym) > std::min<size_t>(e->max_smem, 110 * 1024)) ht /= 2;
+    const int target = std::max(1, e->n_sm) * 8;
+    int n_chunks = std::max(1, target / std::max(1, s->n_tiles));
+    int chunk = (n_hkl + n_chunks - 1) / n_chunks;
+    chunk = std::max(chunk, 4 * ht);
+    chunk = (chunk + ht - 1) / ht * ht;
+    CallBuffers C;
+    C.gw_d = s->d_gw_d.as<double2>();
+    C.gw_f = s->d_gw_f.as<float2>();
+    C.f_acc = s->d_facc.as<double2>();
+    C.g_acc = s->d_gacc.as<double>();
+    DSF_CUDA(launch_sf_grad(s->dev, C, fp64, mp, chunk, ht, st));
+    launches++;
+    f_epilogue_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, s->d_facc.as<double2>(), s->d_hmult.as<double>(),
+                                                           s->d_cinv.as<double2>(), s->centro_mode, out->f);
+    launches++;
+    DSF_CUDA(cudaGetLastError());
+    if (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) {
+        GradParams P;
+        P.n_atoms = n;
+        P.xyz_conv = s->xyz_conv;
+        std::copy(s->Minv, s->Minv + 9, P.Minv);
+        std::copy(s->A6, s->A6 + 36, P.A6);
+        P.want_xyz = (flags & DSF_D_XYZ) != 0;
+        P.want_adp = (flags & DSF_D_ADP) != 0;
+        P.want_occ = (flags & DSF_D_OCC) != 0;
+        P.want_mp = mp;
+        grad_epilogue_kernel<<<(n + 127) / 128, 128, 0, st>>>(
+            P, s->d_gacc.as<double>(), s->d_perm.as<int>(), s->d_atom_adpk.as<int>(), s->d_w_d.as<double>(),
+            s->d_multw.as<double>(), s->d_dmat.as<double>(), s->d_plm_lmax.as<int>(), out->d_xyz, out->d_adp, out->d_occ, out->d_pval,
+            out->d_plm, out->d_kappa, out->d_kappa_prime);
+        launches++;
+        DSF_CUDA(cudaGetLastError());
+    }
+    s->last_launches = launches;
+    return DSF_OK;
+}
+
+int dsf_calculate(dsf_structure *s, int precision, int flags, const double *dtdf, const int *include,
+                  const dsf_outputs *out)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (!out || !out->f || !dtdf) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
+    if (!s->have_hkl) return fail(e, DSF_ERR_STATE, "no reflections set");
+    cudaSetDevice(e->device);
+    const int n_hkl = s->n_hkl, n = s->n_atoms;
+    // inclusion mask (countAtomContribution)
+    bool changed = false;
+    for (int a = 0; a < n; a++) {
+        const uint8_t v = include ? (include[s->perm[a]] != 0) : 1;
+        if (v != s->active_host[a]) { s->active_host[a] = v; changed = true; }
+    }
+    if (changed)
+        DSF_CUDA(cudaMemcpyAsync(s->d_active.p, s->active_host.data(), n, cudaMemcpyHostToDevice, e->stream));
+    // device output block: f, xyz, adp, occ, pval, plm, kappa, kappa'
+    const size_t nf = 2 * (size_t)n_hkl, per_atom = 3 + 6 + 1 + 1 + 25 + 1 + 1;
+    DSF_CUDA(s->d_out.alloc(sizeof(double) * (nf + per_atom * (size_t)n)));
+    double *base = s->d_out.as<double>();
+    dsf_outputs d;
+    d.f = base;
+    d.d_xyz = base + nf;
+    d.d_adp = d.d_xyz + 3 * (size_t)n;
+    d.d_occ = d.d_adp + 6 * (size_t)n;
+    d.d_pval = d.d_occ + n;
+    d.d_plm = d.d_pval + n;
+    d.d_kappa = d.d_plm + 25 * (size_t)n;
+    d.d_kappa_prime = d.d_kappa + n;
+    DSF_CUDA(cudaMemcpyAsync(s->d_dtdf.p, dtdf, 16 * (size_t)n_hkl, cudaMemcpyHostToDevice, e->stream));
+    int rc = dsf_calculate_device(s, precision, flags, s->d_dtdf.as<double>(), &d, e->stream);
+    if (rc) return rc;
+    DSF_CUDA(cudaMemcpyAsync(out->f, d.f, 8 * nf, cudaMemcpyDeviceToHost, e->stream));
+    struct { double *dst; double *src; size_t n; } cp[] = {
+        {out->d_xyz, d.d_xyz, 3 * (size_t)n}, {out->d_adp, d.d_adp, 6 * (size_t)n}, {out->d_occ, d.d_occ, (size_t)n},
+        {out->d_pval, d.d_pval, (size_t)n}, {out->d_plm, d.d_plm, 25 * (size_t)n}, {out->d_kappa, d.d_kappa, (size_t)n},
+        {out->d_kappa_prime, d.d_kappa_prime, (size_t)n}};
+    for (auto &c : cp)
+        if (c.dst) DSF_CUDA(cudaMemcpyAsync(c.dst, c.src, 8 * c.n, cudaMemcpyDeviceToHost, e->stream));
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    return DSF_OK;
+}
+
+}  // extern "C"

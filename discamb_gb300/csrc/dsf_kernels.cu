@@ -1,0 +1,456 @@
+// Fused structure-factor + adjoint kernel for sm_103a.
+//
+// One block owns one tile of up to 128 atoms (one atom per thread, atoms
+// sorted by type so a tile holds few types) and a contiguous chunk of
+// reflections.  Reflections are staged in shared memory in sub-tiles: per
+// (reflection, symmetry operation) the rotated index h' = R^T h, the phase
+// offset h.t and the 25 harmonics d_lm(h'/|h'|); per (reflection, type of the
+// tile) the spherical form factor and the radial Fourier-Bessel terms of the
+// deformation density.  Each thread then runs the sum over operations for
+// its atom, reduces the per-reflection partial F across the block with warp
+// shuffles and keeps its own derivative sums in registers.  Cross-block
+// accumulation is in FP64 (atomics on F per reflection and on the per-atom
+// derivative channels).
+//
+// Reference loop restated: HansenCoppens_SF_Engine3::calculateSF_Serial*
+// (src/Scattering/HansenCoppens_SF_Engine3.cpp:1030-1509, 1511-1992,
+// 2649-2894) and AnyScattererStructureFactorCalculator::calculateStructure
+// FactorsAndDerivatives (src/Scattering/AnyScattererStructureFactor
+// Calculator.cpp:614-829).
+//
+// R = double: the plain form, FP64 throughout.
+// R = float : the FP32-bulk form.  Phases are reduced exactly in integer
+// arithmetic (fractional coordinates as 2^32 fixed point, integer h', h.t
+// from integer translations in 1/12) so no FP64 is needed per term; F and
+// derivative sums over blocks are FP64, and each thread folds its FP32
+// derivative sums into FP64 registers after every sub-tile of reflections.
+#include "dsf_device.cuh"
+#include "dsf_math.cuh"
+
+namespace dsf {
+
+template <typename R>
+struct Vec2;
+template <>
+struct Vec2<float> { using T = float2; };
+template <>
+struct Vec2<double> { using T = double2; };
+
+template <typename R>
+__device__ __forceinline__ void sincos2pi(R phase, R *s, R *c);
+template <>
+__device__ __forceinline__ void sincos2pi<float>(float phase, float *s, float *c)
+{
+    __sincosf(6.283185307179586f * phase, s, c);
+}
+template <>
+__device__ __forceinline__ void sincos2pi<double>(double phase, double *s, double *c)
+{
+    sincospi(2.0 * phase, s, c);
+}
+
+template <typename R>
+__device__ __forceinline__ R exp_(R x);
+template <>
+__device__ __forceinline__ float exp_<float>(float x) { return __expf(x); }
+template <>
+__device__ __forceinline__ double exp_<double>(double x) { return exp(x); }
+
+template <typename R>
+__device__ __forceinline__ R shfl_xor(R v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+
+// radial terms of one (reflection, type): out[0] = spherical f (core + Pv*val
+// or the Gaussian f0), out[1..5] = signed 4 pi N_l g_l  (signs of i^l folded:
+// +,+,-,-,+ for real/imag bookkeeping), out[6] = f_val, out[7] = Pv * df_val/dkappa,
+// out[8..12] = signed 4 pi N_l dg_l/dkappa'
+template <typename R>
+__device__ void radial_terms(const DevStructure &S, const TypeRadial &t, int model, double h2, R *out, bool mp)
+{
+    const R hl = R(sqrt(h2));
+    const R K = R(2.0 * DSF_PI) * hl;
+    for (int q = 0; q < 13; q++) out[q] = R(0);
+    if (model == MODEL_IAM) {
+        R s = R(t.iam_c);
+        const R x2 = R(h2 * 0.25);
+        for (int q = 0; q < t.iam_n; q++) s += R(t.iam_a[q]) * exp_<R>(-R(t.iam_b[q]) * x2);
+        out[0] = s;
+        return;
+    }
+    if (model != MODEL_HC) return;
+    R fc = R(0);
+    for (int q = t.core_begin; q < t.core_end; q++)
+        fc += R(S.term_coeff[q]) * gfun<R>(0, S.term_pow[q] + 2, K, R(S.term_exp[q]));
+    const R kap = R(t.kappa), kp = R(t.kappa_p);
+    const R Kv = K / kap, Kd = K / kp;
+    R fv = R(0), dfv = R(0);
+    for (int q = t.val_begin; q < t.val_end; q++) {
+        fv += R(S.term_coeff[q]) * gfun<R>(0, S.term_pow[q] + 2, Kv, R(S.term_exp[q]));
+        if (mp) dfv += R(S.term_coeff[q]) * gfun_dk<R>(0, S.term_pow[q] + 2, Kv, R(S.term_exp[q]));
+    }
+    const R fourpi = R(4.0 * DSF_PI);
+    out[0] = fourpi * (fc + R(t.pv) * fv);
+    out[6] = fourpi * fv;
+    out[7] = fourpi * R(t.pv) * dfv * (-Kv / kap);
+    const R zeta = R(t.zeta);
+    for (int l = 0; l < 5; l++) {
+        if (l < t.n_def) {
+            const R sgn = (l == 2 || l == 3) ? R(-1) : R(1);
+            out[1 + l] = sgn * fourpi * R(t.norm[l]) * gfun<R>(l, t.npow[l] + 2, Kd, zeta);
+            if (mp) out[8 + l] = sgn * fourpi * R(t.norm[l]) * gfun_dk<R>(l, t.npow[l] + 2, Kd, zeta) * (-Kd / kp);
+        }
+    }
+}
+
+template <typename R, bool MP>
+__global__ void __launch_bounds__(kTileAtoms)
+sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
+{
+    using R2 = typename Vec2<R>::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nS = S.n_sym;
+    const int tile = blockIdx.x;
+    const int chunk = blockIdx.y;
+    const int h_begin = chunk * hkl_chunk;
+    const int h_end = min(S.n_hkl, h_begin + hkl_chunk);
+    if (h_begin >= h_end) return;
+    const int a_begin = S.tile_begin[tile], a_end = S.tile_begin[tile + 1];
+    const int nT = S.tile_ntypes[tile];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kWarps = kTileAtoms / 32;
+    constexpr int kRad = 13;
+
+    // shared memory carve-up
+    R *sY = reinterpret_cast<R *>(smem_raw);                      // [ht][nS][25]
+    R *sRad = sY + (size_t)ht * nS * 25;                           // [ht][nT][kRad]
+    R *sHp = sRad + (size_t)ht * kMaxTileTypes * kRad;            // [ht][nS][3] (as R)
+    R2 *sG = reinterpret_cast<R2 *>(sHp + (size_t)ht * nS * 3);   // [ht]
+    R2 *sF = sG + ht;                                              // [kWarps][ht]
+    R *sH2 = reinterpret_cast<R *>(sF + kWarps * ht);             // [ht]
+    uint32_t *sTq = reinterpret_cast<uint32_t *>(sH2 + ht);       // [ht][nS] phase offset (FP32 path)
+    double *sTd = reinterpret_cast<double *>(((uintptr_t)(sTq + (size_t)ht * nS) + 7) & ~(uintptr_t)7); // [ht][nS]
+    int *sRot = reinterpret_cast<int *>(sTd + (size_t)ht * nS);   // [nS][9]
+    int *sT24 = sRot + nS * 9;                                     // [nS][3]
+    int *sTypes = sT24 + nS * 3;                                   // [nT]
+
+    for (int i = tid; i < nS * 9; i += blockDim.x) sRot[i] = S.sym_rot[i];
+    for (int i = tid; i < nS * 3; i += blockDim.x) sT24[i] = S.sym_t24[i];
+    for (int i = tid; i < nT; i += blockDim.x) sTypes[i] = S.tile_types[tile * kMaxTileTypes + i];
+
+    // per-atom registers
+    const int a = a_begin + tid;
+    const bool have = a < a_end;
+    bool active = false;
+    int lt = 0, adpk = 0;
+    R w = R(0), pg[25], adp[6];
+    R anre = R(0), anim = R(0);
+    uint32_t xq0 = 0, xq1 = 0, xq2 = 0;
+    R x0 = R(0), x1 = R(0), x2 = R(0);  // FP32: low parts (cycles); FP64: coordinates
+    for (int q = 0; q < 25; q++) pg[q] = R(0);
+    for (int q = 0; q < 6; q++) adp[q] = R(0);
+    if (have) {
+        active = S.atom_active[a] != 0;
+        lt = S.atom_ltype[a];
+        adpk = S.atom_adpk[a];
+        if constexpr (sizeof(R) == 4) {
+            w = S.atom_w_f[a];
+            const float2 an = S.atom_anom_f[a];
+            anre = an.x; anim = an.y;
+            xq0 = S.atom_xq[3 * a]; xq1 = S.atom_xq[3 * a + 1]; xq2 = S.atom_xq[3 * a + 2];
+            x0 = S.atom_xlo[3 * a]; x1 = S.atom_xlo[3 * a + 1]; x2 = S.atom_xlo[3 * a + 2];
+            for (int q = 0; q < 6; q++) adp[q] = S.atom_adp_f[6 * a + q];
+            if (S.model == MODEL_HC)
+                for (int q = 0; q < 25; q++) pg[q] = S.atom_pg_f[25 * a + q];
+        } else {
+            w = S.atom_w_d[a];
+            const double2 an = S.atom_anom_d[a];
+            anre = an.x; anim = an.y;
+            x0 = S.atom_xd[3 * a]; x1 = S.atom_xd[3 * a + 1]; x2 = S.atom_xd[3 * a + 2];
+            for (int q = 0; q < 6; q++) adp[q] = S.atom_adp_d[6 * a + q];
+            if (S.model == MODEL_HC)
+                for (int q = 0; q < 25; q++) pg[q] = S.atom_pg_d[25 * a + q];
+        }
+    }
+    const bool table_model = S.model == MODEL_TABLE;
+    const int a_orig = have ? S.atom_orig[a] : 0;
+
+    // FP64 derivative totals
+    double gx[3] = {0, 0, 0}, gadp[6] = {0, 0, 0, 0, 0, 0}, gocc = 0;
+    double gpv = 0, gk = 0, gkp = 0;
+    double gplm[MP ? 25 : 1];
+    for (int q = 0; q < (MP ? 25 : 1); q++) gplm[q] = 0;
+
+    for (int h0 = h_begin; h0 < h_end; h0 += ht) {
+        const int nh = min(ht, h_end - h0);
+        __syncthreads();
+        // ---- stage reflections: h', phase offsets, harmonics
+        for (int i = tid; i < nh * nS; i += blockDim.x) {
+            const int hl = i / nS, s = i - hl * nS;
+            const int4 hv = S.hkl[h0 + hl];
+            const int *Rm = sRot + 9 * s;
+            // h' = R^T h (row vector h times R)
+            const int hp0 = hv.x * Rm[0] + hv.y * Rm[3] + hv.z * Rm[6];
+            const int hp1 = hv.x * Rm[1] + hv.y * Rm[4] + hv.z * Rm[7];
+            const int hp2 = hv.x * Rm[2] + hv.y * Rm[5] + hv.z * Rm[8];
+            R *hp = sHp + 3 * i;
+            hp[0] = R(hp0); hp[1] = R(hp1); hp[2] = R(hp2);
+            // h.t mod 1, exact: translations are multiples of 1/24
+            int tr = (hv.x * sT24[3 * s] + hv.y * sT24[3 * s + 1] + hv.z * sT24[3 * s + 2]) % 24;
+            if (tr < 0) tr += 24;
+            sTd[i] = tr / 24.0;
+            sTq[i] = (uint32_t)((((uint64_t)tr << 32) + 12u) / 24u);
+            R *y = sY + 25 * (size_t)i;
+            if (S.model == MODEL_HC) {
+                const double cx = S.B[0] * hp0 + S.B[1] * hp1 + S.B[2] * hp2;
+                const double cy = S.B[3] * hp0 + S.B[4] * hp1 + S.B[5] * hp2;
+                const double cz = S.B[6] * hp0 + S.B[7] * hp1 + S.B[8] * hp2;
+                const double n2 = cx * cx + cy * cy + cz * cz;
+                if (n2 > 1e-20) {
+                    const double inv = 1.0 / sqrt(n2);
+                    R v[25];
+                    harmonic_polys<R>(R(cx * inv), R(cy * inv), R(cz * inv), v);
+                    for (int q = 0; q < 25; q++) y[q] = v[q] * R(kDensityNorm[q]);
+                } else {
+                    for (int q = 0; q < 25; q++) y[q] = R(0);  // F(000): no deformation term
+                }
+            }
+        }
+        for (int i = tid; i < nh * nT; i += blockDim.x) {
+            const int hl = i / nT, t = i - hl * nT;
+            R rad[13];
+            radial_terms<R>(S, S.types[sTypes[t]], S.model, S.h2[h0 + hl], rad, MP);
+            R *dst = sRad + ((size_t)hl * kMaxTileTypes + t) * kRad;
+            for (int q = 0; q < kRad; q++) dst[q] = rad[q];
+        }
+        for (int i = tid; i < nh; i += blockDim.x) {
+            if constexpr (sizeof(R) == 4) sG[i] = C.gw_f[h0 + i];
+            else sG[i] = C.gw_d[h0 + i];
+            sH2[i] = R(S.h2[h0 + i]);
+        }
+        __syncthreads();
+
+        // ---- per-atom sums over reflections of the sub-tile
+        R px[3] = {0, 0, 0}, padp[6] = {0, 0, 0, 0, 0, 0}, pocc = 0;
+        R ppv = 0, pk = 0, pkp = 0;
+        R pplm[MP ? 25 : 1];
+        for (int q = 0; q < (MP ? 25 : 1); q++) pplm[q] = 0;
+
+        for (int hl = 0; hl < nh; hl++) {
+            R Fre = R(0), Fim = R(0);
+            if (active) {
+                const R2 g = sG[hl];
+                const R *rad = sRad + ((size_t)hl * kMaxTileTypes + lt) * kRad;
+                const R fsre = rad[0] + anre, fsim = anim;
+                const R r0 = rad[1], r1 = rad[2], r2 = rad[3], r3 = rad[4], r4 = rad[5];
+                R Tiso = R(1);
+                if (adpk == 1) Tiso = exp_<R>(-adp[0] * sH2[hl]);
+                // adjoint weight with the isotropic factor folded in (used inside the loop)
+                const R gre = g.x * Tiso, gim = g.y * Tiso;
+                R Ure = 0, Uim = 0;
+                R Xre[3] = {0, 0, 0}, Xim[3] = {0, 0, 0};
+                R Are[6] = {0, 0, 0, 0, 0, 0}, Aim[6] = {0, 0, 0, 0, 0, 0};
+                R Ere = 0, Eim = 0, Kre = 0, Kim = 0;
+                const R *yb = sY + (size_t)hl * nS * 25;
+                const R *hpb = sHp + (size_t)hl * nS * 3;
+                for (int s = 0; s < nS; s++) {
+                    const R *hp = hpb + 3 * s;
+                    const R h0f = hp[0], h1f = hp[1], h2f = hp[2];
+                    // phase (cycles)
+                    R sn, cs;
+                    if constexpr (sizeof(R) == 4) {
+                        const int i0 = (int)h0f, i1 = (int)h1f, i2 = (int)h2f;
+                        const uint32_t P = (uint32_t)i0 * xq0 + (uint32_t)i1 * xq1 + (uint32_t)i2 * xq2 +
+                                           sTq[hl * nS + s];
+                        const float ph = (float)(int32_t)P * 2.3283064365386963e-10f +
+                                         (h0f * x0 + h1f * x1 + h2f * x2);
+                        sincos2pi<R>(ph, &sn, &cs);
+                    } else {
+                        double ph = h0f * x0 + h1f * x1 + h2f * x2 + sTd[hl * nS + s];
+                        ph -= rint(ph);
+                        sincos2pi<R>(ph, &sn, &cs);
+                    }
+                    R zre = cs, zim = sn;  // e^{i theta} T_s
+                    R m6[6];
+                    if (adpk == 6) {
+                        m6[0] = h0f * h0f; m6[1] = h1f * h1f; m6[2] = h2f * h2f;
+                        m6[3] = R(2) * h0f * h1f; m6[4] = R(2) * h0f * h2f; m6[5] = R(2) * h1f * h2f;
+                        const R q = adp[0] * m6[0] + adp[1] * m6[1] + adp[2] * m6[2] + adp[3] * m6[3] +
+                                    adp[4] * m6[4] + adp[5] * m6[5];
+                        const R T = exp_<R>(-q);
+                        zre *= T; zim *= T;
+                    }
+                    R fre, fim;
+                    R A0 = 0, A1 = 0, A2 = 0, A3 = 0, A4 = 0;
+                    const R *y = yb + 25 * s;
+                    if (table_model) {
+                        if constexpr (sizeof(R) == 4) {
+                            const float2 tv = S.table_f[((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig];
+                            fre = tv.x + anre; fim = tv.y + anim;
+                        } else {
+                            const double2 tv = S.table_d[((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig];
+                            fre = tv.x + anre; fim = tv.y + anim;
+                        }
+                    } else {
+                        A0 = pg[0] * y[0];
+                        A1 = pg[1] * y[1] + pg[2] * y[2] + pg[3] * y[3];
+                        A2 = pg[4] * y[4] + pg[5] * y[5] + pg[6] * y[6] + pg[7] * y[7] + pg[8] * y[8];
+                        A3 = pg[9] * y[9] + pg[10] * y[10] + pg[11] * y[11] + pg[12] * y[12] + pg[13] * y[13] +
+                             pg[14] * y[14] + pg[15] * y[15];
+                        A4 = pg[16] * y[16] + pg[17] * y[17] + pg[18] * y[18] + pg[19] * y[19] + pg[20] * y[20] +
+                             pg[21] * y[21] + pg[22] * y[22] + pg[23] * y[23] + pg[24] * y[24];
+                        fre = fsre + r0 * A0 + r2 * A2 + r4 * A4;
+                        fim = fsim + r1 * A1 + r3 * A3;
+                    }
+                    const R ure = fre * zre - fim * zim;
+                    const R uim = fre * zim + fim * zre;
+                    Ure += ure; Uim += uim;
+                    Xre[0] += h0f * ure; Xim[0] += h0f * uim;
+                    Xre[1] += h1f * ure; Xim[1] += h1f * uim;
+                    Xre[2] += h2f * ure; Xim[2] += h2f * uim;
+                    if (adpk == 6) {
+#pragma unroll
+                        for (int k = 0; k < 6; k++) { Are[k] -= m6[k] * ure; Aim[k] -= m6[k] * uim; }
+                    }
+                    if constexpr (MP) {
+                        Ere += zre; Eim += zim;
+                        // q_l = Re(g i^l rr_l z): even l rs_l Re(gz), odd l -rs_l Im(gz)
+                        const R wre = gre * zre - gim * zim, wim = gre * zim + gim * zre;
+                        const R q0 = r0 * wre, q1 = -r1 * wim, q2 = r2 * wre, q3 = -r3 * wim, q4 = r4 * wre;
+                        pplm[0] += q0 * y[0];
+#pragma unroll
+                        for (int q = 1; q < 4; q++) pplm[q] += q1 * y[q];
+#pragma unroll
+                        for (int q = 4; q < 9; q++) pplm[q] += q2 * y[q];
+#pragma unroll
+                        for (int q = 9; q < 16; q++) pplm[q] += q3 * y[q];
+#pragma unroll
+                        for (int q = 16; q < 25; q++) pplm[q] += q4 * y[q];
+                        const R dre = rad[8] * A0 + rad[10] * A2 + rad[12] * A4;
+                        const R dim = rad[9] * A1 + rad[11] * A3;
+                        Kre += dre * zre - dim * zim;
+                        Kim += dre * zim + dim * zre;
+                    }
+                }
+                if (adpk == 1) {
+                    Ure *= Tiso; Uim *= Tiso;
+#pragma unroll
+                    for (int j = 0; j < 3; j++) { Xre[j] *= Tiso; Xim[j] *= Tiso; }
+                    Ere *= Tiso; Eim *= Tiso; Kre *= Tiso; Kim *= Tiso;
+                }
+                Fre = w * Ure;
+                Fim = w * Uim;
+                const R gU = g.x * Ure - g.y * Uim;  // Re(g U)
+                pocc += gU;
+                if (adpk == 1) padp[0] -= sH2[hl] * gU;
+                if (adpk == 6) {
+#pragma unroll
+                    for (int k = 0; k < 6; k++) padp[k] += g.x * Are[k] - g.y * Aim[k];
+                }
+#pragma unroll
+                for (int j = 0; j < 3; j++) px[j] -= g.x * Xim[j] + g.y * Xre[j];  // -Im(g X)
+                if constexpr (MP) {
+                    const R gE = g.x * Ere - g.y * Eim;
+                    ppv += rad[6] * gE;
+                    pk += rad[7] * gE;
+                    pkp += g.x * Kre - g.y * Kim;
+                }
+            }
+            // block reduction of the partial F of this reflection
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                Fre += shfl_xor<R>(Fre, o);
+                Fim += shfl_xor<R>(Fim, o);
+            }
+            if (lane == 0) {
+                R2 v;
+                v.x = Fre; v.y = Fim;
+                sF[warp * ht + hl] = v;
+            }
+        }
+        // fold FP32 sub-tile sums into FP64 totals
+#pragma unroll
+        for (int j = 0; j < 3; j++) gx[j] += (double)px[j];
+#pragma unroll
+        for (int k = 0; k < 6; k++) gadp[k] += (double)padp[k];
+        gocc += (double)pocc;
+        if constexpr (MP) {
+            gpv += (double)ppv; gk += (double)pk; gkp += (double)pkp;
+#pragma unroll
+            for (int q = 0; q < 25; q++) gplm[q] += (double)pplm[q];
+        }
+        __syncthreads();
+        for (int i = tid; i < nh; i += blockDim.x) {
+            double sre = 0, sim = 0;
+#pragma unroll
+            for (int wp = 0; wp < kWarps; wp++) {
+                const R2 v = sF[wp * ht + i];
+                sre += (double)v.x;
+                sim += (double)v.y;
+            }
+            atomicAdd(&C.f_acc[h0 + i].x, sre);
+            atomicAdd(&C.f_acc[h0 + i].y, sim);
+        }
+    }
+    if (active) {
+        double *G = C.g_acc + (size_t)a * kNch;
+#pragma unroll
+        for (int j = 0; j < 3; j++) atomicAdd(G + CH_XYZ + j, gx[j]);
+        if (adpk == 1) atomicAdd(G + CH_ADP, gadp[0]);
+        if (adpk == 6)
+#pragma unroll
+            for (int k = 0; k < 6; k++) atomicAdd(G + CH_ADP + k, gadp[k]);
+        atomicAdd(G + CH_OCC, gocc);
+        if constexpr (MP) {
+            atomicAdd(G + CH_PV, gpv);
+            atomicAdd(G + CH_KAPPA, gk);
+            atomicAdd(G + CH_KAPPA_P, gkp);
+#pragma unroll
+            for (int q = 0; q < 25; q++) atomicAdd(G + CH_PLM + q, gplm[q]);
+        }
+    }
+}
+
+// shared memory bytes of one block
+template <typename R>
+size_t sf_grad_smem(int ht, int n_sym, int n_tile_types)
+{
+    (void)n_tile_types;
+    size_t b = 0;
+    b += (size_t)ht * n_sym * 25 * sizeof(R);
+    b += (size_t)ht * kMaxTileTypes * 13 * sizeof(R);
+    b += (size_t)ht * n_sym * 3 * sizeof(R);
+    b += (size_t)ht * 2 * sizeof(R);                 // sG
+    b += (size_t)(kTileAtoms / 32) * ht * 2 * sizeof(R);  // sF
+    b += (size_t)ht * sizeof(R);                     // sH2
+    b += (size_t)ht * n_sym * sizeof(uint32_t) + 8;  // sTq + align
+    b += (size_t)ht * n_sym * sizeof(double);        // sTd
+    b += (size_t)n_sym * 12 * sizeof(int);
+    b += (size_t)kMaxTileTypes * sizeof(int);
+    return b + 64;
+}
+
+template <typename R, bool MP>
+cudaError_t launch_sf_grad_t(const DevStructure &S, const CallBuffers &C, int hkl_chunk, int ht, cudaStream_t st)
+{
+    const size_t smem = sf_grad_smem<R>(ht, S.n_sym, kMaxTileTypes);
+    cudaError_t e = cudaFuncSetAttribute(sf_grad_kernel<R, MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(S.n_tiles, (S.n_hkl + hkl_chunk - 1) / hkl_chunk);
+    sf_grad_kernel<R, MP><<<grid, kTileAtoms, smem, st>>>(S, C, hkl_chunk, ht);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sf_grad(const DevStructure &S, const CallBuffers &C, bool fp64, bool mp, int hkl_chunk, int ht,
+                           cudaStream_t st)
+{
+    if (fp64) return mp ? launch_sf_grad_t<double, true>(S, C, hkl_chunk, ht, st)
+                        : launch_sf_grad_t<double, false>(S, C, hkl_chunk, ht, st);
+    return mp ? launch_sf_grad_t<float, true>(S, C, hkl_chunk, ht, st)
+              : launch_sf_grad_t<float, false>(S, C, hkl_chunk, ht, st);
+}
+
+size_t sf_grad_smem_bytes(bool fp64, int ht, int n_sym)
+{
+    return fp64 ? sf_grad_smem<double>(ht, n_sym, kMaxTileTypes) : sf_grad_smem<float>(ht, n_sym, kMaxTileTypes);
+}
+
+}  // namespace dsf

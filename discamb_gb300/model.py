@@ -137,3 +137,71 @@ class Structure:
         """atom x symop x hkl terms, symops counted as point-group order
         without centering."""
         return self.n_atoms * self.sg.point_group_order * self.n_hkl
+
+
+# ---------------------------------------------------------------------------
+# flat-array serialisation (fixtures)
+# ---------------------------------------------------------------------------
+
+def structure_to_arrays(st: Structure):
+    """All inputs of a Structure as a dict of numpy arrays."""
+    out = dict(cell=np.array(st.cell), sg_symbol=np.array(st.sg.symbol), ops="|".join(st.sg.ops_text),
+               xyz=st.xyz, adp=st.adp_array(), n_adp=st.n_adp(), occupancy=st.occupancy,
+               multiplicity=np.asarray(st.multiplicity), atom_wfn=st.atom_wfn, atom_type=st.atom_type,
+               lcs=np.asarray(st.lcs), hkl=st.hkl, dtdf=st.dtdf,
+               type_plm=np.array([t.plm for t in st.types]), type_nl=np.array([t.n_l for t in st.types]),
+               type_pval=np.array([t.p_val for t in st.types]), type_kappa=np.array([t.kappa for t in st.types]),
+               type_kappa_p=np.array([t.kappa_prime for t in st.types]),
+               adp_convention=np.array(st.adp_convention), xyz_convention=np.array(st.xyz_convention))
+    if st.anomalous is not None:
+        out["anomalous"] = np.asarray(st.anomalous)
+    if st.include is not None:
+        out["include"] = np.asarray(st.include)
+    # wavefunctions: orbitals flattened
+    wl, wz, wdef, wdpow, wan = [], [], [], [], []
+    orb_w, orb_occ, orb_core, sto_o, sto_pow, sto_exp, sto_c = [], [], [], [], [], [], []
+    for wi, w in enumerate(st.wfns):
+        wl.append(w.label); wz.append(w.atomic_number); wdef.append(w.def_val_exp)
+        wdpow.append(list(w.def_val_pow) + [-1] * (5 - len(w.def_val_pow))); wan.append(complex(w.anomalous))
+        for k, o in enumerate(w.orbitals):
+            oi = len(orb_w)
+            orb_w.append(wi); orb_occ.append(w.occupancy[k]); orb_core.append(1 if k in w.core else 0)
+            for p_, e_, c_ in zip(o.powers, o.exponents, o.coefficients):
+                sto_o.append(oi); sto_pow.append(p_); sto_exp.append(e_); sto_c.append(c_)
+    out.update(wfn_label=np.array(wl), wfn_z=np.array(wz), wfn_def_exp=np.array(wdef), wfn_def_pow=np.array(wdpow),
+               wfn_anom=np.array(wan), orb_wfn=np.array(orb_w), orb_occ=np.array(orb_occ),
+               orb_core=np.array(orb_core), sto_orb=np.array(sto_o), sto_pow=np.array(sto_pow),
+               sto_exp=np.array(sto_exp), sto_coeff=np.array(sto_c))
+    out["ops"] = np.array(out["ops"])
+    out["name"] = np.array(st.name)
+    return out
+
+
+def structure_from_arrays(d):
+    from .crystal import SpaceGroup
+    ops = str(d["ops"]).split("|")
+    sg = SpaceGroup(str(d["sg_symbol"]), ops)
+    wfns = []
+    for wi in range(len(d["wfn_label"])):
+        orbitals, occ, core, val = [], [], [], []
+        for oi in np.nonzero(d["orb_wfn"] == wi)[0]:
+            sel = d["sto_orb"] == oi
+            orbitals.append(Orbital([int(v) for v in d["sto_pow"][sel]], [float(v) for v in d["sto_exp"][sel]],
+                                    [float(v) for v in d["sto_coeff"][sel]]))
+            occ.append(int(d["orb_occ"][oi]))
+            (core if d["orb_core"][oi] else val).append(len(orbitals) - 1)
+        dp = [int(v) for v in d["wfn_def_pow"][wi] if v >= 0]
+        wfns.append(Wavefunction(str(d["wfn_label"][wi]), int(d["wfn_z"][wi]), orbitals, occ, core, val,
+                                 float(d["wfn_def_exp"][wi]), dp, complex(d["wfn_anom"][wi])))
+    types = [AtomType(np.array(d["type_plm"][t]), int(d["type_nl"][t]), float(d["type_pval"][t]),
+                      float(d["type_kappa"][t]), float(d["type_kappa_p"][t])) for t in range(len(d["type_nl"]))]
+    n_adp = d["n_adp"]
+    adp = [list(d["adp"][i, :n_adp[i]]) for i in range(len(n_adp))]
+    return Structure(cell=tuple(float(v) for v in d["cell"]), sg=sg, xyz=np.array(d["xyz"]), adp=adp,
+                     occupancy=np.array(d["occupancy"]), multiplicity=np.array(d["multiplicity"]),
+                     atom_wfn=np.array(d["atom_wfn"]), atom_type=np.array(d["atom_type"]), lcs=np.array(d["lcs"]),
+                     wfns=wfns, types=types, hkl=np.array(d["hkl"], dtype=np.int32), dtdf=np.array(d["dtdf"]),
+                     anomalous=np.array(d["anomalous"]) if "anomalous" in d else None,
+                     include=np.array(d["include"]) if "include" in d else None,
+                     adp_convention=str(d["adp_convention"]), xyz_convention=str(d["xyz_convention"]),
+                     name=str(d["name"]))

@@ -1,0 +1,190 @@
+/*
+ * dsf_gb300 -- C ABI of the GB300 structure-factor + derivative engine.
+ *
+ * Drop-in boundary for the structure-factor hot path of DiSCaMB.  The
+ * functions here replace, call for call:
+ *
+ *   dsf_structure_create_hc     HansenCoppensStructureFactorCalculator(crystal, HC_ModelParameters)
+ *                               + setModel (src/Scattering/HansenCoppensStructureFactorCalculator.cpp:57-72, 157-290)
+ *   dsf_structure_create_iam    AnyIamCalculator::set / IamFormFactorCalculationsManager
+ *                               (src/Scattering/AnyIamCalculator.cpp:49-154)
+ *   dsf_structure_create_tabulated
+ *                               TscFileBasedSfCalculator + ConstFormFactorCalculationsManager
+ *                               (src/Scattering/TscFileBasedSfCalculator.cpp:17-123,
+ *                                src/Scattering/ConstFormFactorCalculationsManager.cpp:34-102)
+ *   dsf_structure_set_hkl       the hkl argument of calculateStructureFactorsAndDerivatives, kept
+ *                               resident across calls (include/discamb/Scattering/SfCalculator.h:45-67)
+ *   dsf_structure_update_atoms  SfCalculator::update / the atoms argument
+ *                               (prepareDataForEngine_part, HansenCoppensStructureFactorCalculator.cpp:897-990)
+ *   dsf_structure_update_types  HC_ModelParameters::type_parameters (P_lm, P_val, kappa, kappa')
+ *   dsf_structure_set_lcs       the localCoordinateSystems argument
+ *                               (include/discamb/Scattering/HansenCoppensStructureFactorCalculator.h:148-165)
+ *   dsf_calculate               calculateStructureFactorsAndDerivatives(atoms, [lcs,] hkl, f,
+ *                               dTarget_dparam, dTarget_df, countAtomContribution, selector)
+ *                               (HansenCoppensStructureFactorCalculator.cpp:380-508 and
+ *                                AnyScattererStructureFactorCalculator.cpp:614-829), host buffers
+ *   dsf_calculate_device        the same with device-resident buffers on a caller stream
+ *   dsf_last_error              on_error::throwException messages (include/discamb/BasicUtilities/on_error.h:24-36):
+ *                               every function returns a status instead of throwing
+ *
+ * Conventions follow the reference: dT/dF = dT/dA + i dT/dB per reflection;
+ * derivatives are returned in the crystal's xyz and ADP conventions;
+ * positions fractional or Cartesian [A]; ADPs U_cif, U_cart or U_star;
+ * anisotropic ADP order U11 U22 U33 U12 U13 U23.
+ * Thread safety: one structure must not be used by two host threads at once
+ * (as for the reference calculators); distinct structures may.
+ */
+#ifndef DSF_GB300_H
+#define DSF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DSF_ABI_VERSION 1
+
+enum dsf_status {
+    DSF_OK = 0,
+    DSF_ERR_ARGUMENT = 1,   /* invalid argument (size mismatch, bad index, unsupported value) */
+    DSF_ERR_CUDA = 2,       /* CUDA runtime error */
+    DSF_ERR_MEMORY = 3,     /* device or host allocation failed, or over the memory budget */
+    DSF_ERR_STATE = 4,      /* call not valid in the current state (e.g. no reflections set) */
+    DSF_ERR_TIMEOUT = 5,    /* a bounded wait ran out */
+    DSF_ERR_UNSUPPORTED = 6
+};
+
+enum dsf_precision { DSF_FP64 = 0, DSF_FP32_BULK = 1 };
+enum dsf_xyz_convention { DSF_XYZ_FRACTIONAL = 0, DSF_XYZ_CARTESIAN = 1 };
+enum dsf_adp_convention { DSF_ADP_U_CIF = 0, DSF_ADP_U_CART = 1, DSF_ADP_U_STAR = 2 };
+
+/* derivative selection (DerivativesSelector, include/discamb/Scattering/SF_CalcDataTypes.h:22-27,
+ * plus the multipole-model parameters the reference does not differentiate) */
+enum dsf_derivative_flags {
+    DSF_D_XYZ = 1, DSF_D_ADP = 2, DSF_D_OCC = 4,
+    DSF_D_MULTIPOLE = 8   /* P_val, P_lm, kappa, kappa' per atom */
+};
+
+typedef struct dsf_engine dsf_engine;
+typedef struct dsf_structure dsf_structure;
+
+/* Crystal symmetry as the engine consumes it.  Either the engine subset
+ * (operations modulo inversion and lattice centering, centrosymmetric = 1,
+ * inversion_translation = t of the inversion -x+t; the HansenCoppens CPU
+ * engine's representation) or any operation list with centrosymmetric = 0
+ * (e.g. all operations modulo centering: the generic AnyScatterer
+ * representation).  Lattice centering enters as the per-reflection
+ * multiplier of scattering_utilities::centeringSfMultipliers. */
+typedef struct {
+    double cell[6];                   /* a b c [A], alpha beta gamma [deg] */
+    int n_symops;
+    const int *symop_rotation;        /* [n_symops][3][3] fractional, row-major: x' = R x + t */
+    const double *symop_translation;  /* [n_symops][3] fractional (multiples of 1/24) */
+    int centrosymmetric;
+    double inversion_translation[3];
+    char centering;                   /* P A B C I F R */
+    int obverse;
+    int n_symops_total;               /* full operation count; weight = multiplicity / n_symops_total */
+} dsf_symmetry;
+
+/* Hansen-Coppens model: spherical densities per wavefunction type as Slater
+ * density terms c r^n exp(-z r) (CSR over wavefunction types), the
+ * deformation-valence radial functions and the atom types. */
+typedef struct {
+    int n_wfn;
+    const int *core_offset;    /* [n_wfn+1] */
+    const double *core_coeff;
+    const double *core_exp;
+    const int *core_pow;
+    const int *val_offset;     /* [n_wfn+1], valence normalised to one electron */
+    const double *val_coeff;
+    const double *val_exp;
+    const int *val_pow;
+    const double *def_val_exp;  /* [n_wfn] zeta [1/A] */
+    const int *def_val_npow;    /* [n_wfn] number of n_l entries (<= 5) */
+    const int *def_val_pow;     /* [n_wfn][5] n_l */
+    const double *anomalous;    /* [n_wfn][2] */
+    int n_types;
+    const int *type_nl;          /* [n_types] number of l levels of P_lm (p_lm.size()) */
+    const double *type_plm;      /* [n_types][25], index l*l + m + l, density normalised */
+    const double *type_pval;
+    const double *type_kappa;
+    const double *type_kappa_prime;
+} dsf_hc_model;
+
+/* IAM: per scatterer type f0(|h|) = sum_i a_i exp(-b_i |h|^2/4) + c */
+typedef struct {
+    int n_types;
+    const int *n_gauss;     /* [n_types] <= 5 */
+    const double *a;        /* [n_types][5] */
+    const double *b;        /* [n_types][5] */
+    const double *c;        /* [n_types] */
+} dsf_iam_model;
+
+typedef struct {
+    int n_atoms;
+    const int *atom_wfn;         /* HC: wavefunction type */
+    const int *atom_type;        /* HC / IAM: type */
+    const int *adp_components;   /* 0, 1 or 6 */
+    const double *lcs;           /* HC: [n_atoms][3][3] row-major, columns = local x, y, z */
+    const double *multiplicity;  /* [n_atoms] */
+    const double *anomalous;     /* [n_atoms][2] or NULL (HC: per wavefunction) */
+    int xyz_convention;
+    int adp_convention;
+} dsf_atoms;
+
+typedef struct {
+    double *f;            /* [n_hkl][2] */
+    double *d_xyz;        /* [n_atoms][3] or NULL */
+    double *d_adp;        /* [n_atoms][6] (first 1 or 6 used) or NULL */
+    double *d_occ;        /* [n_atoms] or NULL */
+    double *d_pval;       /* [n_atoms] or NULL */
+    double *d_plm;        /* [n_atoms][25] local frame or NULL */
+    double *d_kappa;      /* [n_atoms] or NULL */
+    double *d_kappa_prime;/* [n_atoms] or NULL */
+} dsf_outputs;
+
+/* ---- engine (one GPU, one stream) -------------------------------------- */
+int dsf_engine_create(int device, dsf_engine **out);
+int dsf_engine_destroy(dsf_engine *e);
+const char *dsf_last_error(const dsf_engine *e);
+int dsf_abi_version(void);
+
+/* ---- resident structures ---------------------------------------------- */
+int dsf_structure_create_hc(dsf_engine *e, const dsf_symmetry *sym, const dsf_hc_model *model,
+                            const dsf_atoms *atoms, dsf_structure **out);
+int dsf_structure_create_iam(dsf_engine *e, const dsf_symmetry *sym, const dsf_iam_model *model,
+                             const dsf_atoms *atoms, dsf_structure **out);
+/* table: complex form factors [n_hkl][n_symops][n_atoms] (re,im) for the
+ * reflections passed here (they become the structure's reflection set) */
+int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms,
+                                   int n_hkl, const int *hkl, const double *table, int table_fp32,
+                                   dsf_structure **out);
+int dsf_structure_destroy(dsf_structure *s);
+
+int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl);
+/* atoms in the crystal's conventions; adp [n_atoms][6] (first 1 or 6 used) */
+int dsf_structure_update_atoms(dsf_structure *s, const double *xyz, const double *adp, const double *occupancy);
+int dsf_structure_update_types(dsf_structure *s, const double *type_plm, const double *type_pval,
+                               const double *type_kappa, const double *type_kappa_prime);
+int dsf_structure_set_lcs(dsf_structure *s, const double *lcs);
+/* bytes of device memory the structure holds */
+int64_t dsf_structure_device_bytes(const dsf_structure *s);
+
+/* ---- calculation --------------------------------------------------------- */
+/* host buffers: dtdf [n_hkl][2]; include [n_atoms] (NULL = all); outputs on host */
+int dsf_calculate(dsf_structure *s, int precision, int derivative_flags, const double *dtdf,
+                  const int *include, const dsf_outputs *out);
+/* device buffers, asynchronous on `stream` (cudaStream_t, NULL = engine stream) */
+int dsf_calculate_device(dsf_structure *s, int precision, int derivative_flags, const double *dtdf_device,
+                         const dsf_outputs *out_device, void *stream);
+
+/* number of kernel launches issued by the last calculation (for accounting) */
+int dsf_last_launch_count(const dsf_structure *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -116,8 +116,14 @@ def hc(st, n_threads=1):
         atom_anom, I(st.include_mask().astype(np.int32)), C.c_int(n_threads),
         D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]), C.byref(ms))
     if rc != 0:
-        raise RuntimeError("reference HC path raised an exception")
+        raise RuntimeError("reference HC path raised an exception: " + _err())
     return _pack(out, st, ms.value)
+
+
+def _err():
+    f = lib().ref_last_error
+    f.restype = C.c_char_p
+    return f().decode()
 
 
 def D_out(a):
@@ -148,12 +154,15 @@ def iam(st, labels, table="IT92", n_threads=1):
                           D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]),
                           C.byref(ms))
     if rc != 0:
-        raise RuntimeError("reference IAM path raised an exception")
+        raise RuntimeError("reference IAM path raised an exception: " + _err())
     return _pack(out, st, ms.value)
 
 
 def table(st, keys, values):
-    """keys: (k,3) int Miller indices, values: (k, n_atoms) complex."""
+    """keys: (k,3) int Miller indices, values: (k, n_atoms) complex.  The
+    generic engine builds a default IAM manager from the atom labels before
+    the table manager replaces it, so element labels are passed too."""
+    labels = ";".join(st.wfns[w].label for w in st.atom_wfn).encode()
     cell, ops, adp = _common(st)
     n = st.n_atoms
     out = _outputs(st.n_hkl, n)
@@ -164,10 +173,10 @@ def table(st, keys, values):
     g = np.ascontiguousarray(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1))
     k = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1))
     v = np.ascontiguousarray(np.stack([np.real(values), np.imag(values)], -1).reshape(-1))
-    rc = lib().ref_table_sf(D_out(cell), C.c_char_p(ops), C.c_int(n), D_out(xyz), D_out(nadp), D_out(adpf),
+    rc = lib().ref_table_sf(D_out(cell), C.c_char_p(ops), C.c_char_p(labels), C.c_int(n), D_out(xyz), D_out(nadp), D_out(adpf),
                             D_out(occ), D_out(mult), C.c_int(len(keys)), D_out(k), D_out(v), C.c_int(st.n_hkl),
                             D_out(hkl), D_out(g), D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]),
                             D_out(out["d_occ"]), C.byref(ms))
     if rc != 0:
-        raise RuntimeError("reference tabulated path raised an exception")
+        raise RuntimeError("reference tabulated path raised an exception: " + _err())
     return _pack(out, st, ms.value)

@@ -39,6 +39,8 @@ using std::vector;
 
 namespace {
 
+std::string g_last_error;
+
 struct Input {
     const double *cell;
     const char *ops;          // ';' separated operation strings
@@ -94,6 +96,8 @@ void write_out(const vector<complex<double> > &f, const vector<TargetFunctionAto
 } // namespace
 
 extern "C" {
+
+const char *ref_last_error(void) { return g_last_error.c_str(); }
 
 // Hansen-Coppens path through HansenCoppensStructureFactorCalculator ("CPU").
 // Wavefunctions as Slater orbitals: per wfn [orb_off[w], orb_off[w+1]) orbitals,
@@ -175,7 +179,11 @@ int ref_hc_sf(const double *cell, const char *ops, int n_atoms, const double *xy
         if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         write_out(f, d, f_out, d_xyz, d_adp, d_occ);
         return 0;
+    } catch (const std::exception &ex) {
+        g_last_error = ex.what();
+        return 1;
     } catch (...) {
+        g_last_error = "unknown exception";
         return 1;
     }
 }
@@ -191,7 +199,11 @@ int ref_iam_coefficients(const char *label, const char *table, double *a, double
         *n = (int)va.size();
         for (int i = 0; i < *n && i < 5; i++) { a[i] = va[i]; b[i] = vb[i]; }
         return 0;
+    } catch (const std::exception &ex) {
+        g_last_error = ex.what();
+        return 1;
     } catch (...) {
+        g_last_error = "unknown exception";
         return 1;
     }
 }
@@ -224,21 +236,25 @@ int ref_iam_sf(const double *cell, const char *ops, const char *labels, const ch
         if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         write_out(f, d, f_out, d_xyz, d_adp, d_occ);
         return 0;
+    } catch (const std::exception &ex) {
+        g_last_error = ex.what();
+        return 1;
     } catch (...) {
+        g_last_error = "unknown exception";
         return 1;
     }
 }
 
 // Tabulated path: AnyScatterer engine + ConstFormFactorCalculationsManager with a
 // map from Miller index to the per-atom complex form factors.
-int ref_table_sf(const double *cell, const char *ops, int n_atoms, const double *xyz, const int *n_adp,
+int ref_table_sf(const double *cell, const char *ops, const char *labels, int n_atoms, const double *xyz, const int *n_adp,
                  const double *adp, const double *occ, const int *mult,
                  int n_keys, const int *keys, const double *values /* [n_keys][n_atoms][2] */,
                  int n_hkl, const int *hkl, const double *dtdf,
                  double *f_out, double *d_xyz, double *d_adp, double *d_occ, double *ms)
 {
     try {
-        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, nullptr};
+        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, labels};
         Crystal crystal = make_crystal(in);
         std::map<Vector3i, vector<complex<double> > > table;
         for (int k = 0; k < n_keys; k++) {
@@ -265,7 +281,11 @@ int ref_table_sf(const double *cell, const char *ops, int n_atoms, const double 
         if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         write_out(f, d, f_out, d_xyz, d_adp, d_occ);
         return 0;
+    } catch (const std::exception &ex) {
+        g_last_error = ex.what();
+        return 1;
     } catch (...) {
+        g_last_error = "unknown exception";
         return 1;
     }
 }

@@ -1,0 +1,161 @@
+"""Writes the golden fixtures of tests/golden/ by running the reference
+library's own CPU code (oracle/_ref/libref_driver.so, built from the
+reference sources by oracle/Makefile.ref) on seeded synthetic structures.
+
+    python tests/golden/make_golden.py
+
+Each fixture (.npz) holds every input of the case (structure_to_arrays) and
+the reference outputs: F, d_xyz, d_adp, d_occ in the crystal's conventions.
+The multipole fixture adds dT/dP_val, dT/dP_lm, dT/dkappa, dT/dkappa' by
+central finite differences of the reference F (F is linear in P_val and
+P_lm, so one step is exact to rounding; kappa and kappa' use Richardson
+extrapolation over steps h and h/2), because the reference computes no
+analytic derivatives for those parameters.
+"""
+from __future__ import annotations
+
+import copy
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from discamb_gb300 import workloads as W  # noqa: E402
+from discamb_gb300.model import structure_to_arrays  # noqa: E402
+from oracle import ref as R  # noqa: E402
+
+
+def hc_cases():
+    cases = []
+    for i, sg in enumerate(["P1", "P-1", "P21", "P21/c", "P212121", "C2/c", "P43212", "P-1(shift)", "I2/m-like"]):
+        st = W.small_case(sg, n_atoms=5, stol_max=0.55, seed=100 + i, improper_lcs=True)
+        cases.append((f"hc_{sg.replace('/', '_').replace('(', '_').replace(')', '')}", st))
+    st = W.config0(seed=0)
+    cases.append(("hc_config0", st))
+    # per-atom anomalous dispersion, an excluded atom, occupancies below one
+    st = W.small_case("P21/c", n_atoms=6, stol_max=0.5, seed=201, anomalous_per_atom=True, occupancy=(0.6, 1.0))
+    st.include = np.array([1, 1, 0, 1, 1, 1], dtype=bool)
+    cases.append(("hc_anomalous_mask", st))
+    # isotropic-only, special-position multiplicity, one reflection list with 000
+    st = W.small_case("P212121", n_atoms=4, stol_max=0.5, seed=202, aniso=False)
+    st.multiplicity = np.array([4, 2, 4, 1], dtype=np.int32)
+    st.hkl = np.concatenate([np.zeros((1, 3), dtype=np.int32), st.hkl])
+    st.dtdf = np.concatenate([[0.3 - 0.7j], st.dtdf])
+    cases.append(("hc_iso_special_000", st))
+    # dipole/quadrupole-along-z types only (the engine's pz/dz path)
+    st = W.small_case("P-1", n_atoms=4, stol_max=0.5, seed=203, l_max=2)
+    for t in st.types:
+        t.plm[:] = 0.0
+        t.plm[2] = 0.07
+        t.plm[6] = -0.03
+        t.n_l = 3
+    cases.append(("hc_pz_dz", st))
+    return cases
+
+
+def run_hc(name, st):
+    r = R.hc(st, n_threads=4)
+    out = structure_to_arrays(st)
+    nadp = st.n_adp()
+    d_adp = np.zeros((st.n_atoms, 6))
+    for i, v in enumerate(r["d_adp"]):
+        d_adp[i, :nadp[i]] = v
+    out.update(ref_f=r["f"], ref_d_xyz=r["d_xyz"], ref_d_adp=d_adp, ref_d_occ=r["d_occ"])
+    return out
+
+
+def target(st):
+    r = R.hc(st, n_threads=4)
+    return float(np.sum((np.conj(st.dtdf) * r["f"]).real))
+
+
+def multipole_fd(st):
+    """dT/dparam of every type parameter by finite differences of the
+    reference F; one type per atom, so these are the per-atom derivatives."""
+    n = st.n_atoms
+    d_pval, d_kappa, d_kappa_p = np.zeros(n), np.zeros(n), np.zeros(n)
+    d_plm = np.zeros((n, 25))
+
+    def diff(mod, h):
+        s1 = copy.deepcopy(st); mod(s1, +h)
+        s2 = copy.deepcopy(st); mod(s2, -h)
+        return (target(s1) - target(s2)) / (2 * h)
+
+    for a in range(n):
+        t = st.atom_type[a]
+
+        def set_attr(name):
+            def f(s, h):
+                setattr(s.types[t], name, getattr(s.types[t], name) + h)
+            return f
+        d_pval[a] = diff(set_attr("p_val"), 1e-2)
+        for name, arr in (("kappa", d_kappa), ("kappa_prime", d_kappa_p)):
+            h = 1e-3
+            d1 = diff(set_attr(name), h)
+            d2 = diff(set_attr(name), h / 2)
+            arr[a] = (4 * d2 - d1) / 3
+        for q in range(st.types[t].n_l ** 2):
+            def fq(s, h, q=q):
+                s.types[t].plm[q] += h
+            d_plm[a, q] = diff(fq, 1e-2)
+    return d_pval, d_plm, d_kappa, d_kappa_p
+
+
+def main():
+    os.makedirs(HERE, exist_ok=True)
+    for name, st in hc_cases():
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **run_hc(name, st))
+        print("wrote", name, st.n_atoms, st.n_hkl)
+    # multipole-parameter derivatives
+    st = W.small_case("P21/c", n_atoms=3, stol_max=0.45, seed=301)
+    out = run_hc("hc_multipole_fd", st)
+    d_pval, d_plm, d_k, d_kp = multipole_fd(st)
+    out.update(ref_d_pval=d_pval, ref_d_plm=d_plm, ref_d_kappa=d_k, ref_d_kappa_p=d_kp)
+    np.savez_compressed(os.path.join(HERE, "hc_multipole_fd.npz"), **out)
+    print("wrote hc_multipole_fd")
+    # IAM with the reference's IT92 Gaussian table
+    st = W.small_case("C2/c", n_atoms=6, stol_max=0.6, seed=401)
+    labels = [w.label for w in st.wfns]
+    labels_atoms = [st.wfns[w].label for w in st.atom_wfn]
+    ng, ga, gb, gc = [], np.zeros((len(labels), 5)), np.zeros((len(labels), 5)), []
+    for i, lab in enumerate(labels):
+        a, b, c = R.iam_coefficients(lab, "IT92")
+        ng.append(len(a)); ga[i, :len(a)] = a; gb[i, :len(b)] = b; gc.append(c)
+    st.atom_type = st.atom_wfn.copy()
+    r = R.iam(st, labels_atoms, "IT92")
+    out = structure_to_arrays(st)
+    d_adp = np.zeros((st.n_atoms, 6))
+    for i, v in enumerate(r["d_adp"]):
+        d_adp[i, :len(v)] = v
+    out.update(iam_ngauss=np.array(ng), iam_a=ga, iam_b=gb, iam_c=np.array(gc), ref_f=r["f"], ref_d_xyz=r["d_xyz"],
+               ref_d_adp=d_adp, ref_d_occ=r["d_occ"])
+    np.savez_compressed(os.path.join(HERE, "iam_it92.npz"), **out)
+    print("wrote iam_it92")
+    # tabulated form factors: one complex f per (atom, rotated index)
+    st = W.small_case("P21/c", n_atoms=4, stol_max=0.5, seed=501)
+    rng = np.random.default_rng(502)
+    keys = {}
+    for h in st.hkl:
+        for r_ in st.sg.rot:
+            hp = tuple(int(v) for v in (h @ r_))
+            if hp not in keys:
+                keys[hp] = (rng.normal(2, 1, st.n_atoms) + 1j * rng.normal(0, 0.3, st.n_atoms))
+    kk = np.array(list(keys.keys()), dtype=np.int32)
+    vv = np.array(list(keys.values()))
+    r = R.table(st, kk, vv)
+    out = structure_to_arrays(st)
+    d_adp = np.zeros((st.n_atoms, 6))
+    for i, v in enumerate(r["d_adp"]):
+        d_adp[i, :len(v)] = v
+    out.update(table_keys=kk, table_values=vv, ref_f=r["f"], ref_d_xyz=r["d_xyz"], ref_d_adp=d_adp,
+               ref_d_occ=r["d_occ"])
+    np.savez_compressed(os.path.join(HERE, "table_p21c.npz"), **out)
+    print("wrote table_p21c")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,205 @@
+"""GPU parity through the C ABI: the CUDA engine against the reference's own
+outputs (golden fixtures) and against the CPU oracle.
+
+Tolerances: plain FP64 form within 1e-10 relative (sum|dF|/sum|F| and the
+per-class norm error ||dg||/||g||); FP32-bulk form within 1e-6 for F and
+1e-5 per derivative class.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from conftest import fixture_names, load_fixture, rel_f, rel_norm, ref_adp_list
+from discamb_gb300 import api, workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FP64, FP32 = api.DSF_FP64, api.DSF_FP32_BULK
+TOL = {FP64: (1e-10, 1e-10), FP32: (1e-6, 1e-5)}
+HC = fixture_names("hc_")
+
+
+def check(r, ref_f, ref_xyz, ref_adp, ref_occ, prec):
+    tf, tg = TOL[prec]
+    e = dict(f=rel_f(r["f"], ref_f), xyz=rel_norm(r["d_xyz"], ref_xyz), adp=rel_norm(r["d_adp"], ref_adp),
+             occ=rel_norm(r["d_occ"], ref_occ))
+    assert e["f"] < tf, e
+    assert e["xyz"] < tg and e["adp"] < tg and e["occ"] < tg, e
+    return e
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+@pytest.mark.parametrize("name", HC)
+def test_hc_matches_reference(engine, name, prec):
+    st, d = load_fixture(name)
+    calc = api.HcCalculator(engine, st)
+    inc = None if st.include is None else st.include.astype(np.int32)
+    r = calc.calculate(st.dtdf, precision=prec, include=inc)
+    check(r, d["ref_f"], d["ref_d_xyz"], ref_adp_list(st, d), d["ref_d_occ"], prec)
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_hc_all_operations_representation(engine, prec):
+    # the generic engine's representation (all operations modulo centering, no
+    # inversion shortcut) gives the same F for a structure without anomalous
+    # dispersion
+    st, d = load_fixture("hc_P21_c")
+    for w in st.wfns:
+        w.anomalous = 0j
+    ref = O.compute(st)
+    calc = api.HcCalculator(engine, st, representation="all")
+    r = calc.calculate(st.dtdf, precision=prec)
+    check(r, ref["f"], ref["d_xyz"], ref["d_adp"], ref["d_occ"], prec)
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_multipole_derivatives(engine, prec):
+    st, d = load_fixture("hc_multipole_fd")
+    calc = api.HcCalculator(engine, st)
+    r = calc.calculate(st.dtdf, precision=prec, multipoles=True)
+    o = O.compute(st, multipoles=True)
+    tol = 1e-10 if prec == FP64 else 1e-5
+    for k in ("d_pval", "d_plm", "d_kappa", "d_kappa_p"):
+        assert rel_norm(r[k], o[k]) < tol, (k, rel_norm(r[k], o[k]))
+    # against finite differences of the reference F
+    assert rel_norm(r["d_pval"], d["ref_d_pval"]) < max(tol, 1e-8)
+    assert rel_norm(r["d_plm"], d["ref_d_plm"]) < max(tol, 1e-8)
+    assert rel_norm(r["d_kappa"], d["ref_d_kappa"]) < max(tol, 1e-6)
+    assert rel_norm(r["d_kappa_p"], d["ref_d_kappa_p"]) < max(tol, 1e-6)
+
+
+def iam_dict(d):
+    return dict(ngauss=d["iam_ngauss"], a=d["iam_a"], b=d["iam_b"], c=d["iam_c"])
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_iam_matches_reference(engine, prec):
+    st, d = load_fixture("iam_it92")
+    calc = api.IamCalculator(engine, st, iam_dict(d))
+    r = calc.calculate(st.dtdf, precision=prec)
+    check(r, d["ref_f"], d["ref_d_xyz"], ref_adp_list(st, d), d["ref_d_occ"], prec)
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_tabulated_matches_reference(engine, prec):
+    st, d = load_fixture("table_p21c")
+    lut = {tuple(k): v for k, v in zip(d["table_keys"], d["table_values"])}
+    rot, _ = api.all_ops_mod_centering(st.sg)
+    t = np.zeros((st.n_hkl, len(rot), st.n_atoms), dtype=complex)
+    for i, h in enumerate(st.hkl):
+        for s, r_ in enumerate(rot):
+            t[i, s] = lut[tuple(int(v) for v in h @ r_)]
+    calc = api.TabulatedCalculator(engine, st, t)
+    r = calc.calculate(st.dtdf, precision=prec)
+    check(r, d["ref_f"], d["ref_d_xyz"], ref_adp_list(st, d), d["ref_d_occ"], prec)
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_config1_subset_matches_oracle(engine, prec):
+    st = W.config1()
+    sel = np.random.default_rng(11).choice(st.n_hkl, 1500, replace=False)
+    st.hkl, st.dtdf = st.hkl[sel], st.dtdf[sel]
+    o = O.compute(st)
+    calc = api.HcCalculator(engine, st)
+    r = calc.calculate(st.dtdf, precision=prec)
+    check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_config2_subset_full_derivatives(engine, prec):
+    st = W.config2(n_atoms=6000)
+    sel = np.random.default_rng(12).choice(st.n_hkl, 300, replace=False)
+    st.hkl, st.dtdf = st.hkl[sel], st.dtdf[sel]
+    o = O.compute(st, multipoles=True)
+    calc = api.HcCalculator(engine, st)
+    r = calc.calculate(st.dtdf, precision=prec, multipoles=True)
+    check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
+    tol = TOL[prec][1]
+    for k in ("d_pval", "d_plm", "d_kappa", "d_kappa_p"):
+        assert rel_norm(r[k], o[k]) < tol, (k, rel_norm(r[k], o[k]))
+
+
+def test_fp32_against_fp64_full_config1(engine):
+    st = W.config1()
+    calc = api.HcCalculator(engine, st)
+    a = calc.calculate(st.dtdf, precision=FP64)
+    b = calc.calculate(st.dtdf, precision=FP32)
+    assert rel_f(b["f"], a["f"]) < 1e-6
+    for k in ("d_xyz", "d_adp", "d_occ"):
+        assert rel_norm(b[k], a[k]) < 1e-5, k
+
+
+def test_lattice_translation_and_occupancy_linearity(engine):
+    st = W.small_case("P212121", n_atoms=7, stol_max=0.6, seed=21)
+    calc = api.HcCalculator(engine, st)
+    a = calc.calculate(st.dtdf, precision=FP64)
+    calc.update_atoms(st.xyz + np.array([1.0, -2.0, 3.0]), st.adp, st.occupancy)
+    b = calc.calculate(st.dtdf, precision=FP64)
+    assert rel_f(b["f"], a["f"]) < 1e-13
+    calc.update_atoms(st.xyz, st.adp, 2 * st.occupancy)
+    c = calc.calculate(st.dtdf, precision=FP64)
+    assert rel_f(c["f"], 2 * a["f"]) < 1e-14
+
+
+def test_directional_derivative_consistency(engine):
+    # sum_p dT/dp dp == T(p + dp) - T(p - dp) / 2 for T = sum Re(conj(dT/dF) F)
+    st = W.small_case("C2/c", n_atoms=5, stol_max=0.5, seed=22)
+    calc = api.HcCalculator(engine, st)
+    r = calc.calculate(st.dtdf, precision=FP64)
+    rng = np.random.default_rng(3)
+    dx = rng.normal(size=st.xyz.shape) * 1e-6
+    adp = [np.array(a) for a in st.adp]
+    dadp = [rng.normal(size=len(a)) * 1e-7 for a in adp]
+    docc = rng.normal(size=st.n_atoms) * 1e-6
+
+    def target(sign):
+        calc.update_atoms(st.xyz + sign * dx, [a + sign * b for a, b in zip(adp, dadp)], st.occupancy + sign * docc)
+        f = calc.calculate(st.dtdf, precision=FP64)["f"]
+        return np.sum((np.conj(st.dtdf) * f).real)
+
+    fd = (target(1) - target(-1)) / 2
+    an = np.sum(r["d_xyz"] * dx) + sum(np.dot(g, b) for g, b in zip(r["d_adp"], dadp)) + np.dot(r["d_occ"], docc)
+    assert abs(fd - an) < 1e-7 * max(abs(an), 1e-3)
+
+
+def test_single_atom_single_reflection(engine):
+    st = W.small_case("P1", n_atoms=1, stol_max=0.3, seed=23)
+    st.hkl, st.dtdf = st.hkl[:1], st.dtdf[:1]
+    o = O.compute(st)
+    for prec in (FP64, FP32):
+        r = api.HcCalculator(engine, st).calculate(st.dtdf, precision=prec)
+        check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
+
+
+def test_all_atoms_excluded_gives_zero(engine):
+    st = W.small_case("P21", n_atoms=3, stol_max=0.4, seed=24)
+    calc = api.HcCalculator(engine, st)
+    r = calc.calculate(st.dtdf, precision=FP64, include=np.zeros(3, dtype=np.int32))
+    assert np.all(r["f"] == 0) and np.all(r["d_xyz"] == 0) and np.all(r["d_occ"] == 0)
+    # and back on: the mask is per call
+    r2 = calc.calculate(st.dtdf, precision=FP64)
+    assert np.sum(np.abs(r2["f"])) > 0
+
+
+def test_reflection_set_change_and_repeat(engine):
+    st = W.small_case("P21/c", n_atoms=4, stol_max=0.5, seed=25)
+    calc = api.HcCalculator(engine, st)
+    a = calc.calculate(st.dtdf, precision=FP64)
+    sub = slice(0, st.n_hkl // 3)
+    r = calc.calculate_structure_factors_and_derivatives(st.xyz, st.adp, st.occupancy, st.hkl[sub], st.dtdf[sub])
+    st2 = copy.deepcopy(st)
+    st2.hkl, st2.dtdf = st.hkl[sub], st.dtdf[sub]
+    o = O.compute(st2)
+    check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], FP64)
+    calc.set_hkl(st.hkl)
+    b = calc.calculate(st.dtdf, precision=FP64)
+    assert rel_f(b["f"], a["f"]) < 1e-15
+
+
+def test_invalid_model_is_rejected(engine):
+    st = W.small_case("P1", n_atoms=2, stol_max=0.3, seed=26)
+    st.atom_type = np.array([0, 7], dtype=np.int32)
+    with pytest.raises(api.DsfError):
+        api.HcCalculator(engine, st)

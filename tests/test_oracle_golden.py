@@ -1,0 +1,68 @@
+"""The CPU oracle against the reference's own outputs (golden fixtures
+written by tests/golden/make_golden.py from the reference build)."""
+import numpy as np
+import pytest
+
+from conftest import fixture_names, load_fixture, rel_f, rel_norm, ref_adp_list
+from oracle import oracle as O
+
+HC = [n for n in fixture_names("hc_")]
+
+
+@pytest.mark.parametrize("name", HC)
+def test_hc_oracle_matches_reference(name):
+    st, d = load_fixture(name)
+    r = O.compute(st, n_threads=2)
+    assert rel_f(r["f"], d["ref_f"]) < 1e-12
+    assert rel_norm(r["d_xyz"], d["ref_d_xyz"]) < 1e-11
+    assert rel_norm(r["d_adp"], ref_adp_list(st, d)) < 1e-11
+    assert rel_norm(r["d_occ"], d["ref_d_occ"]) < 1e-11
+
+
+def test_multipole_derivatives_match_reference_finite_differences():
+    st, d = load_fixture("hc_multipole_fd")
+    r = O.compute(st, n_threads=2, multipoles=True)
+    assert rel_norm(r["d_pval"], d["ref_d_pval"]) < 1e-8
+    assert rel_norm(r["d_plm"], d["ref_d_plm"]) < 1e-8
+    assert rel_norm(r["d_kappa"], d["ref_d_kappa"]) < 1e-6
+    assert rel_norm(r["d_kappa_p"], d["ref_d_kappa_p"]) < 1e-6
+
+
+def iam_dict(d):
+    return dict(ngauss=d["iam_ngauss"], a=d["iam_a"], b=d["iam_b"], c=d["iam_c"])
+
+
+def test_iam_oracle_matches_reference():
+    st, d = load_fixture("iam_it92")
+    r = O.compute(st, model="iam", iam=iam_dict(d), n_threads=2)
+    assert rel_f(r["f"], d["ref_f"]) < 1e-12
+    assert rel_norm(r["d_xyz"], d["ref_d_xyz"]) < 1e-11
+    assert rel_norm(r["d_adp"], ref_adp_list(st, d)) < 1e-11
+    assert rel_norm(r["d_occ"], d["ref_d_occ"]) < 1e-11
+
+
+def table_all_ops(st, d):
+    """[hkl][op][atom] over all operations from the (rotated index -> f) map"""
+    lut = {tuple(k): v for k, v in zip(d["table_keys"], d["table_values"])}
+    t = np.zeros((st.n_hkl, st.sg.n_total, st.n_atoms), dtype=complex)
+    for i, h in enumerate(st.hkl):
+        for s, r_ in enumerate(st.sg.rot):
+            t[i, s] = lut[tuple(int(v) for v in h @ r_)]
+    return t
+
+
+def test_tabulated_oracle_matches_reference():
+    st, d = load_fixture("table_p21c")
+    r = O.compute(st, model="table", table=table_all_ops(st, d), n_threads=2)
+    assert rel_f(r["f"], d["ref_f"]) < 1e-12
+    assert rel_norm(r["d_xyz"], d["ref_d_xyz"]) < 1e-11
+    assert rel_norm(r["d_adp"], ref_adp_list(st, d)) < 1e-11
+    assert rel_norm(r["d_occ"], d["ref_d_occ"]) < 1e-11
+
+
+def test_oracle_is_deterministic_across_thread_counts():
+    st, d = load_fixture("hc_config0")
+    a = O.compute(st, n_threads=1)
+    b = O.compute(st, n_threads=3)
+    assert rel_f(a["f"], b["f"]) < 1e-15
+    assert rel_norm(a["d_xyz"], b["d_xyz"]) < 1e-13
