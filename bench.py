@@ -1,0 +1,307 @@
+#!/usr/bin/env python
+"""Benchmark of the structure-factor + derivative path on GB300.
+
+Workload (config 1 of the benchmark set): 5,000 atoms in protein ratios,
+P2_1 2_1 2_1 (4 operations), cell 60 x 70 x 80 A, all 54,704 unique
+reflections with d >= 1.5 A, isotropic B ~ U(10,40), Hansen-Coppens
+multipoles to l = 4 on 150 shared types; F plus dT/d(xyz, B, occupancy)
+from a complex N(0,1) dT/dF.  Seeded synthetic data (no dataset exists).
+
+One step = one SF + derivative pass over that reflection set.  Metric:
+atom x symop x hkl terms per second (symops = point-group order without
+centering).  ``value`` is the FP32-bulk form with inputs resident in HBM
+(device path); ``e2e`` is the same through the host-buffer C ABI call with
+the step's inputs (atomic parameters, dT/dF) copied from pinned host memory
+and F + derivatives copied back inside the timed region.  The plain FP64
+form is timed beside it (``fp64``).  L2 (129 MB) is flushed by writing a
+256 MB buffer between timed steps (outside the timed events).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+``--impl reference``: the reference engine's CPU algorithm timed on the
+host cores (the reference sources are absent on the GPU host, so the
+oracle's C restatement of it runs, OpenMP over all host threads), each step
+a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+FLOPS_PER_TERM_CONFIG1 = 94  # phase 6 + multipole forward 60 + 1 + f*e*T 8 + accumulate 4 + adjoint 6 + xyz 6 + B 2 + occ 1
+WORKLOAD = "config1: HC multipoles l<=4, 5000 atoms (150 types), P212121, 54704 hkl d>=1.5A, iso B, dF/d(xyz,B,occ)"
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sm.append(float(p[1]))
+                    mx.append(float(p[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def fp32_peak_tflops(device):
+    import ctypes
+    from discamb_gb300.build import PEAK_LIB
+    lib = ctypes.CDLL(PEAK_LIB)
+    out = ctypes.c_double(0)
+    if lib.dsf_probe_fp32_tflops(device, ctypes.byref(out)) != 0:
+        return None
+    return out.value
+
+
+def cpu_baseline(st, sample_frac, threads):
+    """The reference engine's algorithm on the host cores (oracle port)."""
+    from oracle import oracle as O
+    m = max(1, int(st.n_hkl * sample_frac))
+    sel = np.arange(m)
+    t0 = time.perf_counter()
+    O.compute(st, hkl_subset=sel, n_threads=threads)
+    dt = time.perf_counter() - t0
+    terms = st.n_atoms * st.sg.point_group_order * m
+    return terms / dt, dt, m
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from discamb_gb300 import workloads as W
+    st = W.config1()
+    threads = os.cpu_count() or 1
+    frac = args.reference_sample
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt, m = cpu_baseline(st, frac, threads)
+        if i >= args.warmup:
+            vals.append((v, dt))
+    value = statistics.median(v for v, _ in vals)
+    ms = statistics.median(dt for _, dt in vals) * 1e3
+    line = {"metric": "atom*symop*hkl terms/s (SF+grad)", "value": value, "unit": "terms/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "sample": f"first {frac:.0%} of the reflections per step"},
+            "cpu_baseline": {"value": value, "unit": "terms/s", "cores": threads, "kind": "port",
+                             "sample": f"config1 atoms x first {int(st.n_hkl * frac)} reflections per step"},
+            "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+    from discamb_gb300 import api, build, workloads as W
+    build.build()
+    st = W.config1(seed=1 + rank)
+    eng = api.Engine(device)
+    calc = api.HcCalculator(eng, st)
+    n_hkl, n = st.n_hkl, st.n_atoms
+    terms = st.terms()
+    dev = torch.device("cuda", device)
+    # a dedicated stream: the engine launches on it, the CUDA events record on it
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    sptr = stream.cuda_stream
+    assert sptr != 0
+    dtdf = torch.tensor(np.stack([st.dtdf.real, st.dtdf.imag], 1), dtype=torch.float64, device=dev).contiguous()
+    f = torch.empty(n_hkl, 2, dtype=torch.float64, device=dev)
+    g = {k: torch.empty(n, w, dtype=torch.float64, device=dev) for k, w in (("d_xyz", 3), ("d_adp", 6), ("d_occ", 1))}
+    outs = {"f": f.data_ptr(), "d_xyz": g["d_xyz"].data_ptr(), "d_adp": g["d_adp"].data_ptr(),
+            "d_occ": g["d_occ"].data_ptr()}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed_device(prec, steps, warmup):
+        for _ in range(warmup):
+            calc.calculate_device(dtdf.data_ptr(), outs, precision=prec, stream=sptr)
+        torch.cuda.synchronize(dev)
+        barrier()
+        torch.cuda.synchronize(dev)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        kern = []
+        launches = 0
+        t0 = time.perf_counter()
+        for i in range(steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            calc.calculate_device(dtdf.data_ptr(), outs, precision=prec, stream=sptr)
+            ev[i][1].record(stream)
+            launches += calc.last_launch_count()
+            stream.synchronize()
+            kern.append(calc.last_kernel_ms())
+        torch.cuda.synchronize(dev)
+        barrier()
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        step_ms = [a.elapsed_time(b) for a, b in ev]
+        return step_ms, kern, launches, wall
+
+    with ClockSampler(device) as clk:
+        ms32, kern32, launches32, wall32 = timed_device(api.DSF_FP32_BULK, args.steps, args.warmup)
+    clocks = clk.summary()
+    ms64, kern64, _, _ = timed_device(api.DSF_FP64, max(2, min(args.steps, 3)), 1)
+
+    # end to end through the host-buffer ABI call, pinned host memory
+    xyz_h = torch.from_numpy(st.xyz.copy()).pin_memory()
+    adp_h = torch.from_numpy(st.adp_array()).pin_memory()
+    occ_h = torch.from_numpy(st.occupancy.copy()).pin_memory()
+    for _ in range(args.warmup):
+        calc.update_atoms(xyz_h.numpy(), adp_h.numpy(), occ_h.numpy())
+        r = calc.calculate(st.dtdf, precision=api.DSF_FP32_BULK)
+    e2e = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        calc.update_atoms(xyz_h.numpy(), adp_h.numpy(), occ_h.numpy())
+        r = calc.calculate(st.dtdf, precision=api.DSF_FP32_BULK)
+        e2e.append(time.perf_counter() - t0)
+    h2d = 80 * n + 16 * n_hkl
+    d2h = 16 * n_hkl + (3 + 6 + 1) * 8 * n
+
+    step32 = statistics.mean(ms32)
+    step64 = statistics.mean(ms64)
+    k32 = statistics.mean(kern32)
+    # weak scaling: every rank runs its own replica; max time over ranks
+    tot = torch.tensor([step32, statistics.mean(e2e) * 1e3, k32], dtype=torch.float64, device=dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
+    step32, e2e_ms, k32 = tot.tolist()
+    value = world * terms / (step32 * 1e-3)
+    if rank != 0:
+        return 0
+    achieved = FLOPS_PER_TERM_CONFIG1 * terms / (k32 * 1e-3) * 1e-12
+    peak = fp32_peak_tflops(device)
+    cpu_v, cpu_dt, cpu_m = cpu_baseline(st, args.cpu_sample, os.cpu_count() or 1)
+    mp = measured_peaks()
+    line = {
+        "metric": "atom*symop*hkl terms/s (SF+grad)", "value": value, "unit": "terms/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step32, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk (integer phase reduction, f64 accumulation)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "terms_per_step": terms, "l2": "flushed (256 MB write) between timed steps",
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+        "fp64": {"value": world * terms / (step64 * 1e-3), "ms_per_step": step64,
+                 "kernel_ms": statistics.mean(kern64), "fp32_over_fp64": step64 / step32},
+        "e2e": {"value": world * terms / (e2e_ms * 1e-3), "unit": "terms/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "peak_source": "FP32 FMA throughput probe measured in this run (MEASURED_PEAKS.json lists "
+                                    "HBM and bf16 tensor peaks only)",
+                     "flops_per_term": FLOPS_PER_TERM_CONFIG1, "kernel_ms": k32,
+                     "hbm_peak_gbs_measured": mp.get("hbm_gbs")},
+        "cpu_baseline": {"value": cpu_v, "unit": "terms/s", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": f"config1 atoms x first {cpu_m} reflections, one call ({cpu_dt:.1f} s)"},
+        "gpu_launches": launches32,
+        "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+        "wall_s_timed_region": wall32,
+    }
+    print(json.dumps(line))
+    calc.close()
+    eng.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=float, default=0.25)
+    ap.add_argument("--reference-sample", type=float, default=0.1)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

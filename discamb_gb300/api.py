@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -104,6 +105,8 @@ def library():
         L.dsf_calculate.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), _P(C.c_int), _P(_Out)]
         L.dsf_calculate_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, _P(_Out), C.c_void_p]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
+        L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
+        L.dsf_last_kernel_ms.restype = C.c_double
     return _lib
 
 
@@ -123,6 +126,7 @@ class Engine:
     def __init__(self, device=0):
         self.lib = library()
         self.h = C.c_void_p()
+        self._calculators = weakref.WeakSet()
         rc = self.lib.dsf_engine_create(int(device), C.byref(self.h))
         if rc != 0:
             raise DsfError(f"dsf_engine_create failed with status {rc}")
@@ -133,6 +137,9 @@ class Engine:
             raise DsfError(f"{what}: status {rc}: {msg.decode() if msg else ''}")
 
     def close(self):
+        """Destroys the engine after every structure created on it."""
+        for c in list(self._calculators):
+            c.close()
         if self.h:
             self.lib.dsf_engine_destroy(self.h)
             self.h = C.c_void_p()
@@ -240,6 +247,7 @@ class _Calculator:
         self.h = C.c_void_p()
         self.n_atoms = st.n_atoms
         self.n_hkl = 0
+        engine._calculators.add(self)
 
     def set_hkl(self, hkl):
         hkl = np.ascontiguousarray(hkl, dtype=np.int32)
@@ -304,6 +312,21 @@ class _Calculator:
 
     def last_launch_count(self):
         return self.lib.dsf_last_launch_count(self.h)
+
+    def last_kernel_ms(self):
+        return self.lib.dsf_last_kernel_ms(self.h)
+
+    def calculate_device(self, dtdf_ptr, outputs, precision=DSF_FP32_BULK, derivatives=("xyz", "adp", "occ"),
+                         multipoles=False, stream=0):
+        """Device-resident call: dtdf_ptr = device pointer to [n_hkl][2]
+        doubles, outputs = dict of device pointers (f required)."""
+        flags = (DSF_D_XYZ if "xyz" in derivatives else 0) | (DSF_D_ADP if "adp" in derivatives else 0) | \
+                (DSF_D_OCC if "occ" in derivatives else 0) | (DSF_D_MULTIPOLE if multipoles else 0)
+        o = _Out()
+        for k, v in outputs.items():
+            setattr(o, k, v)
+        self.engine.check(self.lib.dsf_calculate_device(self.h, int(precision), flags, C.c_void_p(dtdf_ptr),
+                                                        C.byref(o), C.c_void_p(stream)), "calculate_device")
 
     def close(self):
         if self.h:

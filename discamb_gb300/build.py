@@ -15,6 +15,7 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdsf_gb300.so")
+PEAK_LIB = os.path.join(HERE, "libdsf_peak_probe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["dsf_kernels.cu", "dsf_engine.cu"]
 
@@ -63,6 +64,13 @@ def build(force=False, verbose=False, extra_flags=()):
         if r.returncode != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             raise RuntimeError("link failed")
+    src = os.path.join(CSRC, "peak_probe.cu")
+    if force or _stale(PEAK_LIB, [src]):
+        cmd = [nvcc] + ARCH + ["-O3", "-Xcompiler", "-fPIC", "-shared", "-o", PEAK_LIB, src]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            raise RuntimeError("peak probe build failed")
     return LIB
 
 

@@ -36,6 +36,7 @@ using namespace dsf;
 
 struct dsf_engine {
     int device = 0;
+    int live_structures = 0;
     cudaStream_t stream = nullptr;
     int n_sm = 0;
     size_t max_smem = 0;
@@ -185,6 +186,7 @@ struct dsf_structure {
     std::vector<uint8_t> active_host;
     bool have_hkl = false, have_atoms = false;
     int last_launches = 0;
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
     DevStructure dev{};
 };
 
@@ -334,15 +336,17 @@ __global__ void atom_convert_kernel(AtomParams P, const double *raw, const int *
         adp_d[6 * a + i] = 0.0;
         adp_f[6 * a + i] = 0.0f;
     }
+    // FP32 copies carry log2(e) so the kernel can use exp2
+    const double log2e = 1.4426950408889634;
     if (k == 1) {
         adp_d[6 * a] = two_pi2 * r[3];
-        adp_f[6 * a] = (float)(two_pi2 * r[3]);
+        adp_f[6 * a] = (float)(two_pi2 * r[3] * log2e);
     } else if (k == 6) {
         for (int p = 0; p < 6; p++) {
             double s = 0;
             for (int q = 0; q < 6; q++) s += P.A6[6 * p + q] * r[3 + q];
             adp_d[6 * a + p] = two_pi2 * s;
-            adp_f[6 * a + p] = (float)(two_pi2 * s);
+            adp_f[6 * a + p] = (float)(two_pi2 * s * log2e);
         }
     }
     const double wt = r[9] * mult_w[a];
@@ -777,6 +781,7 @@ int dsf_engine_create(int device, dsf_engine **out)
 int dsf_engine_destroy(dsf_engine *e)
 {
     if (!e) return DSF_ERR_ARGUMENT;
+    if (e->live_structures > 0) return fail(e, DSF_ERR_STATE, "engine still owns structures; destroy them first");
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
@@ -852,6 +857,7 @@ int dsf_structure_create_hc(dsf_engine *e, const dsf_symmetry *sym, const dsf_hc
     if ((rc = build_tiles(s, true))) return bail(rc);
     if ((rc = compute_global_plm(s))) return bail(rc);
     if ((rc = finish_create(e, s))) return bail(rc);
+    e->live_structures++;
     *out = s;
     return DSF_OK;
 }
@@ -888,6 +894,7 @@ int dsf_structure_create_iam(dsf_engine *e, const dsf_symmetry *sym, const dsf_i
         if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return bail(rc);
     }
     if ((rc = finish_create(e, s))) return bail(rc);
+    e->live_structures++;
     *out = s;
     return DSF_OK;
 }
@@ -928,7 +935,8 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
         if ((rc = upload(e, s->d_table_f, tf.data(), tf.size()))) return bail(rc);
     }
     if ((rc = finish_create(e, s))) return bail(rc);
-    if ((rc = dsf_structure_set_hkl(s, n_hkl, hkl))) return bail(rc);
+    s->eng->live_structures++;
+    if ((rc = dsf_structure_set_hkl(s, n_hkl, hkl))) { s->eng->live_structures--; return bail(rc); }
     *out = s;
     return DSF_OK;
 }
@@ -945,6 +953,9 @@ int dsf_structure_destroy(dsf_structure *s)
                       &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw, &s->d_dmat, &s->d_raw,
                       &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc, &s->d_out, &s->d_plm_lmax};
     for (DevBuf *b : bufs) b->release();
+    if (s->ev_begin) cudaEventDestroy(s->ev_begin);
+    if (s->ev_end) cudaEventDestroy(s->ev_end);
+    s->eng->live_structures--;
     delete s;
     return DSF_OK;
 }
@@ -1086,6 +1097,18 @@ int64_t dsf_structure_device_bytes(const dsf_structure *s)
 
 int dsf_last_launch_count(const dsf_structure *s) { return s ? s->last_launches : 0; }
 
+double dsf_last_kernel_ms(dsf_structure *s)
+{
+    if (!s || !s->ev_begin) return -1.0;
+    cudaSetDevice(s->eng->device);
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, s->ev_begin, s->ev_end) != cudaSuccess) {
+        cudaGetLastError();
+        return -1.0;
+    }
+    return (double)ms;
+}
+
 int dsf_calculate_device(dsf_structure *s, int precision, int flags, const double *dtdf_device,
                          const dsf_outputs *out, void *stream)
 {
@@ -1122,7 +1145,13 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     C.gw_f = s->d_gw_f.as<float2>();
     C.f_acc = s->d_facc.as<double2>();
     C.g_acc = s->d_gacc.as<double>();
+    if (!s->ev_begin) {
+        DSF_CUDA(cudaEventCreate(&s->ev_begin));
+        DSF_CUDA(cudaEventCreate(&s->ev_end));
+    }
+    DSF_CUDA(cudaEventRecord(s->ev_begin, st));
     DSF_CUDA(launch_sf_grad(s->dev, C, fp64, mp, chunk, ht, st));
+    DSF_CUDA(cudaEventRecord(s->ev_end, st));
     launches++;
     f_epilogue_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, s->d_facc.as<double2>(), s->d_hmult.as<double>(),
                                                            s->d_cinv.as<double2>(), s->centro_mode, out->f);

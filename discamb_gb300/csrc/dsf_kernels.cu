@@ -21,7 +21,7 @@
 // R = double: the plain form, FP64 throughout.
 // R = float : the FP32-bulk form.  Phases are reduced exactly in integer
 // arithmetic (fractional coordinates as 2^32 fixed point, integer h', h.t
-// from integer translations in 1/12) so no FP64 is needed per term; F and
+// from integer translations in 1/24) so no FP64 is needed per term; F and
 // derivative sums over blocks are FP64, and each thread folds its FP32
 // derivative sums into FP64 registers after every sub-tile of reflections.
 #include "dsf_device.cuh"
@@ -39,14 +39,37 @@ struct Vec2<double> { using T = double2; };
 template <typename R>
 __device__ __forceinline__ void sincos2pi(R phase, R *s, R *c);
 template <>
-__device__ __forceinline__ void sincos2pi<float>(float phase, float *s, float *c)
-{
-    __sincosf(6.283185307179586f * phase, s, c);
-}
-template <>
 __device__ __forceinline__ void sincos2pi<double>(double phase, double *s, double *c)
 {
     sincospi(2.0 * phase, s, c);
+}
+
+// sin and cos of 2 pi (P 2^-32 + lo) for a phase P in 2^32 fixed point (the
+// exact integer reduction mod one turn) and a small FP32 remainder lo (in
+// turns).  Quadrant from the two top bits, remainder angle in [-pi/4, pi/4]
+// exact in FP32 up to rounding, Taylor polynomials to degree 9 (sin) and 8
+// (cos): truncation below 3e-8, so the result is limited by FP32 rounding
+// (~1e-7 absolute) instead of the ~1e-6 of the hardware approximation.
+__device__ __forceinline__ void sincos_fixed(uint32_t P, float lo, float *sn, float *cs)
+{
+    const uint32_t q = (P + 0x20000000u) >> 30;
+    const int32_t r = (int32_t)(P - (q << 30));
+    const float th = fmaf((float)r, 1.4629180792671596e-09f, 6.283185307179586f * lo);
+    const float t2 = th * th;
+    float sp = fmaf(t2, 2.7557319e-06f, -1.9841270e-04f);
+    sp = fmaf(t2, sp, 8.3333333e-03f);
+    sp = fmaf(t2, sp, -1.6666667e-01f);
+    const float sv = fmaf(th * t2, sp, th);
+    float cp = fmaf(t2, 2.4801587e-05f, -1.3888889e-03f);
+    cp = fmaf(t2, cp, 4.1666668e-02f);
+    cp = fmaf(t2, cp, -0.5f);
+    const float cv = fmaf(t2, cp, 1.0f);
+    float ss = (q & 1u) ? cv : sv;
+    float cc = (q & 1u) ? sv : cv;
+    if (q & 2u) ss = -ss;
+    if ((q + 1u) & 2u) cc = -cc;
+    *sn = ss;
+    *cs = cc;
 }
 
 template <typename R>
@@ -55,6 +78,15 @@ template <>
 __device__ __forceinline__ float exp_<float>(float x) { return __expf(x); }
 template <>
 __device__ __forceinline__ double exp_<double>(double x) { return exp(x); }
+
+// temperature factor from the exponent of the ADP quadratic form: FP64 exp;
+// FP32 exp2 (the FP32 ADPs are stored multiplied by log2 e)
+template <typename R>
+__device__ __forceinline__ R texp(R x);
+template <>
+__device__ __forceinline__ float texp<float>(float x) { return exp2f(x); }
+template <>
+__device__ __forceinline__ double texp<double>(double x) { return exp(x); }
 
 template <typename R>
 __device__ __forceinline__ R shfl_xor(R v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
@@ -171,6 +203,7 @@ sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
         }
     }
     const bool table_model = S.model == MODEL_TABLE;
+    const bool hc_model = S.model == MODEL_HC;
     const int a_orig = have ? S.atom_orig[a] : 0;
 
     // FP64 derivative totals
@@ -242,7 +275,7 @@ sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
                 const R fsre = rad[0] + anre, fsim = anim;
                 const R r0 = rad[1], r1 = rad[2], r2 = rad[3], r3 = rad[4], r4 = rad[5];
                 R Tiso = R(1);
-                if (adpk == 1) Tiso = exp_<R>(-adp[0] * sH2[hl]);
+                if (adpk == 1) Tiso = texp<R>(-adp[0] * sH2[hl]);
                 // adjoint weight with the isotropic factor folded in (used inside the loop)
                 const R gre = g.x * Tiso, gim = g.y * Tiso;
                 R Ure = 0, Uim = 0;
@@ -260,9 +293,7 @@ sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
                         const int i0 = (int)h0f, i1 = (int)h1f, i2 = (int)h2f;
                         const uint32_t P = (uint32_t)i0 * xq0 + (uint32_t)i1 * xq1 + (uint32_t)i2 * xq2 +
                                            sTq[hl * nS + s];
-                        const float ph = (float)(int32_t)P * 2.3283064365386963e-10f +
-                                         (h0f * x0 + h1f * x1 + h2f * x2);
-                        sincos2pi<R>(ph, &sn, &cs);
+                        sincos_fixed(P, h0f * x0 + h1f * x1 + h2f * x2, &sn, &cs);
                     } else {
                         double ph = h0f * x0 + h1f * x1 + h2f * x2 + sTd[hl * nS + s];
                         ph -= rint(ph);
@@ -275,7 +306,7 @@ sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
                         m6[3] = R(2) * h0f * h1f; m6[4] = R(2) * h0f * h2f; m6[5] = R(2) * h1f * h2f;
                         const R q = adp[0] * m6[0] + adp[1] * m6[1] + adp[2] * m6[2] + adp[3] * m6[3] +
                                     adp[4] * m6[4] + adp[5] * m6[5];
-                        const R T = exp_<R>(-q);
+                        const R T = texp<R>(-q);
                         zre *= T; zim *= T;
                     }
                     R fre, fim;
@@ -289,7 +320,7 @@ sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
                             const double2 tv = S.table_d[((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig];
                             fre = tv.x + anre; fim = tv.y + anim;
                         }
-                    } else {
+                    } else if (hc_model) {
                         A0 = pg[0] * y[0];
                         A1 = pg[1] * y[1] + pg[2] * y[2] + pg[3] * y[3];
                         A2 = pg[4] * y[4] + pg[5] * y[5] + pg[6] * y[6] + pg[7] * y[7] + pg[8] * y[8];
@@ -299,6 +330,9 @@ sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
                              pg[21] * y[21] + pg[22] * y[22] + pg[23] * y[23] + pg[24] * y[24];
                         fre = fsre + r0 * A0 + r2 * A2 + r4 * A4;
                         fim = fsim + r1 * A1 + r3 * A3;
+                    } else {
+                        fre = fsre;
+                        fim = fsim;
                     }
                     const R ure = fre * zre - fim * zim;
                     const R uim = fre * zim + fim * zre;
@@ -311,6 +345,7 @@ sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
                         for (int k = 0; k < 6; k++) { Are[k] -= m6[k] * ure; Aim[k] -= m6[k] * uim; }
                     }
                     if constexpr (MP) {
+                      if (hc_model) {
                         Ere += zre; Eim += zim;
                         // q_l = Re(g i^l rr_l z): even l rs_l Re(gz), odd l -rs_l Im(gz)
                         const R wre = gre * zre - gim * zim, wim = gre * zim + gim * zre;
@@ -328,6 +363,7 @@ sf_grad_kernel(DevStructure S, CallBuffers C, int hkl_chunk, int ht)
                         const R dim = rad[9] * A1 + rad[11] * A3;
                         Kre += dre * zre - dim * zim;
                         Kim += dre * zim + dim * zre;
+                      }
                     }
                 }
                 if (adpk == 1) {

@@ -183,6 +183,10 @@ int dsf_calculate_device(dsf_structure *s, int precision, int derivative_flags, 
 
 /* number of kernel launches issued by the last calculation (for accounting) */
 int dsf_last_launch_count(const dsf_structure *s);
+/* device time [ms] of the fused SF+adjoint kernel of the last calculation,
+ * from CUDA events recorded around it on its launch stream; -1 while that
+ * stream has not finished it */
+double dsf_last_kernel_ms(dsf_structure *s);
 
 #ifdef __cplusplus
 }
