@@ -34,6 +34,20 @@ size_t sf_grad_smem_bytes(bool fp64, int ht, int n_sym);
 
 using namespace dsf;
 
+namespace {
+// host record of one atom type (HC or IAM)
+struct TypeHost {
+    double pv = 0, kappa = 1, kappa_p = 1, zeta = 1;
+    double norm[5] = {0, 0, 0, 0, 0};  // density normalisation of the deformation radial functions
+    int npow[5] = {0, 0, 0, 0, 0};
+    int n_def = 0;
+    int lmax_used = -1;
+    int core_begin = 0, core_end = 0, val_begin = 0, val_end = 0;
+    int iam_n = 0;
+    double iam_a[5] = {0, 0, 0, 0, 0}, iam_b[5] = {0, 0, 0, 0, 0}, iam_c = 0;
+};
+}  // namespace
+
 struct dsf_engine {
     int device = 0;
     int live_structures = 0;
@@ -174,14 +188,14 @@ struct dsf_structure {
     std::vector<double> mult_w, anom, lcs;
     std::vector<int> type_nl, type_wfn;
     std::vector<double> type_plm, type_pval, type_kappa, type_kappa_p;
-    std::vector<TypeRadial> trad;
+    std::vector<TypeHost> trad;
     std::vector<double> tcoeff, texp;
     std::vector<int> tpow;
     std::vector<double> dmat;  // [n_atoms][165] D_l blocks (sorted order)
     // device
     DevBuf d_sym_rot, d_sym_t24, d_tile_begin, d_tile_ntypes, d_tile_types, d_atom_ltype, d_atom_adpk,
         d_active, d_xq, d_xlo, d_xd, d_adp_f, d_adp_d, d_w_f, d_w_d, d_anom_f, d_anom_d, d_pg_f, d_pg_d, d_types,
-        d_tcoeff, d_texp, d_tpow, d_hkl, d_h2, d_hmult, d_cinv, d_table_f, d_table_d, d_perm, d_multw, d_dmat,
+        d_types_f, d_tcoeff, d_texp, d_tpow, d_texp_f, d_tpre_f, d_hkl, d_h2, d_h2f, d_hmult, d_cinv, d_table_f, d_table_d, d_perm, d_multw, d_dmat,
         d_raw, d_dtdf, d_gw_d, d_gw_f, d_facc, d_gacc, d_out, d_plm_lmax;
     std::vector<uint8_t> active_host;
     bool have_hkl = false, have_atoms = false;
@@ -542,9 +556,9 @@ int build_type_radial(dsf_structure *s, const dsf_hc_model *m)
 {
     dsf_engine *e = s->eng;
     const int nT = s->n_types;
-    s->trad.assign(nT, TypeRadial{});
+    s->trad.assign(nT, TypeHost{});
     for (int t = 0; t < nT; t++) {
-        TypeRadial &r = s->trad[t];
+        TypeHost &r = s->trad[t];
         r.pv = s->type_pval[t];
         r.kappa = s->type_kappa[t];
         r.kappa_p = s->type_kappa_p[t];
@@ -654,6 +668,56 @@ int build_tiles(dsf_structure *s, bool by_type)
     return DSF_OK;
 }
 
+void refresh_dev(dsf_structure *s);
+
+// per-type constants of the kernels in both precisions (prefactors folded)
+template <typename R>
+TypeRadialT<R> type_constants(const TypeHost &h)
+{
+    TypeRadialT<R> t{};
+    t.pv = R(h.pv);
+    t.inv_kappa = R(1.0 / h.kappa);
+    t.inv_kappa_p = R(1.0 / h.kappa_p);
+    t.zeta = R(h.zeta);
+    t.n_def = h.n_def;
+    for (int l = 0; l < 5; l++) {
+        t.def_m[l] = 0;
+        t.def_pre[l] = R(0);
+        if (l < h.n_def) {
+            const int m = h.npow[l] + 1 - l;
+            const double sgn = (l == 2 || l == 3) ? -1.0 : 1.0;
+            t.def_m[l] = m;
+            t.def_pre[l] = R(sgn * 4.0 * DSF_PI * h.norm[l] * g_prefactor(l, m));
+        }
+    }
+    t.core_begin = h.core_begin;
+    t.core_end = h.core_end;
+    t.val_begin = h.val_begin;
+    t.val_end = h.val_end;
+    t.iam_n = h.iam_n;
+    for (int q = 0; q < 5; q++) {
+        t.iam_a[q] = R(h.iam_a[q]);
+        t.iam_b[q] = R(h.iam_b[q]);
+    }
+    t.iam_c = R(h.iam_c);
+    return t;
+}
+
+int upload_types(dsf_structure *s)
+{
+    std::vector<TypeRadialT<double> > td;
+    std::vector<TypeRadialT<float> > tf;
+    for (const TypeHost &h : s->trad) {
+        td.push_back(type_constants<double>(h));
+        tf.push_back(type_constants<float>(h));
+    }
+    int rc;
+    if ((rc = upload(s->eng, s->d_types, td.data(), td.size()))) return rc;
+    if ((rc = upload(s->eng, s->d_types_f, tf.data(), tf.size()))) return rc;
+    refresh_dev(s);
+    return DSF_OK;
+}
+
 void refresh_dev(dsf_structure *s)
 {
     DevStructure &d = s->dev;
@@ -683,12 +747,17 @@ void refresh_dev(dsf_structure *s)
     d.atom_anom_d = s->d_anom_d.as<double2>();
     d.atom_pg_f = s->d_pg_f.as<float>();
     d.atom_pg_d = s->d_pg_d.as<double>();
-    d.types = s->d_types.as<TypeRadial>();
-    d.term_coeff = s->d_tcoeff.as<double>();
-    d.term_exp = s->d_texp.as<double>();
-    d.term_pow = s->d_tpow.as<int>();
+    for (int i = 0; i < 9; i++) d.Bf[i] = (float)s->B[i];
+    d.types_d = s->d_types.as<TypeRadialT<double> >();
+    d.types_f = s->d_types_f.as<TypeRadialT<float> >();
+    d.term_pre_d = s->d_tcoeff.as<double>();
+    d.term_pre_f = s->d_tpre_f.as<float>();
+    d.term_exp_d = s->d_texp.as<double>();
+    d.term_exp_f = s->d_texp_f.as<float>();
+    d.term_m = s->d_tpow.as<int>();
     d.hkl = s->d_hkl.as<int4>();
     d.h2 = s->d_h2.as<double>();
+    d.h2f = s->d_h2f.as<float>();
     d.table_f = s->d_table_f.as<float2>();
     d.table_d = s->d_table_d.as<double2>();
     d.atom_orig = s->d_perm.as<int>();
@@ -743,7 +812,7 @@ int finish_create(dsf_engine *e, dsf_structure *s)
     int rc;
     if ((rc = upload(e, s->d_sym_rot, s->sym_rot.data(), s->sym_rot.size()))) return rc;
     if ((rc = upload(e, s->d_sym_t24, s->sym_t24.data(), s->sym_t24.size()))) return rc;
-    if ((rc = upload(e, s->d_types, s->trad.data(), s->trad.size()))) return rc;
+    if ((rc = upload_types(s))) return rc;
     refresh_dev(s);
     DSF_CUDA(cudaStreamSynchronize(e->stream));
     return DSF_OK;
@@ -851,9 +920,24 @@ int dsf_structure_create_hc(dsf_engine *e, const dsf_symmetry *sym, const dsf_hc
         s->trad[t].val_begin = ncore + m->val_offset[w];
         s->trad[t].val_end = ncore + m->val_offset[w + 1];
     }
-    if ((rc = upload(e, s->d_tcoeff, s->tcoeff.data(), s->tcoeff.size()))) return bail(rc);
-    if ((rc = upload(e, s->d_texp, s->texp.data(), s->texp.size()))) return bail(rc);
-    if ((rc = upload(e, s->d_tpow, s->tpow.data(), s->tpow.size()))) return bail(rc);
+    {
+        // the kernels evaluate 4 pi c G(n,0) as pre * core with pre = 4 pi c m!, m = n - 1 = pow + 1
+        const size_t nt = s->tcoeff.size();
+        std::vector<double> pre(nt);
+        std::vector<float> pref(nt), zf(nt);
+        std::vector<int> mm(nt);
+        for (size_t q = 0; q < nt; q++) {
+            mm[q] = s->tpow[q] + 1;
+            pre[q] = 4.0 * DSF_PI * s->tcoeff[q] * g_prefactor(0, mm[q]);
+            pref[q] = (float)pre[q];
+            zf[q] = (float)s->texp[q];
+        }
+        if ((rc = upload(e, s->d_tcoeff, pre.data(), nt))) return bail(rc);
+        if ((rc = upload(e, s->d_tpre_f, pref.data(), nt))) return bail(rc);
+        if ((rc = upload(e, s->d_texp, s->texp.data(), nt))) return bail(rc);
+        if ((rc = upload(e, s->d_texp_f, zf.data(), nt))) return bail(rc);
+        if ((rc = upload(e, s->d_tpow, mm.data(), nt))) return bail(rc);
+    }
     if ((rc = build_tiles(s, true))) return bail(rc);
     if ((rc = compute_global_plm(s))) return bail(rc);
     if ((rc = finish_create(e, s))) return bail(rc);
@@ -871,9 +955,9 @@ int dsf_structure_create_iam(dsf_engine *e, const dsf_symmetry *sym, const dsf_i
     auto bail = [&](int code) { delete s; return code; };
     if (!m || m->n_types < 1) return bail(fail(e, DSF_ERR_ARGUMENT, "IAM model needs types"));
     s->n_types = m->n_types;
-    s->trad.assign(m->n_types, TypeRadial{});
+    s->trad.assign(m->n_types, TypeHost{});
     for (int t = 0; t < m->n_types; t++) {
-        TypeRadial &r = s->trad[t];
+        TypeHost &r = s->trad[t];
         r.lmax_used = -1;
         r.iam_n = m->n_gauss[t];
         if (r.iam_n < 0 || r.iam_n > 5) return bail(fail(e, DSF_ERR_ARGUMENT, "at most 5 Gaussians per IAM type"));
@@ -910,7 +994,7 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
     auto bail = [&](int code) { delete s; return code; };
     if (!table || n_hkl < 1) return bail(fail(e, DSF_ERR_ARGUMENT, "tabulated model needs a table and reflections"));
     s->n_types = 1;
-    s->trad.assign(1, TypeRadial{});
+    s->trad.assign(1, TypeHost{});
     s->trad[0].lmax_used = -1;
     if ((rc = build_tiles(s, false))) return bail(rc);
     std::vector<double> z(25 * (size_t)s->n_atoms, 0.0);
@@ -949,7 +1033,7 @@ int dsf_structure_destroy(dsf_structure *s)
     DevBuf *bufs[] = {&s->d_sym_rot, &s->d_sym_t24, &s->d_tile_begin, &s->d_tile_ntypes, &s->d_tile_types,
                       &s->d_atom_ltype, &s->d_atom_adpk, &s->d_active, &s->d_xq, &s->d_xlo, &s->d_xd, &s->d_adp_f,
                       &s->d_adp_d, &s->d_w_f, &s->d_w_d, &s->d_anom_f, &s->d_anom_d, &s->d_pg_f, &s->d_pg_d,
-                      &s->d_types, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_hkl, &s->d_h2, &s->d_hmult,
+                      &s->d_types, &s->d_types_f, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_texp_f, &s->d_tpre_f, &s->d_hkl, &s->d_h2, &s->d_h2f, &s->d_hmult,
                       &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw, &s->d_dmat, &s->d_raw,
                       &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc, &s->d_out, &s->d_plm_lmax};
     for (DevBuf *b : bufs) b->release();
@@ -990,6 +1074,10 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
     int rc;
     if ((rc = upload(e, s->d_hkl, h4.data(), h4.size()))) return rc;
     if ((rc = upload(e, s->d_h2, h2.data(), h2.size()))) return rc;
+    {
+        std::vector<float> h2f(h2.begin(), h2.end());
+        if ((rc = upload(e, s->d_h2f, h2f.data(), h2f.size()))) return rc;
+    }
     if ((rc = upload(e, s->d_hmult, mult.data(), mult.size()))) return rc;
     if ((rc = upload(e, s->d_cinv, cinv.data(), cinv.size()))) return rc;
     DSF_CUDA(s->d_dtdf.alloc(16 * (size_t)n_hkl));
@@ -1048,7 +1136,7 @@ int dsf_structure_update_types(dsf_structure *s, const double *plm, const double
     if (kappa) s->type_kappa.assign(kappa, kappa + nT);
     if (kappa_p) s->type_kappa_p.assign(kappa_p, kappa_p + nT);
     for (int t = 0; t < nT; t++) {
-        TypeRadial &r = s->trad[t];
+        TypeHost &r = s->trad[t];
         r.pv = s->type_pval[t];
         r.kappa = s->type_kappa[t];
         r.kappa_p = s->type_kappa_p[t];
@@ -1059,7 +1147,7 @@ int dsf_structure_update_types(dsf_structure *s, const double *plm, const double
         r.lmax_used = std::min(lp, std::min(4, r.n_def - 1));
     }
     int rc;
-    if ((rc = upload(e, s->d_types, s->trad.data(), s->trad.size()))) return rc;
+    if ((rc = upload_types(s))) return rc;
     if (plm && (rc = compute_global_plm(s))) return rc;
     refresh_dev(s);
     DSF_CUDA(cudaStreamSynchronize(e->stream));
@@ -1086,7 +1174,7 @@ int64_t dsf_structure_device_bytes(const dsf_structure *s)
     const DevBuf *bufs[] = {&s->d_sym_rot, &s->d_sym_t24, &s->d_tile_begin, &s->d_tile_ntypes, &s->d_tile_types,
                             &s->d_atom_ltype, &s->d_atom_adpk, &s->d_active, &s->d_xq, &s->d_xlo, &s->d_xd,
                             &s->d_adp_f, &s->d_adp_d, &s->d_w_f, &s->d_w_d, &s->d_anom_f, &s->d_anom_d, &s->d_pg_f,
-                            &s->d_pg_d, &s->d_types, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_hkl, &s->d_h2,
+                            &s->d_pg_d, &s->d_types, &s->d_types_f, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_texp_f, &s->d_tpre_f, &s->d_hkl, &s->d_h2, &s->d_h2f,
                             &s->d_hmult, &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw,
                             &s->d_dmat, &s->d_raw, &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc,
                             &s->d_out, &s->d_plm_lmax};

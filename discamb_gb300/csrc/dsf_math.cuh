@@ -118,6 +118,40 @@ DSF_HD R gfun_dk(int l, int n, R K, R Z)
     return v;
 }
 
+// s^l C_m^{(l+1)}(c) / rho^{l+m+2}: G(n,l,K,Z) without its constant
+// prefactor 2^l l! m!, n = l + m + 1.  No division (reciprocals of k from a
+// small table), so the FP32 form runs on the FP32 pipe only.
+__device__ __constant__ float kInvF[13] = {0.f, 1.f, 0.5f, 0.33333334f, 0.25f, 0.2f, 0.16666667f, 0.14285715f,
+                                           0.125f, 0.11111111f, 0.1f, 0.09090909f, 0.083333336f};
+__device__ __constant__ double kInvD[13] = {0.0, 1.0, 0.5, 1.0 / 3, 0.25, 0.2, 1.0 / 6, 1.0 / 7, 0.125, 1.0 / 9, 0.1,
+                                            1.0 / 11, 1.0 / 12};
+
+template <typename R>
+__device__ __forceinline__ R inv_k(int k);
+template <>
+__device__ __forceinline__ float inv_k<float>(int k) { return kInvF[k]; }
+template <>
+__device__ __forceinline__ double inv_k<double>(int k) { return kInvD[k]; }
+
+template <typename R>
+__device__ __forceinline__ R gcore(int l, int m, R K, R Z)
+{
+    const R irho = rsqrt_<R>(Z * Z + K * K);
+    const R c = Z * irho, s = K * irho;
+    R c0 = R(1), c1 = R(2 * (l + 1)) * c;
+    R cm = m == 0 ? R(1) : c1;
+    for (int k = 2; k <= m; k++) {
+        const R c2 = (R(2 * (k + l)) * c * c1 - R(k + 2 * l) * c0) * inv_k<R>(k);
+        c0 = c1;
+        c1 = c2;
+    }
+    if (m >= 2) cm = c1;
+    R p = irho * irho;
+    for (int k = 0; k < l + m; k++) p *= irho;
+    for (int k = 0; k < l; k++) p *= s;
+    return cm * p;
+}
+
 template <typename R>
 struct cx {
     R re, im;
