@@ -820,6 +820,47 @@ int finish_create(dsf_engine *e, dsf_structure *s)
 
 }  // namespace
 
+// Launch helpers of the per-call kernels, for the allocation-free entry
+// point (dsf_noalloc.cu), which runs them on caller-provided buffers.
+namespace dsf {
+void host_cell_matrices(const double *cell, double *M, double *Minv, double *B) { cell_matrices(cell, M, Minv, B); }
+void host_adp_param_map(const double *A, double *A6) { adp_param_map(A, A6); }
+double host_centering_multiplier(char c, int obverse, int h, int k, int l)
+{
+    return centering_multiplier(c, obverse, h, k, l);
+}
+cudaError_t launch_adjoint_weights(int n, const double2 *dtdf, const double *mult, const double2 *cinv, int centro,
+                                   double2 *gw_d, float2 *gw_f, cudaStream_t st)
+{
+    gw_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, dtdf, mult, cinv, centro, gw_d, gw_f);
+    return cudaGetLastError();
+}
+cudaError_t launch_f_epilogue(int n, const double2 *facc, const double *mult, const double2 *cinv, int centro,
+                              double *f_out, cudaStream_t st)
+{
+    f_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, facc, mult, cinv, centro, f_out);
+    return cudaGetLastError();
+}
+cudaError_t launch_grad_epilogue(int n_atoms, int xyz_conv, const double *Minv, const double *A6, int flags,
+                                 const double *g_acc, const int *perm, const int *adpk, const double *w,
+                                 const double *mult_w, const dsf_outputs *out, cudaStream_t st)
+{
+    GradParams P;
+    P.n_atoms = n_atoms;
+    P.xyz_conv = xyz_conv;
+    std::copy(Minv, Minv + 9, P.Minv);
+    std::copy(A6, A6 + 36, P.A6);
+    P.want_xyz = (flags & DSF_D_XYZ) != 0;
+    P.want_adp = (flags & DSF_D_ADP) != 0;
+    P.want_occ = (flags & DSF_D_OCC) != 0;
+    P.want_mp = 0;
+    grad_epilogue_kernel<<<(n_atoms + 127) / 128, 128, 0, st>>>(P, g_acc, perm, adpk, w, mult_w, nullptr, nullptr,
+                                                                 out->d_xyz, out->d_adp, out->d_occ, nullptr, nullptr,
+                                                                 nullptr, nullptr);
+    return cudaGetLastError();
+}
+}  // namespace dsf
+
 // ==========================================================================
 // C ABI
 // ==========================================================================

@@ -188,6 +188,36 @@ int dsf_last_launch_count(const dsf_structure *s);
  * stream has not finished it */
 double dsf_last_kernel_ms(dsf_structure *s);
 
+/* ---- allocation-free call ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: a host program that owns every device allocation through its own
+ * pool, or a per-cycle refinement loop that must not trigger allocation.
+ * IAM structure factors and derivatives with every input and output in the
+ * caller's own device buffers; the scratch lives in one static device array
+ * of DSF_NOALLOC_SCRATCH_BYTES (32 MiB) that every GPU which loads the
+ * library holds until exit, enough for roughly 500 bytes per atom plus 100
+ * bytes per reflection (e.g. 20,000 atoms with 200,000 reflections).  Larger
+ * problems are rejected with DSF_ERR_ARGUMENT and a message in err.  No
+ * cudaMalloc, cudaFree or other allocating call is made.
+ * The first call on a device does a one-time set-up (it looks up the device
+ * address of the array); make that first call before any stream capture.
+ * All calls share the array, which keeps the last call's contents: calls
+ * that overlap on the GPU (other streams, other host threads) race on it and
+ * must be serialised by the caller.
+ * Device inputs: atom_type [n], adp_components [n] (0/1/6), xyz [n][3]
+ * fractional, adp [n][6] U_cif (Uiso in [0]), occupancy [n], multiplicity
+ * [n], anomalous [n][2] or NULL, hkl [n_hkl][3], dtdf [n_hkl][2]; device
+ * outputs in out (f required; d_xyz, d_adp, d_occ or NULL).  sym and model
+ * are host structures (at most DSF_NOALLOC_MAX_TYPES types). */
+#define DSF_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define DSF_NOALLOC_MAX_TYPES 32
+int dsf_iam_calculate_noalloc(const dsf_symmetry *sym, const dsf_iam_model *model, int n_atoms,
+                              const int *atom_type, const int *adp_components, const double *xyz,
+                              const double *adp, const double *occupancy, const double *multiplicity,
+                              const double *anomalous, int n_hkl, const int *hkl, const double *dtdf,
+                              int precision, int derivative_flags, const dsf_outputs *out, void *stream,
+                              char *err, int err_len);
+
 #ifdef __cplusplus
 }
 #endif
