@@ -16,6 +16,7 @@
 #include "../../include/dsf_gb300.h"
 #include "dsf_device.cuh"
 #include "dsf_math.cuh"
+#include "dsf_sf_kernel.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -27,6 +28,14 @@
 #include <vector>
 
 namespace dsf {
+struct SfLaunch;
+cudaError_t launch_rs_prep(const DevStructure &S, int n_hkl_pad, void *rs_f, void *rs_d, cudaStream_t st);
+cudaError_t launch_tr_prep(const DevStructure &S, int n_hkl_pad, void *tr_f, void *tr_d, void *trm_f, void *trm_d,
+                           bool mp, cudaStream_t st);
+size_t rs_record_bytes(bool fp64);
+size_t sf2_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types);
+cudaError_t launch_sf2(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool fp64, bool mp, bool aniso,
+                       int n_tiles, int n_chunks, cudaStream_t st);
 cudaError_t launch_sf_grad(const DevStructure &S, const CallBuffers &C, bool fp64, bool mp, int hkl_chunk, int ht,
                            cudaStream_t st);
 size_t sf_grad_smem_bytes(bool fp64, int ht, int n_sym);
@@ -196,7 +205,12 @@ struct dsf_structure {
     DevBuf d_sym_rot, d_sym_t24, d_tile_begin, d_tile_ntypes, d_tile_types, d_atom_ltype, d_atom_adpk,
         d_active, d_xq, d_xlo, d_xd, d_adp_f, d_adp_d, d_w_f, d_w_d, d_anom_f, d_anom_d, d_pg_f, d_pg_d, d_types,
         d_types_f, d_tcoeff, d_texp, d_tpow, d_texp_f, d_tpre_f, d_hkl, d_h2, d_h2f, d_hmult, d_cinv, d_table_f, d_table_d, d_perm, d_multw, d_dmat,
-        d_raw, d_dtdf, d_gw_d, d_gw_f, d_facc, d_gacc, d_out, d_plm_lmax;
+        d_raw, d_dtdf, d_gw_d, d_gw_f, d_facc, d_gacc, d_out, d_plm_lmax,
+        d_rs_f, d_rs_d, d_tr_f, d_tr_d, d_trm_f, d_trm_d, d_err;
+    int n_hkl_pad = 0;
+    bool tr_valid = false, trm_valid = false;
+    int n_tiles_plain = 0;   // tiles [0, n_tiles_plain) hold atoms without anisotropic ADPs
+    int max_types_plain = 1, max_types_aniso = 1;
     std::vector<uint8_t> active_host;
     bool have_hkl = false, have_atoms = false;
     int last_launches = 0;
@@ -595,11 +609,13 @@ int build_tiles(dsf_structure *s, bool by_type)
     const int n = s->n_atoms;
     s->perm.resize(n);
     std::iota(s->perm.begin(), s->perm.end(), 0);
-    if (by_type)
-        std::stable_sort(s->perm.begin(), s->perm.end(), [&](int x, int y) {
-            if (s->atom_type[x] != s->atom_type[y]) return s->atom_type[x] < s->atom_type[y];
-            return s->adpk[x] < s->adpk[y];
-        });
+    // atoms without anisotropic ADPs first, then by type: a tile holds one ADP kind
+    std::stable_sort(s->perm.begin(), s->perm.end(), [&](int x, int y) {
+        const int kx = s->adpk[x] == 6, ky = s->adpk[y] == 6;
+        if (kx != ky) return kx < ky;
+        if (by_type && s->atom_type[x] != s->atom_type[y]) return s->atom_type[x] < s->atom_type[y];
+        return false;
+    });
     s->tile_begin.clear();
     s->tile_ntypes.clear();
     s->tile_types.clear();
@@ -609,7 +625,8 @@ int build_tiles(dsf_structure *s, bool by_type)
         s->tile_begin.push_back(a);
         std::vector<int> types;
         int cnt = 0;
-        while (a < n && cnt < kTileAtoms) {
+        const int kind = s->adpk[s->perm[a]] == 6;
+        while (a < n && cnt < kTileAtoms && (s->adpk[s->perm[a]] == 6) == kind) {
             const int t = by_type ? s->atom_type[s->perm[a]] : 0;
             auto it = std::find(types.begin(), types.end(), t);
             int li;
@@ -629,6 +646,17 @@ int build_tiles(dsf_structure *s, bool by_type)
     }
     s->tile_begin.push_back(n);
     s->n_tiles = (int)s->tile_ntypes.size();
+    s->n_tiles_plain = 0;
+    s->max_types_plain = s->max_types_aniso = 1;
+    for (int t = 0; t < s->n_tiles; t++) {
+        const bool aniso = s->adpk[s->perm[s->tile_begin[t]]] == 6;
+        if (!aniso) {
+            s->n_tiles_plain = t + 1;
+            s->max_types_plain = std::max(s->max_types_plain, s->tile_ntypes[t]);
+        } else {
+            s->max_types_aniso = std::max(s->max_types_aniso, s->tile_ntypes[t]);
+        }
+    }
     dsf_engine *e = s->eng;
     int rc;
     std::vector<int> adpk_sorted(n);
@@ -669,6 +697,26 @@ int build_tiles(dsf_structure *s, bool by_type)
 }
 
 void refresh_dev(dsf_structure *s);
+
+// resident per-(type, reflection) radial tables; mp = the multipole-adjoint table
+int build_radial_tables(dsf_structure *s, bool mp)
+{
+    dsf_engine *e = s->eng;
+    if (!s->have_hkl) return DSF_OK;
+    const size_t row = 8 * (size_t)s->n_hkl_pad * std::max(1, s->n_types);
+    if (!mp) {
+        DSF_CUDA(s->d_tr_f.alloc(sizeof(float) * row));
+        DSF_CUDA(s->d_tr_d.alloc(sizeof(double) * row));
+        DSF_CUDA(launch_tr_prep(s->dev, s->n_hkl_pad, s->d_tr_f.p, s->d_tr_d.p, nullptr, nullptr, false, e->stream));
+        s->tr_valid = true;
+    } else {
+        DSF_CUDA(s->d_trm_f.alloc(sizeof(float) * row));
+        DSF_CUDA(s->d_trm_d.alloc(sizeof(double) * row));
+        DSF_CUDA(launch_tr_prep(s->dev, s->n_hkl_pad, nullptr, nullptr, s->d_trm_f.p, s->d_trm_d.p, true, e->stream));
+        s->trm_valid = true;
+    }
+    return DSF_OK;
+}
 
 // per-type constants of the kernels in both precisions (prefactors folded)
 template <typename R>
@@ -1076,7 +1124,8 @@ int dsf_structure_destroy(dsf_structure *s)
                       &s->d_adp_d, &s->d_w_f, &s->d_w_d, &s->d_anom_f, &s->d_anom_d, &s->d_pg_f, &s->d_pg_d,
                       &s->d_types, &s->d_types_f, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_texp_f, &s->d_tpre_f, &s->d_hkl, &s->d_h2, &s->d_h2f, &s->d_hmult,
                       &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw, &s->d_dmat, &s->d_raw,
-                      &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc, &s->d_out, &s->d_plm_lmax};
+                      &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc, &s->d_out, &s->d_plm_lmax,
+                      &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d, &s->d_trm_f, &s->d_trm_d, &s->d_err};
     for (DevBuf *b : bufs) b->release();
     if (s->ev_begin) cudaEventDestroy(s->ev_begin);
     if (s->ev_end) cudaEventDestroy(s->ev_end);
@@ -1093,8 +1142,9 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
     if (s->model == MODEL_TABLE && s->have_hkl && n_hkl != s->n_hkl)
         return fail(e, DSF_ERR_ARGUMENT, "tabulated structures keep the reflection set of their table");
     cudaSetDevice(e->device);
-    std::vector<int4> h4(n_hkl);
-    std::vector<double> h2(n_hkl), mult(n_hkl), cinv(2 * (size_t)n_hkl);
+    const int n_pad = (n_hkl + 15) / 16 * 16;  // tables and per-reflection arrays padded with zero rows
+    std::vector<int4> h4(n_pad, make_int4(0, 0, 0, 0));
+    std::vector<double> h2(n_pad, 0.0), mult(n_pad, 0.0), cinv(2 * (size_t)n_pad, 0.0);
     for (int i = 0; i < n_hkl; i++) {
         const int h = hkl[3 * i], k = hkl[3 * i + 1], l = hkl[3 * i + 2];
         h4[i] = make_int4(h, k, l, 0);
@@ -1121,13 +1171,25 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
     }
     if ((rc = upload(e, s->d_hmult, mult.data(), mult.size()))) return rc;
     if ((rc = upload(e, s->d_cinv, cinv.data(), cinv.size()))) return rc;
-    DSF_CUDA(s->d_dtdf.alloc(16 * (size_t)n_hkl));
-    DSF_CUDA(s->d_gw_d.alloc(16 * (size_t)n_hkl));
-    DSF_CUDA(s->d_gw_f.alloc(8 * (size_t)n_hkl));
-    DSF_CUDA(s->d_facc.alloc(16 * (size_t)n_hkl));
+    DSF_CUDA(s->d_dtdf.alloc(16 * (size_t)n_pad));
+    DSF_CUDA(s->d_gw_d.alloc(16 * (size_t)n_pad));
+    DSF_CUDA(s->d_gw_f.alloc(8 * (size_t)n_pad));
+    DSF_CUDA(s->d_facc.alloc(16 * (size_t)n_pad));
+    DSF_CUDA(cudaMemsetAsync(s->d_gw_d.p, 0, 16 * (size_t)n_pad, e->stream));
+    DSF_CUDA(cudaMemsetAsync(s->d_gw_f.p, 0, 8 * (size_t)n_pad, e->stream));
+    DSF_CUDA(s->d_err.alloc(sizeof(int)));
+    DSF_CUDA(cudaMemsetAsync(s->d_err.p, 0, sizeof(int), e->stream));
     s->n_hkl = n_hkl;
+    s->n_hkl_pad = n_pad;
     s->have_hkl = true;
     refresh_dev(s);
+    // resident per-(reflection, operation) table
+    DSF_CUDA(s->d_rs_f.alloc(rs_record_bytes(false) * (size_t)n_pad * s->n_sym));
+    DSF_CUDA(s->d_rs_d.alloc(rs_record_bytes(true) * (size_t)n_pad * s->n_sym));
+    DSF_CUDA(launch_rs_prep(s->dev, n_pad, s->d_rs_f.p, s->d_rs_d.p, e->stream));
+    s->tr_valid = s->trm_valid = false;
+    int rc2 = build_radial_tables(s, false);
+    if (rc2) return rc2;
     DSF_CUDA(cudaStreamSynchronize(e->stream));
     return DSF_OK;
 }
@@ -1190,6 +1252,8 @@ int dsf_structure_update_types(dsf_structure *s, const double *plm, const double
     int rc;
     if ((rc = upload_types(s))) return rc;
     if (plm && (rc = compute_global_plm(s))) return rc;
+    s->trm_valid = false;
+    if ((rc = build_radial_tables(s, false))) return rc;
     refresh_dev(s);
     DSF_CUDA(cudaStreamSynchronize(e->stream));
     return DSF_OK;
@@ -1218,7 +1282,8 @@ int64_t dsf_structure_device_bytes(const dsf_structure *s)
                             &s->d_pg_d, &s->d_types, &s->d_types_f, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_texp_f, &s->d_tpre_f, &s->d_hkl, &s->d_h2, &s->d_h2f,
                             &s->d_hmult, &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw,
                             &s->d_dmat, &s->d_raw, &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc,
-                            &s->d_out, &s->d_plm_lmax};
+                            &s->d_out, &s->d_plm_lmax, &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d,
+                            &s->d_trm_f, &s->d_trm_d, &s->d_err};
     int64_t b = 0;
     for (const DevBuf *p : bufs) b += (int64_t)p->bytes;
     return b;
@@ -1260,28 +1325,52 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     DSF_CUDA(cudaGetLastError());
     DSF_CUDA(cudaMemsetAsync(s->d_facc.p, 0, 16 * (size_t)n_hkl, st));
     DSF_CUDA(cudaMemsetAsync(s->d_gacc.p, 0, sizeof(double) * kNch * (size_t)n, st));
-    // launch shape: reflections per sub-tile from the shared-memory budget,
-    // reflection chunks so the grid covers the SMs several times
-    int ht = kMaxHT;
-    while (ht > 2 && sf_grad_smem_bytes(fp64, ht, s->n_sym) > std::min<size_t>(e->max_smem, 110 * 1024)) ht /= 2;
-    const int target = std::max(1, e->n_sm) * 8;
-    int n_chunks = std::max(1, target / std::max(1, s->n_tiles));
-    int chunk = (n_hkl + n_chunks - 1) / n_chunks;
-    chunk = std::max(chunk, 4 * ht);
-    chunk = (chunk + ht - 1) / ht * ht;
+    if (mp && !s->trm_valid) {
+        int rc = build_radial_tables(s, true);
+        if (rc) return rc;
+    }
     CallBuffers C;
     C.gw_d = s->d_gw_d.as<double2>();
     C.gw_f = s->d_gw_f.as<float2>();
     C.f_acc = s->d_facc.as<double2>();
     C.g_acc = s->d_gacc.as<double>();
+    SfLaunch L{};
+    L.n_hkl_pad = s->n_hkl_pad;
+    L.rs = fp64 ? s->d_rs_d.p : s->d_rs_f.p;
+    L.tr = fp64 ? s->d_tr_d.p : s->d_tr_f.p;
+    L.trm = fp64 ? s->d_trm_d.p : s->d_trm_f.p;
+    L.error = s->d_err.as<int>();
     if (!s->ev_begin) {
         DSF_CUDA(cudaEventCreate(&s->ev_begin));
         DSF_CUDA(cudaEventCreate(&s->ev_end));
     }
     DSF_CUDA(cudaEventRecord(s->ev_begin, st));
-    DSF_CUDA(launch_sf_grad(s->dev, C, fp64, mp, chunk, ht, st));
+    // one launch per ADP kind (tiles [0, n_tiles_plain) without anisotropic ADPs)
+    const int ranges[2][2] = {{0, s->n_tiles_plain}, {s->n_tiles_plain, s->n_tiles}};
+    for (int kind = 0; kind < 2; kind++) {
+        const int t0 = ranges[kind][0], nt = ranges[kind][1] - ranges[kind][0];
+        if (nt <= 0) continue;
+        L.tile_offset = t0;
+        L.max_types = kind ? s->max_types_aniso : s->max_types_plain;
+        // reflections per sub-tile from the shared-memory budget (several blocks per SM)
+        int ht = kMaxHT;
+        const size_t budget = std::min<size_t>(e->max_smem, fp64 ? 200 * 1024 : 100 * 1024);
+        while (ht > 4 && sf2_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > budget) ht /= 2;
+        if (sf2_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > e->max_smem)
+            return fail(e, DSF_ERR_UNSUPPORTED, "shared-memory tile does not fit this device");
+        L.ht = ht;
+        // reflection chunks so the grid covers the SMs several times
+        const int target = std::max(1, e->n_sm) * 8;
+        const int n_chunks0 = std::max(1, target / nt);
+        int chunk = (n_hkl + n_chunks0 - 1) / n_chunks0;
+        chunk = std::max(chunk, 4 * ht);
+        chunk = (chunk + ht - 1) / ht * ht;
+        L.hkl_chunk = chunk;
+        const int n_chunks = (n_hkl + chunk - 1) / chunk;
+        DSF_CUDA(launch_sf2(s->dev, C, L, fp64, mp, kind == 1, nt, n_chunks, st));
+        launches++;
+    }
     DSF_CUDA(cudaEventRecord(s->ev_end, st));
-    launches++;
     f_epilogue_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, s->d_facc.as<double2>(), s->d_hmult.as<double>(),
                                                            s->d_cinv.as<double2>(), s->centro_mode, out->f);
     launches++;
@@ -1347,7 +1436,13 @@ int dsf_calculate(dsf_structure *s, int precision, int flags, const double *dtdf
         {out->d_kappa_prime, d.d_kappa_prime, (size_t)n}};
     for (auto &c : cp)
         if (c.dst) DSF_CUDA(cudaMemcpyAsync(c.dst, c.src, 8 * c.n, cudaMemcpyDeviceToHost, e->stream));
+    int kerr = 0;
+    DSF_CUDA(cudaMemcpyAsync(&kerr, s->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
     DSF_CUDA(cudaStreamSynchronize(e->stream));
+    if (kerr) {
+        cudaMemsetAsync(s->d_err.p, 0, sizeof(int), e->stream);
+        return fail(e, DSF_ERR_TIMEOUT, "a shared-memory pipeline wait of the kernel ran out");
+    }
     return DSF_OK;
 }
 

@@ -1,0 +1,163 @@
+// Resident per-structure tables of the structure-factor kernel.
+//
+//   RS[h][s]  per (reflection, symmetry operation): h' = R^T h (integer and
+//             real), the phase offset h.t (2^32 fixed point and real; exact,
+//             translations are multiples of 1/24) and the density-normalised
+//             harmonics d_lm of h'/|h'| in the global frame
+//             (pre_atom_loop_sf_calc, src/Scattering/HansenCoppens_SF_Engine3.cpp:319-418;
+//              getDensityNormalized<4>, include/discamb/MathUtilities/real_spherical_harmonics.h:102-115)
+//   TR[t][h]  per (type, reflection): spherical f = f_core + P_val f_val(|h|/kappa)
+//             (or the n-Gaussian f0 of IAM types) and the signed radial terms
+//             4 pi N_l g_l(|h|/kappa') of the deformation density
+//             (pre_atom_loop_sf_calc, same file :365-418)
+//   TRM[t][h] f_val, P_val df_val/dkappa and 4 pi N_l dg_l/dkappa' (the
+//             multipole-parameter adjoint; no counterpart in the reference)
+// Rows past the last reflection (padding to a multiple of 16) are zero.
+#include "dsf_device.cuh"
+#include "dsf_math.cuh"
+#include "dsf_sf_kernel.cuh"
+
+namespace dsf {
+
+template <typename R>
+struct SelP;
+template <>
+struct SelP<float> {
+    static __device__ const TypeRadialT<float> *types(const DevStructure &S) { return S.types_f; }
+    static __device__ const float *pre(const DevStructure &S) { return S.term_pre_f; }
+    static __device__ const float *zexp(const DevStructure &S) { return S.term_exp_f; }
+};
+template <>
+struct SelP<double> {
+    static __device__ const TypeRadialT<double> *types(const DevStructure &S) { return S.types_d; }
+    static __device__ const double *pre(const DevStructure &S) { return S.term_pre_d; }
+    static __device__ const double *zexp(const DevStructure &S) { return S.term_exp_d; }
+};
+
+__device__ __forceinline__ float fexp_(float x) { return expf(x); }
+__device__ __forceinline__ double fexp_(double x) { return exp(x); }
+
+template <typename R>
+__global__ void rs_prep_kernel(DevStructure S, int n_hkl_pad, RsRec<R> *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nS = S.n_sym;
+    if (i >= n_hkl_pad * nS) return;
+    const int h = i / nS, s = i - h * nS;
+    RsRec<R> rec;
+    for (int q = 0; q < 28; q++) rec.y[q] = R(0);
+    for (int q = 0; q < 4; q++) rec.hf[q] = R(0);
+    rec.hi = make_int4(0, 0, 0, 0);
+    if (h < S.n_hkl) {
+        const int4 hv = S.hkl[h];
+        const int *Rm = S.sym_rot + 9 * s;
+        const int *t = S.sym_t24 + 3 * s;
+        const int hp0 = hv.x * Rm[0] + hv.y * Rm[3] + hv.z * Rm[6];
+        const int hp1 = hv.x * Rm[1] + hv.y * Rm[4] + hv.z * Rm[7];
+        const int hp2 = hv.x * Rm[2] + hv.y * Rm[5] + hv.z * Rm[8];
+        int tr = (hv.x * t[0] + hv.y * t[1] + hv.z * t[2]) % 24;
+        if (tr < 0) tr += 24;
+        const uint32_t tq = (uint32_t)((((uint64_t)tr << 32) + 12u) / 24u);
+        rec.hi = make_int4(hp0, hp1, hp2, (int)tq);
+        rec.hf[0] = R(hp0);
+        rec.hf[1] = R(hp1);
+        rec.hf[2] = R(hp2);
+        rec.hf[3] = R(tr / 24.0);
+        if (S.model == MODEL_HC) {
+            const double cx = S.B[0] * hp0 + S.B[1] * hp1 + S.B[2] * hp2;
+            const double cy = S.B[3] * hp0 + S.B[4] * hp1 + S.B[5] * hp2;
+            const double cz = S.B[6] * hp0 + S.B[7] * hp1 + S.B[8] * hp2;
+            const double n2 = cx * cx + cy * cy + cz * cz;
+            if (n2 > 1e-20) {  // F(000): no deformation term
+                const double inv = 1.0 / sqrt(n2);
+                double v[25];
+                harmonic_polys<double>(cx * inv, cy * inv, cz * inv, v);
+                for (int q = 0; q < 25; q++) rec.y[q] = R(v[q] * kDensityNorm[q]);
+            }
+        }
+    }
+    out[i] = rec;
+}
+
+// radial terms of one (type, reflection), see the file comment
+template <typename R>
+__device__ void radial_terms2(const DevStructure &S, const TypeRadialT<R> &t, R h2, R *base, R *mpv, bool mp)
+{
+    for (int q = 0; q < 8; q++) {
+        base[q] = R(0);
+        mpv[q] = R(0);
+    }
+    const R hl = sqrt(h2);
+    const R K = R(2.0 * DSF_PI) * hl;
+    if (S.model == MODEL_IAM) {
+        R s = t.iam_c;
+        const R x2 = h2 * R(0.25);
+        for (int q = 0; q < t.iam_n; q++) s += t.iam_a[q] * fexp_(-t.iam_b[q] * x2);
+        base[0] = s;
+        return;
+    }
+    if (S.model != MODEL_HC) return;
+    const R *pre = SelP<R>::pre(S);
+    const R *zx = SelP<R>::zexp(S);
+    R fc = R(0);
+    for (int q = t.core_begin; q < t.core_end; q++) fc += pre[q] * gcore<R>(0, S.term_m[q], K, zx[q]);
+    const R Kv = K * t.inv_kappa, Kd = K * t.inv_kappa_p;
+    R fv = R(0), dfv = R(0);
+    for (int q = t.val_begin; q < t.val_end; q++) {
+        fv += pre[q] * gcore<R>(0, S.term_m[q], Kv, zx[q]);
+        if (mp) dfv -= R(2) * pre[q] * gcore<R>(1, S.term_m[q], Kv, zx[q]);  // dG(n,0)/dK = -G(n+1,1)
+    }
+    base[0] = fc + t.pv * fv;
+    mpv[0] = fv;
+    mpv[1] = t.pv * dfv * (-Kv * t.inv_kappa);
+    for (int l = 0; l < t.n_def; l++) {
+        const R g = gcore<R>(l, t.def_m[l], Kd, t.zeta);
+        base[1 + l] = t.def_pre[l] * g;
+        if (mp && Kd > R(0)) {
+            // dG/dK = (l/K) G(n,l) - G(n+1,l+1); the second term's prefactor is 2(l+1) times larger
+            const R dg = R(l) / Kd * g - R(2 * (l + 1)) * gcore<R>(l + 1, t.def_m[l], Kd, t.zeta);
+            mpv[2 + l] = t.def_pre[l] * dg * (-Kd * t.inv_kappa_p);
+        }
+    }
+}
+
+template <typename R>
+__global__ void tr_prep_kernel(DevStructure S, int n_hkl_pad, R *tr, R *trm, int mp)
+{
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.y;
+    if (h >= n_hkl_pad) return;
+    R base[8], mpv[8];
+    if (h < S.n_hkl) {
+        const R h2 = R(S.h2[h]);
+        radial_terms2<R>(S, SelP<R>::types(S)[t], h2, base, mpv, mp != 0);
+    } else {
+        for (int q = 0; q < 8; q++) base[q] = mpv[q] = R(0);
+    }
+    const size_t row = ((size_t)t * n_hkl_pad + h) * 8;
+    if (tr)
+        for (int q = 0; q < 8; q++) tr[row + q] = base[q];
+    if (mp && trm)
+        for (int q = 0; q < 8; q++) trm[row + q] = mpv[q];
+}
+
+cudaError_t launch_rs_prep(const DevStructure &S, int n_hkl_pad, void *rs_f, void *rs_d, cudaStream_t st)
+{
+    const int n = n_hkl_pad * S.n_sym;
+    rs_prep_kernel<float><<<(n + 127) / 128, 128, 0, st>>>(S, n_hkl_pad, (RsRec<float> *)rs_f);
+    rs_prep_kernel<double><<<(n + 127) / 128, 128, 0, st>>>(S, n_hkl_pad, (RsRec<double> *)rs_d);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tr_prep(const DevStructure &S, int n_hkl_pad, void *tr_f, void *tr_d, void *trm_f, void *trm_d,
+                           bool mp, cudaStream_t st)
+{
+    dim3 grid((n_hkl_pad + 127) / 128, S.n_types);
+    tr_prep_kernel<float><<<grid, 128, 0, st>>>(S, n_hkl_pad, mp ? nullptr : (float *)tr_f, (float *)trm_f, mp);
+    tr_prep_kernel<double><<<grid, 128, 0, st>>>(S, n_hkl_pad, mp ? nullptr : (double *)tr_d, (double *)trm_d, mp);
+    return cudaGetLastError();
+}
+
+size_t rs_record_bytes(bool fp64) { return fp64 ? sizeof(RsRec<double>) : sizeof(RsRec<float>); }
+
+}  // namespace dsf

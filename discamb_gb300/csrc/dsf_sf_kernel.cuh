@@ -1,0 +1,533 @@
+// Fused structure-factor + adjoint kernel (sm_103a), templated on precision,
+// multipole derivatives, ADP kind and symmetry-operation count.
+//
+// One block owns one tile of up to 128 atoms (one atom per thread, atoms
+// sorted by ADP kind and type so a tile holds one ADP kind and few types) and
+// a contiguous chunk of reflections.  The structure keeps two resident tables
+// in HBM, built once per reflection set / type update (dsf_prep_kernels.cu):
+//   RS[h][s]   per (reflection, operation): h' = R^T h as integers and reals,
+//              the 2^32 fixed-point phase offset h.t (or h.t for FP64), and
+//              the 25 harmonics d_lm(h'/|h'|);
+//   TR[t][h]   per (type, reflection): the spherical form factor and the
+//              signed radial terms 4 pi N_l g_l (plus their kappa/kappa'
+//              derivatives in a second table for the multipole adjoint).
+// Sub-tiles of HT reflections of these tables are streamed into shared memory
+// by TMA bulk copies (cp.async.bulk + mbarrier, double-buffered, bounded
+// waits).  Each thread then runs the sum over operations for its atom, the
+// per-reflection partial F is reduced across the block with warp shuffles and
+// committed with FP64 atomics, and the per-atom derivative sums are folded
+// into Kahan-compensated totals in shared memory.
+//
+// Reference loop restated: HansenCoppens_SF_Engine3::calculateSF_Serial*
+// (src/Scattering/HansenCoppens_SF_Engine3.cpp:1030-1509, 1511-1992,
+// 2649-2894) and AnyScattererStructureFactorCalculator::calculateStructure
+// FactorsAndDerivatives (src/Scattering/AnyScattererStructureFactor
+// Calculator.cpp:614-829).
+//
+// R = double: the plain form, FP64 throughout.
+// R = float : the FP32-bulk form.  Phases are reduced exactly in integer
+// arithmetic (fractional coordinates as 2^32 fixed point, integer h', h.t
+// from integer translations in 1/24) and turned into sin/cos by a
+// polynomial on the exact remainder, so no FP64 is needed per term (FP64
+// runs at 1/64 of the FP32 rate on GB300).  F and the cross-block derivative
+// sums are FP64.
+#pragma once
+#include "dsf_device.cuh"
+#include "dsf_math.cuh"
+
+namespace dsf {
+
+template <typename R>
+struct Vec2;
+template <>
+struct Vec2<float> { using T = float2; };
+template <>
+struct Vec2<double> { using T = double2; };
+
+// one (reflection, operation) record of the RS table
+template <typename R>
+struct __align__(16) RsRec {
+    int4 hi;   // h'0, h'1, h'2, fixed-point phase offset of h.t
+    R hf[4];   // h' as reals, h.t (FP64 form)
+    R y[28];   // 25 harmonics, padded
+};
+
+// sin and cos of 2 pi (P 2^-32 + lo) for a phase P in 2^32 fixed point (the
+// exact integer reduction mod one turn) and a small FP32 remainder lo (in
+// turns).  Quadrant from the two top bits, remainder angle in [-pi/4, pi/4]
+// exact in FP32 up to rounding, Taylor polynomials to degree 9 (sin) and 8
+// (cos): truncation below 3e-8, so the result is limited by FP32 rounding
+// (~1e-7 absolute) instead of the ~1e-6 of the hardware approximation.
+__device__ __forceinline__ void sincos_fixed(uint32_t P, float lo, float *sn, float *cs)
+{
+    const uint32_t q = (P + 0x20000000u) >> 30;
+    const int32_t r = (int32_t)(P - (q << 30));
+    const float th = fmaf((float)r, 1.4629180792671596e-09f, 6.283185307179586f * lo);
+    const float t2 = th * th;
+    float sp = fmaf(t2, 2.7557319e-06f, -1.9841270e-04f);
+    sp = fmaf(t2, sp, 8.3333333e-03f);
+    sp = fmaf(t2, sp, -1.6666667e-01f);
+    const float sv = fmaf(th * t2, sp, th);
+    float cp = fmaf(t2, 2.4801587e-05f, -1.3888889e-03f);
+    cp = fmaf(t2, cp, 4.1666668e-02f);
+    cp = fmaf(t2, cp, -0.5f);
+    const float cv = fmaf(t2, cp, 1.0f);
+    float ss = (q & 1u) ? cv : sv;
+    float cc = (q & 1u) ? sv : cv;
+    if (q & 2u) ss = -ss;
+    if ((q + 1u) & 2u) cc = -cc;
+    *sn = ss;
+    *cs = cc;
+}
+
+// temperature factor from the exponent of the ADP quadratic form: FP64 exp;
+// FP32 exp2 (the FP32 ADPs are stored multiplied by log2 e)
+template <typename R>
+__device__ __forceinline__ R texp(R x);
+template <>
+__device__ __forceinline__ float texp<float>(float x) { return exp2f(x); }
+template <>
+__device__ __forceinline__ double texp<double>(double x) { return exp(x); }
+
+template <typename R>
+__device__ __forceinline__ R shfl_xor(R v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+
+// ---------------------------------------------------------------------------
+// TMA bulk copy + mbarrier helpers (PTX)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wait for phase `parity` of the barrier; false after ~2 s (the kernel then
+// reports DSF_ERR_TIMEOUT instead of hanging)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    const uint32_t a = smem_u32(bar);
+    uint64_t t0 = 0;
+    for (uint32_t it = 0;; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (it == 0) t0 = global_ns();
+        else if ((it & 63u) == 0 && global_ns() - t0 > 2000000000ull) return false;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// kernel
+// ---------------------------------------------------------------------------
+struct SfLaunch {
+    int hkl_chunk;   // reflections per block (multiple of ht)
+    int ht;          // reflections per shared-memory sub-tile (multiple of 4)
+    int tile_offset; // first tile of this launch
+    int max_types;   // largest number of types in a tile of this launch
+    int n_hkl_pad;   // padded reflection count of the tables
+    const void *rs;  // RsRec<R> [n_hkl_pad][n_sym]
+    const void *tr;  // R [n_types][n_hkl_pad][8]
+    const void *trm; // R [n_types][n_hkl_pad][8] (multipole adjoint)
+    int *error;      // set to 1 on a timed-out wait
+};
+
+template <typename R>
+struct StageLayout {
+    size_t rs, tr, trm, gw, h2, bytes;
+    __host__ __device__ StageLayout(int ht, int ns, int max_types, bool mp)
+    {
+        rs = 0;
+        tr = rs + sizeof(RsRec<R>) * (size_t)ht * ns;
+        trm = tr + sizeof(R) * 8 * (size_t)ht * max_types;
+        gw = trm + (mp ? sizeof(R) * 8 * (size_t)ht * max_types : 0);
+        h2 = gw + sizeof(R) * 2 * (size_t)ht;
+        bytes = h2 + sizeof(R) * (size_t)ht;
+        bytes = (bytes + 15) & ~(size_t)15;
+    }
+};
+
+template <typename R, bool MP>
+__host__ __device__ constexpr int n_channels() { return MP ? 38 : 10; }
+
+template <typename R, bool MP>
+__host__ __device__ inline size_t sf_smem_bytes(int ht, int ns, int max_types)
+{
+    StageLayout<R> L(ht, ns, max_types, MP);
+    size_t b = 64;                                                        // barriers
+    b += 2 * L.bytes;                                                     // two stages
+    b += sizeof(R) * 2 * (size_t)(kTileAtoms / 32) * ht;                  // warp partials of F
+    b += sizeof(R) * 2 * (size_t)n_channels<R, MP>() * kTileAtoms;        // Kahan totals
+    b += sizeof(int) * kMaxTileTypes;
+    return b;
+}
+
+template <typename R, bool MP, bool ANISO, int NSC>
+__global__ void __launch_bounds__(kTileAtoms)
+sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
+{
+    using R2 = typename Vec2<R>::T;
+    constexpr bool F32 = sizeof(R) == 4;
+    constexpr int NT = n_channels<R, MP>();
+    constexpr int kWarps = kTileAtoms / 32;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nS = NSC > 0 ? NSC : S.n_sym;
+    const int ht = L.ht;
+    const int tile = L.tile_offset + blockIdx.x;
+    const int h_begin = blockIdx.y * L.hkl_chunk;
+    const int h_end = min(S.n_hkl, h_begin + L.hkl_chunk);
+    if (h_begin >= h_end) return;
+    const int a_begin = S.tile_begin[tile], a_end = S.tile_begin[tile + 1];
+    const int nT = S.tile_ntypes[tile];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool hc_model = S.model == MODEL_HC;
+    const bool table_model = S.model == MODEL_TABLE;
+
+    // shared memory carve-up
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);  // [2]
+    const StageLayout<R> SL(ht, nS, L.max_types, MP);
+    unsigned char *stage0 = smem_raw + 64;
+    R2 *sF = reinterpret_cast<R2 *>(stage0 + 2 * SL.bytes);           // [kWarps][ht]
+    R *sTot = reinterpret_cast<R *>(sF + kWarps * ht);                 // [NT][kTileAtoms]
+    R *sCmp = sTot + NT * kTileAtoms;                                   // [NT][kTileAtoms]
+    int *sTypes = reinterpret_cast<int *>(sCmp + NT * kTileAtoms);     // [nT]
+
+    for (int i = tid; i < nT; i += blockDim.x) sTypes[i] = S.tile_types[tile * kMaxTileTypes + i];
+    for (int q = 0; q < NT; q++) {
+        sTot[q * kTileAtoms + tid] = R(0);
+        sCmp[q * kTileAtoms + tid] = R(0);
+    }
+    if (tid == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    const RsRec<R> *rs_g = reinterpret_cast<const RsRec<R> *>(L.rs);
+    const R *tr_g = reinterpret_cast<const R *>(L.tr);
+    const R *trm_g = reinterpret_cast<const R *>(L.trm);
+    const R2 *gw_g;
+    const R *h2_g;
+    if constexpr (F32) {
+        gw_g = C.gw_f;
+        h2_g = S.h2f;
+    } else {
+        gw_g = C.gw_d;
+        h2_g = S.h2;
+    }
+
+    // thread 0 streams a sub-tile of the tables into one stage buffer
+    auto issue = [&](int buf, int h0) {
+        unsigned char *st = stage0 + buf * SL.bytes;
+        uint32_t bytes = (uint32_t)(sizeof(RsRec<R>) * ht * nS) + (uint32_t)(2 * sizeof(R) * ht) +
+                         (uint32_t)(sizeof(R) * ht) + (uint32_t)(sizeof(R) * 8 * ht) * nT * (MP ? 2u : 1u);
+        fence_proxy_async();
+        mbar_expect_tx(&bar[buf], bytes);
+        bulk_copy(st + SL.rs, rs_g + (size_t)h0 * nS, (uint32_t)(sizeof(RsRec<R>) * ht * nS), &bar[buf]);
+        for (int t = 0; t < nT; t++) {
+            const size_t row = ((size_t)sTypes[t] * L.n_hkl_pad + h0) * 8;
+            bulk_copy(st + SL.tr + sizeof(R) * 8 * (size_t)ht * t, tr_g + row, (uint32_t)(sizeof(R) * 8 * ht),
+                      &bar[buf]);
+            if constexpr (MP)
+                bulk_copy(st + SL.trm + sizeof(R) * 8 * (size_t)ht * t, trm_g + row,
+                          (uint32_t)(sizeof(R) * 8 * ht), &bar[buf]);
+        }
+        bulk_copy(st + SL.gw, gw_g + h0, (uint32_t)(2 * sizeof(R) * ht), &bar[buf]);
+        bulk_copy(st + SL.h2, h2_g + h0, (uint32_t)(sizeof(R) * ht), &bar[buf]);
+    };
+
+    // per-atom registers
+    const int a = a_begin + tid;
+    const bool have = a < a_end;
+    bool active = false;
+    int lt = 0;
+    R w = R(0), pg[25], adp[ANISO ? 6 : 1];
+    R anre = R(0), anim = R(0);
+    uint32_t xq0 = 0, xq1 = 0, xq2 = 0;
+    R x0 = R(0), x1 = R(0), x2 = R(0);  // FP32: low parts (turns); FP64: coordinates
+    bool has_adp = false;
+#pragma unroll
+    for (int q = 0; q < 25; q++) pg[q] = R(0);
+#pragma unroll
+    for (int q = 0; q < (ANISO ? 6 : 1); q++) adp[q] = R(0);
+    if (have) {
+        active = S.atom_active[a] != 0;
+        lt = S.atom_ltype[a];
+        has_adp = S.atom_adpk[a] != 0;
+        if constexpr (F32) {
+            w = S.atom_w_f[a];
+            const float2 an = S.atom_anom_f[a];
+            anre = an.x; anim = an.y;
+            xq0 = S.atom_xq[3 * a]; xq1 = S.atom_xq[3 * a + 1]; xq2 = S.atom_xq[3 * a + 2];
+            x0 = S.atom_xlo[3 * a]; x1 = S.atom_xlo[3 * a + 1]; x2 = S.atom_xlo[3 * a + 2];
+#pragma unroll
+            for (int q = 0; q < (ANISO ? 6 : 1); q++) adp[q] = S.atom_adp_f[6 * a + q];
+            if (hc_model)
+#pragma unroll
+                for (int q = 0; q < 25; q++) pg[q] = S.atom_pg_f[25 * a + q];
+        } else {
+            w = S.atom_w_d[a];
+            const double2 an = S.atom_anom_d[a];
+            anre = an.x; anim = an.y;
+            x0 = S.atom_xd[3 * a]; x1 = S.atom_xd[3 * a + 1]; x2 = S.atom_xd[3 * a + 2];
+#pragma unroll
+            for (int q = 0; q < (ANISO ? 6 : 1); q++) adp[q] = S.atom_adp_d[6 * a + q];
+            if (hc_model)
+#pragma unroll
+                for (int q = 0; q < 25; q++) pg[q] = S.atom_pg_d[25 * a + q];
+        }
+    }
+    const int a_orig = have ? S.atom_orig[a] : 0;
+
+    if (tid == 0) issue(0, h_begin);
+    uint32_t parity[2] = {0u, 0u};
+    int k = 0;
+    for (int h0 = h_begin; h0 < h_end; h0 += ht, k++) {
+        const int buf = k & 1;
+        const int nh = min(ht, h_end - h0);
+        if (tid == 0 && h0 + ht < h_end) issue(buf ^ 1, h0 + ht);
+        const bool ok = mbar_wait(&bar[buf], parity[buf]);
+        parity[buf] ^= 1u;
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(L.error, 1);
+                mbar_wait(&bar[buf ^ 1], parity[buf ^ 1]);  // bounded: let copies in flight land
+            }
+            return;
+        }
+        const unsigned char *st = stage0 + buf * SL.bytes;
+        const RsRec<R> *sRs = reinterpret_cast<const RsRec<R> *>(st + SL.rs);
+        const R *sTr = reinterpret_cast<const R *>(st + SL.tr);
+        const R *sTrm = reinterpret_cast<const R *>(st + SL.trm);
+        const R2 *sG = reinterpret_cast<const R2 *>(st + SL.gw);
+        const R *sH2 = reinterpret_cast<const R *>(st + SL.h2);
+
+        R part[NT];
+#pragma unroll
+        for (int q = 0; q < NT; q++) part[q] = R(0);
+
+        for (int hl = 0; hl < nh; hl++) {
+            R Fre = R(0), Fim = R(0);
+            if (active) {
+                const R2 g = sG[hl];
+                const R *rad = sTr + (size_t)(lt * ht + hl) * 8;
+                const R fsre = rad[0] + anre, fsim = anim;
+                const R r0 = rad[1], r1 = rad[2], r2 = rad[3], r3 = rad[4], r4 = rad[5];
+                R Tiso = R(1);
+                if (!ANISO && has_adp) Tiso = texp<R>(-adp[0] * sH2[hl]);
+                const R gre = g.x * Tiso, gim = g.y * Tiso;  // adjoint weight with the isotropic factor
+                R Ure = 0, Uim = 0;
+                R Xre[3] = {0, 0, 0}, Xim[3] = {0, 0, 0};
+                R Are[ANISO ? 6 : 1], Aim[ANISO ? 6 : 1];
+#pragma unroll
+                for (int q = 0; q < (ANISO ? 6 : 1); q++) { Are[q] = R(0); Aim[q] = R(0); }
+                R Ere = 0, Eim = 0, Kre = 0, Kim = 0;
+                const RsRec<R> *recs = sRs + (size_t)hl * nS;
+                auto term = [&](int s) {
+                    const RsRec<R> &rec = recs[s];
+                    const R h0f = rec.hf[0], h1f = rec.hf[1], h2f = rec.hf[2];
+                    R sn, cs;
+                    if constexpr (F32) {
+                        const int4 hi = rec.hi;
+                        const uint32_t P = (uint32_t)hi.x * xq0 + (uint32_t)hi.y * xq1 + (uint32_t)hi.z * xq2 +
+                                           (uint32_t)hi.w;
+                        sincos_fixed(P, h0f * x0 + h1f * x1 + h2f * x2, &sn, &cs);
+                    } else {
+                        double ph = h0f * x0 + h1f * x1 + h2f * x2 + rec.hf[3];
+                        ph -= rint(ph);
+                        sincospi(2.0 * ph, &sn, &cs);
+                    }
+                    R zre = cs, zim = sn;  // e^{i theta} T_s
+                    R m6[ANISO ? 6 : 1];
+                    if constexpr (ANISO) {
+                        m6[0] = h0f * h0f; m6[1] = h1f * h1f; m6[2] = h2f * h2f;
+                        m6[3] = R(2) * h0f * h1f; m6[4] = R(2) * h0f * h2f; m6[5] = R(2) * h1f * h2f;
+                        const R q = adp[0] * m6[0] + adp[1] * m6[1] + adp[2] * m6[2] + adp[3] * m6[3] +
+                                    adp[4] * m6[4] + adp[5] * m6[5];
+                        const R T = texp<R>(-q);
+                        zre *= T; zim *= T;
+                    }
+                    R fre, fim;
+                    R A0 = 0, A1 = 0, A2 = 0, A3 = 0, A4 = 0;
+                    const R *y = rec.y;
+                    if (table_model) {
+                        if constexpr (F32) {
+                            const float2 tv = S.table_f[((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig];
+                            fre = tv.x + anre; fim = tv.y + anim;
+                        } else {
+                            const double2 tv = S.table_d[((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig];
+                            fre = tv.x + anre; fim = tv.y + anim;
+                        }
+                    } else if (hc_model) {
+                        A0 = pg[0] * y[0];
+                        A1 = pg[1] * y[1] + pg[2] * y[2] + pg[3] * y[3];
+                        A2 = pg[4] * y[4] + pg[5] * y[5] + pg[6] * y[6] + pg[7] * y[7] + pg[8] * y[8];
+                        A3 = pg[9] * y[9] + pg[10] * y[10] + pg[11] * y[11] + pg[12] * y[12] + pg[13] * y[13] +
+                             pg[14] * y[14] + pg[15] * y[15];
+                        A4 = pg[16] * y[16] + pg[17] * y[17] + pg[18] * y[18] + pg[19] * y[19] + pg[20] * y[20] +
+                             pg[21] * y[21] + pg[22] * y[22] + pg[23] * y[23] + pg[24] * y[24];
+                        fre = fsre + r0 * A0 + r2 * A2 + r4 * A4;
+                        fim = fsim + r1 * A1 + r3 * A3;
+                    } else {
+                        fre = fsre;
+                        fim = fsim;
+                    }
+                    const R ure = fre * zre - fim * zim;
+                    const R uim = fre * zim + fim * zre;
+                    Ure += ure; Uim += uim;
+                    Xre[0] += h0f * ure; Xim[0] += h0f * uim;
+                    Xre[1] += h1f * ure; Xim[1] += h1f * uim;
+                    Xre[2] += h2f * ure; Xim[2] += h2f * uim;
+                    if constexpr (ANISO) {
+#pragma unroll
+                        for (int q = 0; q < 6; q++) { Are[q] -= m6[q] * ure; Aim[q] -= m6[q] * uim; }
+                    }
+                    if constexpr (MP) {
+                        if (hc_model) {
+                            const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
+                            Ere += zre; Eim += zim;
+                            // q_l = Re(g i^l rr_l z): even l rs_l Re(gz), odd l -rs_l Im(gz)
+                            const R wre = gre * zre - gim * zim, wim = gre * zim + gim * zre;
+                            const R q0 = r0 * wre, q1 = -r1 * wim, q2 = r2 * wre, q3 = -r3 * wim, q4 = r4 * wre;
+                            part[CH_PLM] += q0 * y[0];
+#pragma unroll
+                            for (int q = 1; q < 4; q++) part[CH_PLM + q] += q1 * y[q];
+#pragma unroll
+                            for (int q = 4; q < 9; q++) part[CH_PLM + q] += q2 * y[q];
+#pragma unroll
+                            for (int q = 9; q < 16; q++) part[CH_PLM + q] += q3 * y[q];
+#pragma unroll
+                            for (int q = 16; q < 25; q++) part[CH_PLM + q] += q4 * y[q];
+                            const R dre = dr[2] * A0 + dr[4] * A2 + dr[6] * A4;
+                            const R dim = dr[3] * A1 + dr[5] * A3;
+                            Kre += dre * zre - dim * zim;
+                            Kim += dre * zim + dim * zre;
+                        }
+                    }
+                };
+                if constexpr (NSC > 0) {
+#pragma unroll
+                    for (int s = 0; s < NSC; s++) term(s);
+                } else {
+#pragma unroll 1
+                    for (int s = 0; s < nS; s++) term(s);
+                }
+                if (!ANISO && has_adp) {
+                    Ure *= Tiso; Uim *= Tiso;
+#pragma unroll
+                    for (int j = 0; j < 3; j++) { Xre[j] *= Tiso; Xim[j] *= Tiso; }
+                    if constexpr (MP) { Ere *= Tiso; Eim *= Tiso; Kre *= Tiso; Kim *= Tiso; }
+                }
+                Fre = w * Ure;
+                Fim = w * Uim;
+                const R gU = g.x * Ure - g.y * Uim;  // Re(g U)
+                part[CH_OCC] += gU;
+                if constexpr (ANISO) {
+#pragma unroll
+                    for (int q = 0; q < 6; q++) part[CH_ADP + q] += g.x * Are[q] - g.y * Aim[q];
+                } else {
+                    part[CH_ADP] -= sH2[hl] * gU;
+                }
+#pragma unroll
+                for (int j = 0; j < 3; j++) part[CH_XYZ + j] -= g.x * Xim[j] + g.y * Xre[j];  // -Im(g X)
+                if constexpr (MP) {
+                    const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
+                    const R gE = g.x * Ere - g.y * Eim;
+                    part[CH_PV] += dr[0] * gE;
+                    part[CH_KAPPA] += dr[1] * gE;
+                    part[CH_KAPPA_P] += g.x * Kre - g.y * Kim;
+                }
+            }
+            // block reduction of the partial F of this reflection
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                Fre += shfl_xor<R>(Fre, o);
+                Fim += shfl_xor<R>(Fim, o);
+            }
+            if (lane == 0) {
+                R2 v;
+                v.x = Fre; v.y = Fim;
+                sF[warp * ht + hl] = v;
+            }
+        }
+        // fold the sub-tile sums into the Kahan totals (each thread its own column)
+#pragma unroll
+        for (int q = 0; q < NT; q++) {
+            R sum = sTot[q * kTileAtoms + tid], comp = sCmp[q * kTileAtoms + tid];
+            const R yv = part[q] - comp;
+            const R tv = sum + yv;
+            comp = (tv - sum) - yv;
+            sTot[q * kTileAtoms + tid] = tv;
+            sCmp[q * kTileAtoms + tid] = comp;
+        }
+        __syncthreads();
+        for (int i = tid; i < nh; i += blockDim.x) {
+            R sre = 0, sim = 0;
+#pragma unroll
+            for (int wp = 0; wp < kWarps; wp++) {
+                const R2 v = sF[wp * ht + i];
+                sre += v.x;
+                sim += v.y;
+            }
+            atomicAdd(&C.f_acc[h0 + i].x, (double)sre);
+            atomicAdd(&C.f_acc[h0 + i].y, (double)sim);
+        }
+        __syncthreads();
+    }
+    if (active) {
+        double *G = C.g_acc + (size_t)a * kNch;
+        auto total = [&](int q) {
+            return (double)sTot[q * kTileAtoms + tid] - (double)sCmp[q * kTileAtoms + tid];
+        };
+#pragma unroll
+        for (int j = 0; j < 3; j++) atomicAdd(G + CH_XYZ + j, total(CH_XYZ + j));
+        if (ANISO) {
+#pragma unroll
+            for (int q = 0; q < 6; q++) atomicAdd(G + CH_ADP + q, total(CH_ADP + q));
+        } else if (has_adp) {
+            atomicAdd(G + CH_ADP, total(CH_ADP));
+        }
+        atomicAdd(G + CH_OCC, total(CH_OCC));
+        if constexpr (MP) {
+#pragma unroll
+            for (int q = CH_PV; q < NT; q++) atomicAdd(G + q, total(q));
+        }
+    }
+}
+
+}  // namespace dsf
