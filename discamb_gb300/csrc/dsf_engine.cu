@@ -33,8 +33,8 @@ cudaError_t launch_rs_prep(const DevStructure &S, int n_hkl_pad, void *rs_f, voi
 cudaError_t launch_tr_prep(const DevStructure &S, int n_hkl_pad, void *tr_f, void *tr_d, void *trm_f, void *trm_d,
                            bool mp, cudaStream_t st);
 size_t rs_record_bytes(bool fp64);
-size_t sf2_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types);
-cudaError_t launch_sf2(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool fp64, bool mp, bool aniso,
+size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types);
+cudaError_t launch_sf3(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool fp64, bool mp, bool aniso,
                        int n_tiles, int n_chunks, cudaStream_t st);
 cudaError_t launch_sf_grad(const DevStructure &S, const CallBuffers &C, bool fp64, bool mp, int hkl_chunk, int ht,
                            cudaStream_t st);
@@ -206,7 +206,8 @@ struct dsf_structure {
         d_active, d_xq, d_xlo, d_xd, d_adp_f, d_adp_d, d_w_f, d_w_d, d_anom_f, d_anom_d, d_pg_f, d_pg_d, d_types,
         d_types_f, d_tcoeff, d_texp, d_tpow, d_texp_f, d_tpre_f, d_hkl, d_h2, d_h2f, d_hmult, d_cinv, d_table_f, d_table_d, d_perm, d_multw, d_dmat,
         d_raw, d_dtdf, d_gw_d, d_gw_f, d_facc, d_gacc, d_out, d_plm_lmax,
-        d_rs_f, d_rs_d, d_tr_f, d_tr_d, d_trm_f, d_trm_d, d_err;
+        d_rs_f, d_rs_d, d_tr_f, d_tr_d, d_trm_f, d_trm_d, d_err, d_hperm, d_cont, d_tile_lmax;
+    std::vector<int> hperm;  // line-ordered reflection -> caller's index
     int n_hkl_pad = 0;
     bool tr_valid = false, trm_valid = false;
     int n_tiles_plain = 0;   // tiles [0, n_tiles_plain) hold atoms without anisotropic ADPs
@@ -227,12 +228,13 @@ namespace {
 // g = conj(dT/dF) * centering multiplier; effective weight of the
 // centrosymmetric forms: 2 Re g (inversion at origin), g + conj(g c_inv) (shifted)
 __global__ void gw_kernel(int n, const double2 *dtdf, const double *mult, const double2 *cinv, int centro,
-                          double2 *gw_d, float2 *gw_f)
+                          double2 *gw_d, float2 *gw_f, const int *perm)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double m = mult[i];
-    double gre = dtdf[i].x * m, gim = -dtdf[i].y * m;
+    const int o = perm ? perm[i] : i;
+    double gre = dtdf[o].x * m, gim = -dtdf[o].y * m;
     if (centro == 1) {
         gre = 2.0 * gre;
         gim = 0.0;
@@ -247,7 +249,7 @@ __global__ void gw_kernel(int n, const double2 *dtdf, const double *mult, const 
 }
 
 __global__ void f_epilogue_kernel(int n, const double2 *facc, const double *mult, const double2 *cinv, int centro,
-                                  double *f_out)
+                                  double *f_out, const int *perm)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -263,8 +265,9 @@ __global__ void f_epilogue_kernel(int n, const double2 *facc, const double *mult
         F.x = re;
         F.y = im;
     }
-    f_out[2 * i] = F.x * mult[i];
-    f_out[2 * i + 1] = F.y * mult[i];
+    const int o = perm ? perm[i] : i;
+    f_out[2 * o] = F.x * mult[i];
+    f_out[2 * o + 1] = F.y * mult[i];
 }
 
 struct GradParams {
@@ -557,7 +560,13 @@ int compute_global_plm(dsf_structure *s)
         const int t = s->atom_type[s->perm[a]];
         lmx[a] = std::min(std::min(s->type_nl[t] - 1, s->trad[t].n_def - 1), 4);
     }
+    // per tile: highest l of the angular sums (tiles of hydrogen-like types skip l = 3, 4)
+    std::vector<int> tl(s->n_tiles, -1);
+    for (int t = 0; t < s->n_tiles; t++)
+        for (int a = s->tile_begin[t]; a < s->tile_begin[t + 1]; a++)
+            tl[t] = std::max(tl[t], s->trad[s->atom_type[s->perm[a]]].lmax_used);
     int rc;
+    if ((rc = upload(e, s->d_tile_lmax, tl.data(), tl.size()))) return rc;
     if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return rc;
     if ((rc = upload(e, s->d_pg_d, pg.data(), pg.size()))) return rc;
     if ((rc = upload(e, s->d_pg_f, pgf.data(), pgf.size()))) return rc;
@@ -880,13 +889,13 @@ double host_centering_multiplier(char c, int obverse, int h, int k, int l)
 cudaError_t launch_adjoint_weights(int n, const double2 *dtdf, const double *mult, const double2 *cinv, int centro,
                                    double2 *gw_d, float2 *gw_f, cudaStream_t st)
 {
-    gw_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, dtdf, mult, cinv, centro, gw_d, gw_f);
+    gw_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, dtdf, mult, cinv, centro, gw_d, gw_f, nullptr);
     return cudaGetLastError();
 }
 cudaError_t launch_f_epilogue(int n, const double2 *facc, const double *mult, const double2 *cinv, int centro,
                               double *f_out, cudaStream_t st)
 {
-    f_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, facc, mult, cinv, centro, f_out);
+    f_epilogue_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, facc, mult, cinv, centro, f_out, nullptr);
     return cudaGetLastError();
 }
 cudaError_t launch_grad_epilogue(int n_atoms, int xyz_conv, const double *Minv, const double *A6, int flags,
@@ -1063,8 +1072,9 @@ int dsf_structure_create_iam(dsf_engine *e, const dsf_symmetry *sym, const dsf_i
     s->dmat.assign(165 * (size_t)s->n_atoms, 0.0);
     if ((rc = upload(e, s->d_dmat, s->dmat.data(), s->dmat.size()))) return bail(rc);
     {
-        std::vector<int> lmx(s->n_atoms, -1);
+        std::vector<int> lmx(s->n_atoms, -1), tl(s->n_tiles, -1);
         if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return bail(rc);
+        if ((rc = upload(e, s->d_tile_lmax, tl.data(), tl.size()))) return bail(rc);
     }
     if ((rc = finish_create(e, s))) return bail(rc);
     e->live_structures++;
@@ -1093,19 +1103,34 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
     s->dmat.assign(165 * (size_t)s->n_atoms, 0.0);
     if ((rc = upload(e, s->d_dmat, s->dmat.data(), s->dmat.size()))) return bail(rc);
     {
-        std::vector<int> lmx(s->n_atoms, -1);
+        std::vector<int> lmx(s->n_atoms, -1), tl(s->n_tiles, -1);
         if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return bail(rc);
+        if ((rc = upload(e, s->d_tile_lmax, tl.data(), tl.size()))) return bail(rc);
     }
-    const size_t nel = (size_t)n_hkl * s->n_sym * s->n_atoms;
-    if (table_fp32) {
-        std::vector<float> tf(2 * nel);
-        for (size_t i = 0; i < 2 * nel; i++) tf[i] = (float)table[i];
-        if ((rc = upload(e, s->d_table_f, tf.data(), tf.size()))) return bail(rc);
+    // rows in the engine's line order (the order dsf_structure_set_hkl gives the reflections), padded with
+    // zero rows to a multiple of 16 reflections: the kernel reads whole sub-tiles
+    const int n_pad = (n_hkl + 15) / 16 * 16;
+    std::vector<int> order(n_hkl);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        for (int j = 0; j < 3; j++)
+            if (hkl[3 * x + j] != hkl[3 * y + j]) return hkl[3 * x + j] < hkl[3 * y + j];
+        return false;
+    });
+    const size_t row = (size_t)s->n_sym * s->n_atoms;  // complex values per reflection
+    std::vector<float> tf(2 * row * n_pad, 0.0f);
+    for (int i = 0; i < n_hkl; i++)
+        for (size_t q = 0; q < 2 * row; q++) tf[2 * row * i + q] = (float)table[2 * row * order[i] + q];
+    if ((rc = upload(e, s->d_table_f, tf.data(), tf.size()))) return bail(rc);
+    if (!table_fp32) {
+        std::vector<double> td(2 * row * n_pad, 0.0);
+        for (int i = 0; i < n_hkl; i++)
+            for (size_t q = 0; q < 2 * row; q++) td[2 * row * i + q] = table[2 * row * order[i] + q];
+        if ((rc = upload(e, s->d_table_d, td.data(), td.size()))) return bail(rc);
     } else {
-        if ((rc = upload(e, s->d_table_d, table, 2 * nel))) return bail(rc);
-        std::vector<float> tf(2 * nel);
-        for (size_t i = 0; i < 2 * nel; i++) tf[i] = (float)table[i];
-        if ((rc = upload(e, s->d_table_f, tf.data(), tf.size()))) return bail(rc);
+        // the plain form reads the FP32 values widened
+        std::vector<double> td(tf.begin(), tf.end());
+        if ((rc = upload(e, s->d_table_d, td.data(), td.size()))) return bail(rc);
     }
     if ((rc = finish_create(e, s))) return bail(rc);
     s->eng->live_structures++;
@@ -1125,7 +1150,8 @@ int dsf_structure_destroy(dsf_structure *s)
                       &s->d_types, &s->d_types_f, &s->d_tcoeff, &s->d_texp, &s->d_tpow, &s->d_texp_f, &s->d_tpre_f, &s->d_hkl, &s->d_h2, &s->d_h2f, &s->d_hmult,
                       &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw, &s->d_dmat, &s->d_raw,
                       &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc, &s->d_out, &s->d_plm_lmax,
-                      &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d, &s->d_trm_f, &s->d_trm_d, &s->d_err};
+                      &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d, &s->d_trm_f, &s->d_trm_d, &s->d_err,
+                      &s->d_hperm, &s->d_cont, &s->d_tile_lmax};
     for (DevBuf *b : bufs) b->release();
     if (s->ev_begin) cudaEventDestroy(s->ev_begin);
     if (s->ev_end) cudaEventDestroy(s->ev_end);
@@ -1143,10 +1169,24 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
         return fail(e, DSF_ERR_ARGUMENT, "tabulated structures keep the reflection set of their table");
     cudaSetDevice(e->device);
     const int n_pad = (n_hkl + 15) / 16 * 16;  // tables and per-reflection arrays padded with zero rows
+    // line order: sorted by (h, k, l) so runs of l + 1 share a lattice line
+    s->hperm.resize(n_hkl);
+    std::iota(s->hperm.begin(), s->hperm.end(), 0);
+    std::stable_sort(s->hperm.begin(), s->hperm.end(), [&](int x, int y) {
+        for (int j = 0; j < 3; j++)
+            if (hkl[3 * x + j] != hkl[3 * y + j]) return hkl[3 * x + j] < hkl[3 * y + j];
+        return false;
+    });
+    std::vector<int> cont(n_pad, 0);
+    for (int i = 1; i < n_hkl; i++) {
+        const int *p = hkl + 3 * s->hperm[i - 1], *q = hkl + 3 * s->hperm[i];
+        cont[i] = (p[0] == q[0] && p[1] == q[1] && q[2] == p[2] + 1) ? 1 : 0;
+    }
     std::vector<int4> h4(n_pad, make_int4(0, 0, 0, 0));
     std::vector<double> h2(n_pad, 0.0), mult(n_pad, 0.0), cinv(2 * (size_t)n_pad, 0.0);
     for (int i = 0; i < n_hkl; i++) {
-        const int h = hkl[3 * i], k = hkl[3 * i + 1], l = hkl[3 * i + 2];
+        const int *hp = hkl + 3 * s->hperm[i];
+        const int h = hp[0], k = hp[1], l = hp[2];
         h4[i] = make_int4(h, k, l, 0);
         double c[3];
         for (int j = 0; j < 3; j++) c[j] = s->B[3 * j] * h + s->B[3 * j + 1] * k + s->B[3 * j + 2] * l;
@@ -1163,6 +1203,8 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
         }
     }
     int rc;
+    if ((rc = upload(e, s->d_hperm, s->hperm.data(), s->hperm.size()))) return rc;
+    if ((rc = upload(e, s->d_cont, cont.data(), cont.size()))) return rc;
     if ((rc = upload(e, s->d_hkl, h4.data(), h4.size()))) return rc;
     if ((rc = upload(e, s->d_h2, h2.data(), h2.size()))) return rc;
     {
@@ -1283,7 +1325,7 @@ int64_t dsf_structure_device_bytes(const dsf_structure *s)
                             &s->d_hmult, &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw,
                             &s->d_dmat, &s->d_raw, &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc,
                             &s->d_out, &s->d_plm_lmax, &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d,
-                            &s->d_trm_f, &s->d_trm_d, &s->d_err};
+                            &s->d_trm_f, &s->d_trm_d, &s->d_err, &s->d_hperm, &s->d_cont, &s->d_tile_lmax};
     int64_t b = 0;
     for (const DevBuf *p : bufs) b += (int64_t)p->bytes;
     return b;
@@ -1320,7 +1362,8 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     int launches = 0;
     gw_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, reinterpret_cast<const double2 *>(dtdf_device),
                                                    s->d_hmult.as<double>(), s->d_cinv.as<double2>(), s->centro_mode,
-                                                   s->d_gw_d.as<double2>(), s->d_gw_f.as<float2>());
+                                                   s->d_gw_d.as<double2>(), s->d_gw_f.as<float2>(),
+                                                   s->d_hperm.as<int>());
     launches++;
     DSF_CUDA(cudaGetLastError());
     DSF_CUDA(cudaMemsetAsync(s->d_facc.p, 0, 16 * (size_t)n_hkl, st));
@@ -1340,6 +1383,8 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     L.tr = fp64 ? s->d_tr_d.p : s->d_tr_f.p;
     L.trm = fp64 ? s->d_trm_d.p : s->d_trm_f.p;
     L.error = s->d_err.as<int>();
+    L.cont = s->d_cont.as<int>();
+    L.tile_lmax = s->d_tile_lmax.as<int>();
     if (!s->ev_begin) {
         DSF_CUDA(cudaEventCreate(&s->ev_begin));
         DSF_CUDA(cudaEventCreate(&s->ev_end));
@@ -1355,8 +1400,8 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         // reflections per sub-tile from the shared-memory budget (several blocks per SM)
         int ht = kMaxHT;
         const size_t budget = std::min<size_t>(e->max_smem, fp64 ? 200 * 1024 : 100 * 1024);
-        while (ht > 4 && sf2_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > budget) ht /= 2;
-        if (sf2_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > e->max_smem)
+        while (ht > 4 && sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > budget) ht /= 2;
+        if (sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > e->max_smem)
             return fail(e, DSF_ERR_UNSUPPORTED, "shared-memory tile does not fit this device");
         L.ht = ht;
         // reflection chunks so the grid covers the SMs several times
@@ -1367,12 +1412,13 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         chunk = (chunk + ht - 1) / ht * ht;
         L.hkl_chunk = chunk;
         const int n_chunks = (n_hkl + chunk - 1) / chunk;
-        DSF_CUDA(launch_sf2(s->dev, C, L, fp64, mp, kind == 1, nt, n_chunks, st));
+        DSF_CUDA(launch_sf3(s->dev, C, L, fp64, mp, kind == 1, nt, n_chunks, st));
         launches++;
     }
     DSF_CUDA(cudaEventRecord(s->ev_end, st));
     f_epilogue_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, s->d_facc.as<double2>(), s->d_hmult.as<double>(),
-                                                           s->d_cinv.as<double2>(), s->centro_mode, out->f);
+                                                           s->d_cinv.as<double2>(), s->centro_mode, out->f,
+                                                           s->d_hperm.as<int>());
     launches++;
     DSF_CUDA(cudaGetLastError());
     if (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) {

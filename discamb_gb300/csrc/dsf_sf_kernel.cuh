@@ -155,20 +155,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 // kernel
 // ---------------------------------------------------------------------------
 struct SfLaunch {
-    int hkl_chunk;   // reflections per block (multiple of ht)
-    int ht;          // reflections per shared-memory sub-tile (multiple of 4)
-    int tile_offset; // first tile of this launch
-    int max_types;   // largest number of types in a tile of this launch
-    int n_hkl_pad;   // padded reflection count of the tables
-    const void *rs;  // RsRec<R> [n_hkl_pad][n_sym]
-    const void *tr;  // R [n_types][n_hkl_pad][8]
-    const void *trm; // R [n_types][n_hkl_pad][8] (multipole adjoint)
-    int *error;      // set to 1 on a timed-out wait
+    int hkl_chunk;         // reflections per block (multiple of ht)
+    int ht;                // reflections per shared-memory sub-tile (multiple of 4, divides 16)
+    int tile_offset;       // first tile of this launch
+    int max_types;         // largest number of types in a tile of this launch
+    int n_hkl_pad;         // padded reflection count of the tables (multiple of 16)
+    const void *rs;        // RsRec<R> [n_hkl_pad][n_sym]
+    const void *tr;        // R [n_types][n_hkl_pad][8]
+    const void *trm;       // R [n_types][n_hkl_pad][8] (multipole adjoint)
+    const int *cont;       // [n_hkl_pad] 1: reflection = previous one + (0,0,1) (reflections in line order)
+    const int *tile_lmax;  // [n_tiles] highest l of the angular sums of the tile's atoms
+    int *error;            // set to 1 on a timed-out wait
 };
 
 template <typename R>
 struct StageLayout {
-    size_t rs, tr, trm, gw, h2, bytes;
+    size_t rs, tr, trm, gw, h2, cont, bytes;
     __host__ __device__ StageLayout(int ht, int ns, int max_types, bool mp)
     {
         rs = 0;
@@ -176,7 +178,8 @@ struct StageLayout {
         trm = tr + sizeof(R) * 8 * (size_t)ht * max_types;
         gw = trm + (mp ? sizeof(R) * 8 * (size_t)ht * max_types : 0);
         h2 = gw + sizeof(R) * 2 * (size_t)ht;
-        bytes = h2 + sizeof(R) * (size_t)ht;
+        cont = h2 + sizeof(R) * (size_t)ht;
+        bytes = cont + sizeof(int) * (size_t)ht;
         bytes = (bytes + 15) & ~(size_t)15;
     }
 };
@@ -196,14 +199,52 @@ __host__ __device__ inline size_t sf_smem_bytes(int ht, int ns, int max_types)
     return b;
 }
 
-template <typename R, bool MP, bool ANISO, int NSC>
+// e^{2 pi i phi}: FP32 from the fixed-point phase, FP64 from h'.x + h.t reduced mod 1
+template <typename R>
+struct PhaseOps;
+template <>
+struct PhaseOps<float> {
+    static __device__ __forceinline__ void exact(const RsRec<float> &rec, uint32_t xq0, uint32_t xq1, uint32_t xq2,
+                                                 float x0, float x1, float x2, float *sn, float *cs)
+    {
+        const int4 hi = rec.hi;
+        const uint32_t P = (uint32_t)hi.x * xq0 + (uint32_t)hi.y * xq1 + (uint32_t)hi.z * xq2 + (uint32_t)hi.w;
+        sincos_fixed(P, rec.hf[0] * x0 + rec.hf[1] * x1 + rec.hf[2] * x2, sn, cs);
+    }
+};
+template <>
+struct PhaseOps<double> {
+    static __device__ __forceinline__ void exact(const RsRec<double> &rec, uint32_t, uint32_t, uint32_t, double x0,
+                                                 double x1, double x2, double *sn, double *cs)
+    {
+        double ph = rec.hf[0] * x0 + rec.hf[1] * x1 + rec.hf[2] * x2 + rec.hf[3];
+        ph -= rint(ph);
+        sincospi(2.0 * ph, sn, cs);
+    }
+};
+
+// Reflections that continue a lattice line (h, k, l) -> (h, k, l+1) get their
+// phase factors by one complex multiplication with the per-atom, per-operation
+// step e^{2 pi i ((R^T e_l).x + e_l.t)} (the reference engine's line
+// recurrence, scattering_utilities::calculate_line_phase_factors,
+// src/Scattering/scattering_utilities.cpp:575-627); the exact phase is
+// re-anchored at every line start, at every sub-tile start and, in the FP32
+// form, every kAnchorF32 reflections so the FP32 rounding of the step cannot
+// build up.
+constexpr int kAnchorF32 = 4;
+
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC>
 __global__ void __launch_bounds__(kTileAtoms)
-sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
+sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
 {
     using R2 = typename Vec2<R>::T;
     constexpr bool F32 = sizeof(R) == 4;
     constexpr int NT = n_channels<R, MP>();
     constexpr int kWarps = kTileAtoms / 32;
+    constexpr bool HC = MODEL == MODEL_HC;
+    constexpr bool TABLE = MODEL == MODEL_TABLE;
+    constexpr bool REC = NSC > 0;                 // line recurrence (register arrays need a fixed count)
+    constexpr int NR = NSC > 0 ? NSC : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nS = NSC > 0 ? NSC : S.n_sym;
     const int ht = L.ht;
@@ -214,8 +255,7 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
     const int a_begin = S.tile_begin[tile], a_end = S.tile_begin[tile + 1];
     const int nT = S.tile_ntypes[tile];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool hc_model = S.model == MODEL_HC;
-    const bool table_model = S.model == MODEL_TABLE;
+    const bool high_l = HC && L.tile_lmax[tile] >= 3;  // uniform over the block
 
     // shared memory carve-up
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);  // [2]
@@ -254,21 +294,23 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
     // thread 0 streams a sub-tile of the tables into one stage buffer
     auto issue = [&](int buf, int h0) {
         unsigned char *st = stage0 + buf * SL.bytes;
-        uint32_t bytes = (uint32_t)(sizeof(RsRec<R>) * ht * nS) + (uint32_t)(2 * sizeof(R) * ht) +
-                         (uint32_t)(sizeof(R) * ht) + (uint32_t)(sizeof(R) * 8 * ht) * nT * (MP ? 2u : 1u);
+        const uint32_t rs_bytes = (uint32_t)(sizeof(RsRec<R>) * ht * nS);
+        const uint32_t tr_bytes = (uint32_t)(sizeof(R) * 8 * ht);
+        const uint32_t bytes = rs_bytes + (uint32_t)(2 * sizeof(R) * ht) + (uint32_t)(sizeof(R) * ht) +
+                               (uint32_t)(sizeof(int) * ht) + (TABLE ? 0u : tr_bytes * nT * (MP ? 2u : 1u));
         fence_proxy_async();
         mbar_expect_tx(&bar[buf], bytes);
-        bulk_copy(st + SL.rs, rs_g + (size_t)h0 * nS, (uint32_t)(sizeof(RsRec<R>) * ht * nS), &bar[buf]);
-        for (int t = 0; t < nT; t++) {
-            const size_t row = ((size_t)sTypes[t] * L.n_hkl_pad + h0) * 8;
-            bulk_copy(st + SL.tr + sizeof(R) * 8 * (size_t)ht * t, tr_g + row, (uint32_t)(sizeof(R) * 8 * ht),
-                      &bar[buf]);
-            if constexpr (MP)
-                bulk_copy(st + SL.trm + sizeof(R) * 8 * (size_t)ht * t, trm_g + row,
-                          (uint32_t)(sizeof(R) * 8 * ht), &bar[buf]);
+        bulk_copy(st + SL.rs, rs_g + (size_t)h0 * nS, rs_bytes, &bar[buf]);
+        if constexpr (!TABLE) {
+            for (int t = 0; t < nT; t++) {
+                const size_t row = ((size_t)sTypes[t] * L.n_hkl_pad + h0) * 8;
+                bulk_copy(st + SL.tr + (size_t)tr_bytes * t, tr_g + row, tr_bytes, &bar[buf]);
+                if constexpr (MP) bulk_copy(st + SL.trm + (size_t)tr_bytes * t, trm_g + row, tr_bytes, &bar[buf]);
+            }
         }
         bulk_copy(st + SL.gw, gw_g + h0, (uint32_t)(2 * sizeof(R) * ht), &bar[buf]);
         bulk_copy(st + SL.h2, h2_g + h0, (uint32_t)(sizeof(R) * ht), &bar[buf]);
+        bulk_copy(st + SL.cont, L.cont + h0, (uint32_t)(sizeof(int) * ht), &bar[buf]);
     };
 
     // per-atom registers
@@ -276,13 +318,16 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
     const bool have = a < a_end;
     bool active = false;
     int lt = 0;
-    R w = R(0), pg[25], adp[ANISO ? 6 : 1];
+    R w = R(0), pg[HC ? 25 : 1], adp[ANISO ? 6 : 1];
     R anre = R(0), anim = R(0);
     uint32_t xq0 = 0, xq1 = 0, xq2 = 0;
     R x0 = R(0), x1 = R(0), x2 = R(0);  // FP32: low parts (turns); FP64: coordinates
     bool has_adp = false;
+    R step_re[NR], step_im[NR], e_re[NR], e_im[NR];
 #pragma unroll
-    for (int q = 0; q < 25; q++) pg[q] = R(0);
+    for (int q = 0; q < NR; q++) { step_re[q] = R(1); step_im[q] = R(0); e_re[q] = R(1); e_im[q] = R(0); }
+#pragma unroll
+    for (int q = 0; q < (HC ? 25 : 1); q++) pg[q] = R(0);
 #pragma unroll
     for (int q = 0; q < (ANISO ? 6 : 1); q++) adp[q] = R(0);
     if (have) {
@@ -297,7 +342,7 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
             x0 = S.atom_xlo[3 * a]; x1 = S.atom_xlo[3 * a + 1]; x2 = S.atom_xlo[3 * a + 2];
 #pragma unroll
             for (int q = 0; q < (ANISO ? 6 : 1); q++) adp[q] = S.atom_adp_f[6 * a + q];
-            if (hc_model)
+            if constexpr (HC)
 #pragma unroll
                 for (int q = 0; q < 25; q++) pg[q] = S.atom_pg_f[25 * a + q];
         } else {
@@ -307,9 +352,23 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
             x0 = S.atom_xd[3 * a]; x1 = S.atom_xd[3 * a + 1]; x2 = S.atom_xd[3 * a + 2];
 #pragma unroll
             for (int q = 0; q < (ANISO ? 6 : 1); q++) adp[q] = S.atom_adp_d[6 * a + q];
-            if (hc_model)
+            if constexpr (HC)
 #pragma unroll
                 for (int q = 0; q < 25; q++) pg[q] = S.atom_pg_d[25 * a + q];
+        }
+        if constexpr (REC) {
+            // line steps in FP64, rounded once
+            const double xa = S.atom_xd[3 * a], xb = S.atom_xd[3 * a + 1], xc = S.atom_xd[3 * a + 2];
+#pragma unroll
+            for (int s = 0; s < NR; s++) {
+                const int *Rm = S.sym_rot + 9 * s;
+                double ph = Rm[6] * xa + Rm[7] * xb + Rm[8] * xc + S.sym_t24[3 * s + 2] / 24.0;
+                ph -= rint(ph);
+                double sn, cs;
+                sincospi(2.0 * ph, &sn, &cs);
+                step_re[s] = R(cs);
+                step_im[s] = R(sn);
+            }
         }
     }
     const int a_orig = have ? S.atom_orig[a] : 0;
@@ -319,7 +378,6 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
     int k = 0;
     for (int h0 = h_begin; h0 < h_end; h0 += ht, k++) {
         const int buf = k & 1;
-        const int nh = min(ht, h_end - h0);
         if (tid == 0 && h0 + ht < h_end) issue(buf ^ 1, h0 + ht);
         const bool ok = mbar_wait(&bar[buf], parity[buf]);
         parity[buf] ^= 1u;
@@ -336,89 +394,107 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
         const R *sTrm = reinterpret_cast<const R *>(st + SL.trm);
         const R2 *sG = reinterpret_cast<const R2 *>(st + SL.gw);
         const R *sH2 = reinterpret_cast<const R *>(st + SL.h2);
+        const int *sCont = reinterpret_cast<const int *>(st + SL.cont);
 
         R part[NT];
 #pragma unroll
         for (int q = 0; q < NT; q++) part[q] = R(0);
 
-        for (int hl = 0; hl < nh; hl++) {
-            R Fre = R(0), Fim = R(0);
-            if (active) {
-                const R2 g = sG[hl];
-                const R *rad = sTr + (size_t)(lt * ht + hl) * 8;
-                const R fsre = rad[0] + anre, fsim = anim;
-                const R r0 = rad[1], r1 = rad[2], r2 = rad[3], r3 = rad[4], r4 = rad[5];
-                R Tiso = R(1);
-                if (!ANISO && has_adp) Tiso = texp<R>(-adp[0] * sH2[hl]);
-                const R gre = g.x * Tiso, gim = g.y * Tiso;  // adjoint weight with the isotropic factor
-                R Ure = 0, Uim = 0;
-                R Xre[3] = {0, 0, 0}, Xim[3] = {0, 0, 0};
-                R Are[ANISO ? 6 : 1], Aim[ANISO ? 6 : 1];
+        // reflections in groups of four: the partial F of a group is reduced across
+        // the warp by one butterfly reduce-scatter of its eight values
+        for (int g0 = 0; g0 < ht; g0 += 4) {
+            R Fv[8];
 #pragma unroll
-                for (int q = 0; q < (ANISO ? 6 : 1); q++) { Are[q] = R(0); Aim[q] = R(0); }
-                R Ere = 0, Eim = 0, Kre = 0, Kim = 0;
-                const RsRec<R> *recs = sRs + (size_t)hl * nS;
-                auto term = [&](int s) {
-                    const RsRec<R> &rec = recs[s];
-                    const R h0f = rec.hf[0], h1f = rec.hf[1], h2f = rec.hf[2];
-                    R sn, cs;
-                    if constexpr (F32) {
-                        const int4 hi = rec.hi;
-                        const uint32_t P = (uint32_t)hi.x * xq0 + (uint32_t)hi.y * xq1 + (uint32_t)hi.z * xq2 +
-                                           (uint32_t)hi.w;
-                        sincos_fixed(P, h0f * x0 + h1f * x1 + h2f * x2, &sn, &cs);
-                    } else {
-                        double ph = h0f * x0 + h1f * x1 + h2f * x2 + rec.hf[3];
-                        ph -= rint(ph);
-                        sincospi(2.0 * ph, &sn, &cs);
+            for (int q = 0; q < 8; q++) Fv[q] = R(0);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int hl = g0 + j;
+                const bool anchor = !REC || sCont[hl] == 0 || hl == 0 || (F32 && (hl % kAnchorF32) == 0);
+                if (active) {
+                    const R2 g = sG[hl];
+                    R fsre = anre, fsim = anim, r0 = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0;
+                    const R *rad = sTr + (size_t)(lt * ht + hl) * 8;
+                    if constexpr (!TABLE) {
+                        fsre += rad[0];
+                        r0 = rad[1]; r1 = rad[2]; r2 = rad[3]; r3 = rad[4]; r4 = rad[5];
                     }
-                    R zre = cs, zim = sn;  // e^{i theta} T_s
-                    R m6[ANISO ? 6 : 1];
-                    if constexpr (ANISO) {
-                        m6[0] = h0f * h0f; m6[1] = h1f * h1f; m6[2] = h2f * h2f;
-                        m6[3] = R(2) * h0f * h1f; m6[4] = R(2) * h0f * h2f; m6[5] = R(2) * h1f * h2f;
-                        const R q = adp[0] * m6[0] + adp[1] * m6[1] + adp[2] * m6[2] + adp[3] * m6[3] +
-                                    adp[4] * m6[4] + adp[5] * m6[5];
-                        const R T = texp<R>(-q);
-                        zre *= T; zim *= T;
-                    }
-                    R fre, fim;
-                    R A0 = 0, A1 = 0, A2 = 0, A3 = 0, A4 = 0;
-                    const R *y = rec.y;
-                    if (table_model) {
-                        if constexpr (F32) {
-                            const float2 tv = S.table_f[((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig];
-                            fre = tv.x + anre; fim = tv.y + anim;
+                    R Tiso = R(1);
+                    if (!ANISO && has_adp) Tiso = texp<R>(-adp[0] * sH2[hl]);
+                    const R gre = g.x * Tiso, gim = g.y * Tiso;  // adjoint weight with the isotropic factor
+                    R Ure = 0, Uim = 0;
+                    R Xre[3] = {0, 0, 0}, Xim[3] = {0, 0, 0};
+                    R Are[ANISO ? 6 : 1], Aim[ANISO ? 6 : 1];
+#pragma unroll
+                    for (int q = 0; q < (ANISO ? 6 : 1); q++) { Are[q] = R(0); Aim[q] = R(0); }
+                    R Ere = 0, Eim = 0, Kre = 0, Kim = 0;
+                    const RsRec<R> *recs = sRs + (size_t)hl * nS;
+                    auto term = [&](int s) {
+                        const RsRec<R> &rec = recs[s];
+                        const R h0f = rec.hf[0], h1f = rec.hf[1], h2f = rec.hf[2];
+                        R cs, sn;
+                        if constexpr (REC) {
+                            if (anchor) {
+                                PhaseOps<R>::exact(rec, xq0, xq1, xq2, x0, x1, x2, &sn, &cs);
+                            } else {
+                                cs = e_re[s] * step_re[s] - e_im[s] * step_im[s];
+                                sn = e_re[s] * step_im[s] + e_im[s] * step_re[s];
+                            }
+                            e_re[s] = cs;
+                            e_im[s] = sn;
                         } else {
-                            const double2 tv = S.table_d[((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig];
-                            fre = tv.x + anre; fim = tv.y + anim;
+                            PhaseOps<R>::exact(rec, xq0, xq1, xq2, x0, x1, x2, &sn, &cs);
                         }
-                    } else if (hc_model) {
-                        A0 = pg[0] * y[0];
-                        A1 = pg[1] * y[1] + pg[2] * y[2] + pg[3] * y[3];
-                        A2 = pg[4] * y[4] + pg[5] * y[5] + pg[6] * y[6] + pg[7] * y[7] + pg[8] * y[8];
-                        A3 = pg[9] * y[9] + pg[10] * y[10] + pg[11] * y[11] + pg[12] * y[12] + pg[13] * y[13] +
-                             pg[14] * y[14] + pg[15] * y[15];
-                        A4 = pg[16] * y[16] + pg[17] * y[17] + pg[18] * y[18] + pg[19] * y[19] + pg[20] * y[20] +
-                             pg[21] * y[21] + pg[22] * y[22] + pg[23] * y[23] + pg[24] * y[24];
-                        fre = fsre + r0 * A0 + r2 * A2 + r4 * A4;
-                        fim = fsim + r1 * A1 + r3 * A3;
-                    } else {
-                        fre = fsre;
-                        fim = fsim;
-                    }
-                    const R ure = fre * zre - fim * zim;
-                    const R uim = fre * zim + fim * zre;
-                    Ure += ure; Uim += uim;
-                    Xre[0] += h0f * ure; Xim[0] += h0f * uim;
-                    Xre[1] += h1f * ure; Xim[1] += h1f * uim;
-                    Xre[2] += h2f * ure; Xim[2] += h2f * uim;
-                    if constexpr (ANISO) {
+                        R zre = cs, zim = sn;  // e^{i theta} T_s
+                        R m6[ANISO ? 6 : 1];
+                        if constexpr (ANISO) {
+                            m6[0] = h0f * h0f; m6[1] = h1f * h1f; m6[2] = h2f * h2f;
+                            m6[3] = R(2) * h0f * h1f; m6[4] = R(2) * h0f * h2f; m6[5] = R(2) * h1f * h2f;
+                            const R q = adp[0] * m6[0] + adp[1] * m6[1] + adp[2] * m6[2] + adp[3] * m6[3] +
+                                        adp[4] * m6[4] + adp[5] * m6[5];
+                            const R T = texp<R>(-q);
+                            zre *= T; zim *= T;
+                        }
+                        R fre, fim;
+                        R A0 = 0, A1 = 0, A2 = 0, A3 = 0, A4 = 0;
+                        const R *y = rec.y;
+                        if constexpr (TABLE) {
+                            // the table holds n_hkl_pad rows (zero past the last reflection)
+                            const size_t ti = ((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig;
+                            if constexpr (F32) {
+                                const float2 tv = S.table_f[ti];
+                                fre = tv.x + anre; fim = tv.y + anim;
+                            } else {
+                                const double2 tv = S.table_d[ti];
+                                fre = tv.x + anre; fim = tv.y + anim;
+                            }
+                        } else if constexpr (HC) {
+                            A0 = pg[0] * y[0];
+                            A1 = pg[1] * y[1] + pg[2] * y[2] + pg[3] * y[3];
+                            A2 = pg[4] * y[4] + pg[5] * y[5] + pg[6] * y[6] + pg[7] * y[7] + pg[8] * y[8];
+                            if (high_l) {
+                                A3 = pg[9] * y[9] + pg[10] * y[10] + pg[11] * y[11] + pg[12] * y[12] +
+                                     pg[13] * y[13] + pg[14] * y[14] + pg[15] * y[15];
+                                A4 = pg[16] * y[16] + pg[17] * y[17] + pg[18] * y[18] + pg[19] * y[19] +
+                                     pg[20] * y[20] + pg[21] * y[21] + pg[22] * y[22] + pg[23] * y[23] +
+                                     pg[24] * y[24];
+                            }
+                            fre = fsre + r0 * A0 + r2 * A2 + r4 * A4;
+                            fim = fsim + r1 * A1 + r3 * A3;
+                        } else {
+                            fre = fsre;
+                            fim = fsim;
+                        }
+                        const R ure = fre * zre - fim * zim;
+                        const R uim = fre * zim + fim * zre;
+                        Ure += ure; Uim += uim;
+                        Xre[0] += h0f * ure; Xim[0] += h0f * uim;
+                        Xre[1] += h1f * ure; Xim[1] += h1f * uim;
+                        Xre[2] += h2f * ure; Xim[2] += h2f * uim;
+                        if constexpr (ANISO) {
 #pragma unroll
-                        for (int q = 0; q < 6; q++) { Are[q] -= m6[q] * ure; Aim[q] -= m6[q] * uim; }
-                    }
-                    if constexpr (MP) {
-                        if (hc_model) {
+                            for (int q = 0; q < 6; q++) { Are[q] -= m6[q] * ure; Aim[q] -= m6[q] * uim; }
+                        }
+                        if constexpr (MP) {
                             const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
                             Ere += zre; Eim += zim;
                             // q_l = Re(g i^l rr_l z): even l rs_l Re(gz), odd l -rs_l Im(gz)
@@ -438,51 +514,63 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
                             Kre += dre * zre - dim * zim;
                             Kim += dre * zim + dim * zre;
                         }
-                    }
-                };
-                if constexpr (NSC > 0) {
+                    };
+                    if constexpr (NSC > 0) {
 #pragma unroll
-                    for (int s = 0; s < NSC; s++) term(s);
-                } else {
+                        for (int s = 0; s < NSC; s++) term(s);
+                    } else {
 #pragma unroll 1
-                    for (int s = 0; s < nS; s++) term(s);
-                }
-                if (!ANISO && has_adp) {
-                    Ure *= Tiso; Uim *= Tiso;
+                        for (int s = 0; s < nS; s++) term(s);
+                    }
+                    if (!ANISO && has_adp) {
+                        Ure *= Tiso; Uim *= Tiso;
 #pragma unroll
-                    for (int j = 0; j < 3; j++) { Xre[j] *= Tiso; Xim[j] *= Tiso; }
-                    if constexpr (MP) { Ere *= Tiso; Eim *= Tiso; Kre *= Tiso; Kim *= Tiso; }
-                }
-                Fre = w * Ure;
-                Fim = w * Uim;
-                const R gU = g.x * Ure - g.y * Uim;  // Re(g U)
-                part[CH_OCC] += gU;
-                if constexpr (ANISO) {
+                        for (int q = 0; q < 3; q++) { Xre[q] *= Tiso; Xim[q] *= Tiso; }
+                        if constexpr (MP) { Ere *= Tiso; Eim *= Tiso; Kre *= Tiso; Kim *= Tiso; }
+                    }
+                    Fv[2 * j] = w * Ure;
+                    Fv[2 * j + 1] = w * Uim;
+                    const R gU = g.x * Ure - g.y * Uim;  // Re(g U)
+                    part[CH_OCC] += gU;
+                    if constexpr (ANISO) {
 #pragma unroll
-                    for (int q = 0; q < 6; q++) part[CH_ADP + q] += g.x * Are[q] - g.y * Aim[q];
-                } else {
-                    part[CH_ADP] -= sH2[hl] * gU;
-                }
+                        for (int q = 0; q < 6; q++) part[CH_ADP + q] += g.x * Are[q] - g.y * Aim[q];
+                    } else {
+                        part[CH_ADP] -= sH2[hl] * gU;
+                    }
 #pragma unroll
-                for (int j = 0; j < 3; j++) part[CH_XYZ + j] -= g.x * Xim[j] + g.y * Xre[j];  // -Im(g X)
-                if constexpr (MP) {
-                    const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
-                    const R gE = g.x * Ere - g.y * Eim;
-                    part[CH_PV] += dr[0] * gE;
-                    part[CH_KAPPA] += dr[1] * gE;
-                    part[CH_KAPPA_P] += g.x * Kre - g.y * Kim;
+                    for (int q = 0; q < 3; q++) part[CH_XYZ + q] -= g.x * Xim[q] + g.y * Xre[q];  // -Im(g X)
+                    if constexpr (MP) {
+                        const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
+                        const R gE = g.x * Ere - g.y * Eim;
+                        part[CH_PV] += dr[0] * gE;
+                        part[CH_KAPPA] += dr[1] * gE;
+                        part[CH_KAPPA_P] += g.x * Kre - g.y * Kim;
+                    }
                 }
             }
-            // block reduction of the partial F of this reflection
+            // butterfly reduce-scatter of the group's 8 values over the warp:
+            // value index 4*bit4 + 2*bit3 + bit2 of the lane ends summed in lanes with bits 1,0 = 0
+            const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+            R v4[4];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                Fre += shfl_xor<R>(Fre, o);
-                Fim += shfl_xor<R>(Fim, o);
+            for (int q = 0; q < 4; q++) {
+                const R keep = b4 ? Fv[q + 4] : Fv[q], send = b4 ? Fv[q] : Fv[q + 4];
+                v4[q] = keep + shfl_xor<R>(send, 16);
             }
-            if (lane == 0) {
-                R2 v;
-                v.x = Fre; v.y = Fim;
-                sF[warp * ht + hl] = v;
+            R v2[2];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const R keep = b3 ? v4[q + 2] : v4[q], send = b3 ? v4[q] : v4[q + 2];
+                v2[q] = keep + shfl_xor<R>(send, 8);
+            }
+            R v1 = (b2 ? v2[1] : v2[0]) + shfl_xor<R>(b2 ? v2[0] : v2[1], 4);
+            v1 += shfl_xor<R>(v1, 2);
+            v1 += shfl_xor<R>(v1, 1);
+            if ((lane & 3) == 0) {
+                const int idx = lane >> 2;  // 0..7 = 4*b4 + 2*b3 + b2
+                R *dst = reinterpret_cast<R *>(&sF[warp * ht + g0 + (idx >> 1)]);
+                dst[idx & 1] = v1;
             }
         }
         // fold the sub-tile sums into the Kahan totals (each thread its own column)
@@ -496,7 +584,7 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
             sCmp[q * kTileAtoms + tid] = comp;
         }
         __syncthreads();
-        for (int i = tid; i < nh; i += blockDim.x) {
+        for (int i = tid; i < ht; i += blockDim.x) {
             R sre = 0, sim = 0;
 #pragma unroll
             for (int wp = 0; wp < kWarps; wp++) {
@@ -515,7 +603,7 @@ sf_grad_kernel2(DevStructure S, CallBuffers C, SfLaunch L)
             return (double)sTot[q * kTileAtoms + tid] - (double)sCmp[q * kTileAtoms + tid];
         };
 #pragma unroll
-        for (int j = 0; j < 3; j++) atomicAdd(G + CH_XYZ + j, total(CH_XYZ + j));
+        for (int q = 0; q < 3; q++) atomicAdd(G + CH_XYZ + q, total(CH_XYZ + q));
         if (ANISO) {
 #pragma unroll
             for (int q = 0; q < 6; q++) atomicAdd(G + CH_ADP + q, total(CH_ADP + q));

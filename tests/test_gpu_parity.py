@@ -203,3 +203,24 @@ def test_invalid_model_is_rejected(engine):
     st.atom_type = np.array([0, 7], dtype=np.int32)
     with pytest.raises(api.DsfError):
         api.HcCalculator(engine, st)
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_reflection_order_is_free(engine, prec):
+    # the engine keeps reflections in lattice-line order internally; any caller order gives the same answers
+    st, d = load_fixture("hc_C2_c")
+    perm = np.random.default_rng(31).permutation(st.n_hkl)
+    st.hkl, st.dtdf = st.hkl[perm], st.dtdf[perm]
+    r = api.HcCalculator(engine, st).calculate(st.dtdf, precision=prec)
+    check(r, d["ref_f"][perm], d["ref_d_xyz"], ref_adp_list(st, d), d["ref_d_occ"], prec)
+    st2, d2 = load_fixture("table_p21c")
+    perm2 = np.random.default_rng(32).permutation(st2.n_hkl)
+    lut = {tuple(k): v for k, v in zip(d2["table_keys"], d2["table_values"])}
+    st2.hkl, st2.dtdf = st2.hkl[perm2], st2.dtdf[perm2]
+    rot, _ = api.all_ops_mod_centering(st2.sg)
+    t = np.zeros((st2.n_hkl, len(rot), st2.n_atoms), dtype=complex)
+    for i, h in enumerate(st2.hkl):
+        for s, r_ in enumerate(rot):
+            t[i, s] = lut[tuple(int(v) for v in h @ r_)]
+    r2 = api.TabulatedCalculator(engine, st2, t).calculate(st2.dtdf, precision=prec)
+    check(r2, d2["ref_f"][perm2], d2["ref_d_xyz"], ref_adp_list(st2, d2), d2["ref_d_occ"], prec)
