@@ -103,6 +103,8 @@ def library():
         L.dsf_structure_device_bytes.argtypes = [C.c_void_p]
         L.dsf_structure_device_bytes.restype = C.c_int64
         L.dsf_calculate.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), _P(C.c_int), _P(_Out)]
+        L.dsf_calculate_atoms.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), _P(C.c_double),
+                                          _P(C.c_double), _P(C.c_double), _P(C.c_int), _P(_Out)]
         L.dsf_calculate_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, _P(_Out), C.c_void_p]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
@@ -246,6 +248,7 @@ class _Calculator:
         self.st = st
         self.h = C.c_void_p()
         self.n_atoms = st.n_atoms
+        self._n_adp = st.n_adp()
         self.n_hkl = 0
         engine._calculators.add(self)
 
@@ -255,25 +258,31 @@ class _Calculator:
         self.engine.check(self.lib.dsf_structure_set_hkl(self.h, len(hkl), p), "set_hkl")
         self.n_hkl = len(hkl)
 
-    def update_atoms(self, xyz, adp, occupancy):
-        adp6 = np.zeros((self.n_atoms, 6))
+    def _atom_arrays(self, xyz, adp, occupancy):
         if isinstance(adp, np.ndarray) and adp.shape == (self.n_atoms, 6):
             adp6 = adp
         else:
+            adp6 = np.zeros((self.n_atoms, 6))
             for i, a in enumerate(adp):
                 adp6[i, :len(a)] = a
-        x1, p1 = _d(np.asarray(xyz).reshape(-1))
-        x2, p2 = _d(adp6.reshape(-1))
-        x3, p3 = _d(occupancy)
+        return _d(np.asarray(xyz).reshape(-1)), _d(adp6.reshape(-1)), _d(occupancy)
+
+    def update_atoms(self, xyz, adp, occupancy):
+        (x1, p1), (x2, p2), (x3, p3) = self._atom_arrays(xyz, adp, occupancy)
         self.engine.check(self.lib.dsf_structure_update_atoms(self.h, p1, p2, p3), "update_atoms")
 
     def calculate(self, dtdf, precision=DSF_FP64, derivatives=("xyz", "adp", "occ"), multipoles=False,
-                  include=None):
-        """F and dT/dparam in the crystal's conventions (host buffers)."""
+                  include=None, atoms=None, adp_layout="list"):
+        """F and dT/dparam in the crystal's conventions (host buffers).
+        atoms = (xyz, adp, occupancy) uploads the atoms' parameters in the same
+        call (dsf_calculate_atoms); None computes with the resident ones.
+        adp_layout "list": d_adp[i] holds the atom's own ADP components (the
+        reference's adp_derivatives); "padded": one [n][6] array, zero past
+        each atom's component count."""
         n, m = self.n_atoms, self.n_hkl
         flags = (DSF_D_XYZ if "xyz" in derivatives else 0) | (DSF_D_ADP if "adp" in derivatives else 0) | \
                 (DSF_D_OCC if "occ" in derivatives else 0) | (DSF_D_MULTIPOLE if multipoles else 0)
-        g = np.ascontiguousarray(np.stack([np.real(dtdf), np.imag(dtdf)], 1).reshape(-1), dtype=np.float64)
+        g = np.ascontiguousarray(dtdf, dtype=np.complex128).view(np.float64)
         f = np.zeros(2 * m)
         dx, da, do = np.zeros(3 * n), np.zeros(6 * n), np.zeros(n)
         dpv, dplm, dk, dkp = np.zeros(n), np.zeros(25 * n), np.zeros(n), np.zeros(n)
@@ -285,12 +294,20 @@ class _Calculator:
         inc = None
         if include is not None:
             incarr, inc = _i(np.asarray(include, dtype=np.int32))
-        self.engine.check(self.lib.dsf_calculate(self.h, int(precision), flags, g.ctypes.data_as(_P(C.c_double)),
-                                                 inc, C.byref(o)), "calculate")
-        nadp = self.st.n_adp()
+        gp = g.ctypes.data_as(_P(C.c_double))
+        if atoms is None:
+            self.engine.check(self.lib.dsf_calculate(self.h, int(precision), flags, gp, inc, C.byref(o)), "calculate")
+        else:
+            (x1, p1), (x2, p2), (x3, p3) = self._atom_arrays(*atoms)
+            self.engine.check(self.lib.dsf_calculate_atoms(self.h, int(precision), flags, p1, p2, p3, gp, inc,
+                                                           C.byref(o)), "calculate")
         da = da.reshape(n, 6)
-        out = dict(f=f[0::2] + 1j * f[1::2], d_xyz=dx.reshape(n, 3), d_adp=[da[i, :nadp[i]] for i in range(n)],
-                   d_occ=do)
+        if adp_layout == "padded":
+            d_adp = da
+        else:
+            nadp = self._n_adp
+            d_adp = [da[i, :nadp[i]] for i in range(n)]
+        out = dict(f=f.view(np.complex128), d_xyz=dx.reshape(n, 3), d_adp=d_adp, d_occ=do)
         if multipoles:
             out.update(d_pval=dpv, d_plm=dplm.reshape(n, 25), d_kappa=dk, d_kappa_p=dkp)
         return out
@@ -304,8 +321,8 @@ class _Calculator:
         if cached is None or cached.shape != hkl.shape or not np.array_equal(cached, hkl):
             self.set_hkl(hkl)
             self._hkl_cache = hkl.copy()
-        self.update_atoms(xyz, adp, occupancy)
-        return self.calculate(dtdf, precision=precision, multipoles=multipoles, include=include)
+        return self.calculate(dtdf, precision=precision, multipoles=multipoles, include=include,
+                              atoms=(xyz, adp, occupancy))
 
     def device_bytes(self):
         return self.lib.dsf_structure_device_bytes(self.h)

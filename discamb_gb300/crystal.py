@@ -219,6 +219,9 @@ SPACE_GROUPS = {
              "x+1/2,y+1/2,z", "-x+1/2,y+1/2,-z+1/2", "-x+1/2,-y+1/2,-z", "x+1/2,-y+1/2,z+1/2"],
     "P43212": ["x,y,z", "-x,-y,z+1/2", "-y+1/2,x+1/2,z+3/4", "y+1/2,-x+1/2,z+1/4",
                "-x+1/2,y+1/2,-z+3/4", "x+1/2,-y+1/2,-z+1/4", "y,x,-z", "-y,-x,-z+1/2"],
+    "P41": ["x,y,z", "-x,-y,z+1/2", "-y,x,z+1/4", "y,-x,z+3/4"],
+    "Pbca": ["x,y,z", "-x+1/2,-y,z+1/2", "-x,y+1/2,-z+1/2", "x+1/2,-y+1/2,-z",
+             "-x,-y,-z", "x+1/2,y,-z+1/2", "x,-y+1/2,z+1/2", "-x+1/2,y+1/2,z"],
     # inversion centre away from the origin (exercises the shifted-centre branch)
     "P-1(shift)": ["x,y,z", "-x+1/2,-y,-z+1/2"],
     "I2/m-like": ["x,y,z", "-x,y,-z", "-x,-y,-z", "x,-y,z",

@@ -16,7 +16,7 @@
 #include "../../include/dsf_gb300.h"
 #include "dsf_device.cuh"
 #include "dsf_math.cuh"
-#include "dsf_sf_kernel.cuh"
+#include "dsf_launch_v3.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -190,6 +190,11 @@ struct dsf_structure {
     int obverse = 1;
     int n_total = 1;
     std::vector<int> sym_rot, sym_t24;
+    // HC: operations ordered in cosets of coset_size (0: no such order) within
+    // which they differ by a sign-diagonal Cartesian map of the reciprocal
+    // vector; sym_sign: that map's signs relative to the coset's first operation
+    int coset_size = 0;
+    std::vector<int> sym_sign;  // [n_sym][3]
     std::vector<int> perm;  // sorted -> original
     std::vector<int> tile_begin, tile_ntypes, tile_types;
     // host model copies
@@ -216,6 +221,8 @@ struct dsf_structure {
     bool have_hkl = false, have_atoms = false;
     int last_launches = 0;
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    void *pinned = nullptr;  // host staging of dsf_calculate / dsf_calculate_atoms
+    size_t pinned_bytes = 0;
     DevStructure dev{};
 };
 
@@ -389,6 +396,74 @@ __global__ void atom_convert_kernel(AtomParams P, const double *raw, const int *
 // host helpers
 // ------------------------------------------------------------------------
 
+// Orders the operations of an HC structure in cosets within which they differ
+// by a sign-diagonal Cartesian map: Q_t Q_u^T = diag(+-1, +-1, +-1) with
+// Q = B R^T B^{-1} (B^{-1} = M^T) the Cartesian action of h -> R^T h.  The
+// harmonics of the operations of one coset are then signed copies of each
+// other (sf_grad_kernel3's class-sum form).  Leaves the order alone unless all
+// cosets have one size >= 2.
+void order_sign_cosets(dsf_structure *s)
+{
+    const int n = s->n_sym;
+    std::vector<double> Q(9 * (size_t)n);
+    for (int op = 0; op < n; op++) {
+        const int *R = &s->sym_rot[9 * op];
+        double BRt[9];
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double v = 0;
+                for (int k = 0; k < 3; k++) v += s->B[3 * i + k] * R[3 * j + k];
+                BRt[3 * i + j] = v;
+            }
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double v = 0;
+                for (int k = 0; k < 3; k++) v += BRt[3 * i + k] * s->M[3 * j + k];
+                Q[9 * op + 3 * i + j] = v;
+            }
+    }
+    // signs of Q_t Q_u^T when it is sign-diagonal
+    auto rel = [&](int t, int u, int *sg) {
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) {
+                double v = 0;
+                for (int k = 0; k < 3; k++) v += Q[9 * t + 3 * i + k] * Q[9 * u + 3 * j + k];
+                const double want = (i == j) ? std::copysign(1.0, v) : 0.0;
+                if (std::fabs(v - want) > 1e-9) return false;
+                if (i == j) sg[i] = v < 0 ? -1 : 1;
+            }
+        return true;
+    };
+    std::vector<int> order, sign(3 * (size_t)n, 1), used(n, 0);
+    int cs = -1;
+    for (int u = 0; u < n; u++) {
+        if (used[u]) continue;
+        int size = 0;
+        for (int t = u; t < n; t++) {
+            int sg[3];
+            if (used[t] || !rel(t, u, sg)) continue;
+            used[t] = 1;
+            for (int i = 0; i < 3; i++) sign[3 * order.size() + i] = sg[i];
+            order.push_back(t);
+            size++;
+        }
+        if (cs < 0) cs = size;
+        if (size != cs) cs = 0;
+    }
+    s->coset_size = 0;
+    s->sym_sign.assign(3 * (size_t)n, 1);
+    if (cs < 2) return;
+    std::vector<int> rot(9 * (size_t)n), t24(3 * (size_t)n);
+    for (int k = 0; k < n; k++) {
+        std::copy(&s->sym_rot[9 * order[k]], &s->sym_rot[9 * order[k]] + 9, &rot[9 * k]);
+        std::copy(&s->sym_t24[3 * order[k]], &s->sym_t24[3 * order[k]] + 3, &t24[3 * k]);
+    }
+    s->sym_rot.swap(rot);
+    s->sym_t24.swap(t24);
+    s->sym_sign = sign;
+    s->coset_size = cs;
+}
+
 int sym_from_desc(dsf_engine *e, dsf_structure *s, const dsf_symmetry *sym)
 {
     if (!sym || sym->n_symops < 1 || sym->n_symops > kMaxSym)
@@ -407,6 +482,7 @@ int sym_from_desc(dsf_engine *e, dsf_structure *s, const dsf_symmetry *sym)
         if (v < 0) v += 24;
         s->sym_t24[i] = v;
     }
+    if (s->model == MODEL_HC) order_sign_cosets(s);
     s->centro_mode = 0;
     if (sym->centrosymmetric) {
         bool origin = true;
@@ -1108,8 +1184,8 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
         if ((rc = upload(e, s->d_tile_lmax, tl.data(), tl.size()))) return bail(rc);
     }
     // rows in the engine's line order (the order dsf_structure_set_hkl gives the reflections), padded with
-    // zero rows to a multiple of 16 reflections: the kernel reads whole sub-tiles
-    const int n_pad = (n_hkl + 15) / 16 * 16;
+    // zero rows to a multiple of kMaxHT reflections: the kernel reads whole sub-tiles
+    const int n_pad = (n_hkl + kMaxHT - 1) / kMaxHT * kMaxHT;
     std::vector<int> order(n_hkl);
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
@@ -1155,6 +1231,7 @@ int dsf_structure_destroy(dsf_structure *s)
     for (DevBuf *b : bufs) b->release();
     if (s->ev_begin) cudaEventDestroy(s->ev_begin);
     if (s->ev_end) cudaEventDestroy(s->ev_end);
+    if (s->pinned) cudaFreeHost(s->pinned);
     s->eng->live_structures--;
     delete s;
     return DSF_OK;
@@ -1168,7 +1245,8 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
     if (s->model == MODEL_TABLE && s->have_hkl && n_hkl != s->n_hkl)
         return fail(e, DSF_ERR_ARGUMENT, "tabulated structures keep the reflection set of their table");
     cudaSetDevice(e->device);
-    const int n_pad = (n_hkl + 15) / 16 * 16;  // tables and per-reflection arrays padded with zero rows
+    // tables and per-reflection arrays padded with zero rows to whole sub-tiles (ht divides kMaxHT)
+    const int n_pad = (n_hkl + kMaxHT - 1) / kMaxHT * kMaxHT;
     // line order: sorted by (h, k, l) so runs of l + 1 share a lattice line
     s->hperm.resize(n_hkl);
     std::iota(s->hperm.begin(), s->hperm.end(), 0);
@@ -1385,6 +1463,19 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     L.error = s->d_err.as<int>();
     L.cont = s->d_cont.as<int>();
     L.tile_lmax = s->d_tile_lmax.as<int>();
+    // class-sum kernels: HC without the multipole adjoint, operations in sign-diagonal cosets
+    L.coset = 0;
+    if (s->model == MODEL_HC && !mp && s->coset_size && coset_form_compiled(fp64, s->n_sym, s->coset_size)) {
+        L.coset = s->coset_size;
+        for (int op = 0; op < s->n_sym; op++)
+            for (int c = 0; c < 8; c++) {
+                int sg = 1;
+                for (int i = 0; i < 3; i++)
+                    if ((c >> i) & 1) sg *= s->sym_sign[3 * op + i];
+                L.sgn_f[op][c] = (float)sg;
+                L.sgn_d[op][c] = (double)sg;
+            }
+    }
     if (!s->ev_begin) {
         DSF_CUDA(cudaEventCreate(&s->ev_begin));
         DSF_CUDA(cudaEventCreate(&s->ev_end));
@@ -1442,13 +1533,16 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     return DSF_OK;
 }
 
-int dsf_calculate(dsf_structure *s, int precision, int flags, const double *dtdf, const int *include,
-                  const dsf_outputs *out)
+// host-buffer call: optional atom upload, dT/dF upload, the device calculation,
+// read-back; staged through one pinned buffer per structure, one stream sync
+static int calculate_host(dsf_structure *s, int precision, int flags, const double *xyz, const double *adp,
+                          const double *occ, const double *dtdf, const int *include, const dsf_outputs *out)
 {
     if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
     if (!out || !out->f || !dtdf) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
     if (!s->have_hkl) return fail(e, DSF_ERR_STATE, "no reflections set");
+    if ((xyz != nullptr) != (occ != nullptr)) return fail(e, DSF_ERR_ARGUMENT, "xyz and occupancy go together");
     cudaSetDevice(e->device);
     const int n_hkl = s->n_hkl, n = s->n_atoms;
     // inclusion mask (countAtomContribution)
@@ -1461,7 +1555,44 @@ int dsf_calculate(dsf_structure *s, int precision, int flags, const double *dtdf
         DSF_CUDA(cudaMemcpyAsync(s->d_active.p, s->active_host.data(), n, cudaMemcpyHostToDevice, e->stream));
     // device output block: f, xyz, adp, occ, pval, plm, kappa, kappa'
     const size_t nf = 2 * (size_t)n_hkl, per_atom = 3 + 6 + 1 + 1 + 25 + 1 + 1;
-    DSF_CUDA(s->d_out.alloc(sizeof(double) * (nf + per_atom * (size_t)n)));
+    const size_t nout = nf + per_atom * (size_t)n;
+    DSF_CUDA(s->d_out.alloc(sizeof(double) * nout));
+    // pinned staging: [raw atoms 10 n][dtdf 2 n_hkl][outputs nout][status]
+    const size_t nin = 10 * (size_t)n + 2 * (size_t)n_hkl;
+    const size_t stage_bytes = sizeof(double) * (nin + nout) + 16;
+    if (s->pinned_bytes < stage_bytes) {
+        if (s->pinned) cudaFreeHost(s->pinned);
+        s->pinned = nullptr;
+        s->pinned_bytes = 0;
+        DSF_CUDA(cudaHostAlloc(&s->pinned, stage_bytes, cudaHostAllocDefault));
+        s->pinned_bytes = stage_bytes;
+    }
+    double *raw = (double *)s->pinned, *pg = raw + 10 * (size_t)n, *po = pg + 2 * (size_t)n_hkl;
+    int *pk = (int *)(po + nout);
+    if (xyz) {
+        for (int i = 0; i < n; i++) {
+            for (int j = 0; j < 3; j++) {
+                if (!std::isfinite(xyz[3 * i + j])) return fail(e, DSF_ERR_ARGUMENT, "non-finite coordinate");
+                raw[10 * i + j] = xyz[3 * i + j];
+            }
+            for (int j = 0; j < 6; j++) raw[10 * i + 3 + j] = (adp && j < s->adpk[i]) ? adp[6 * i + j] : 0.0;
+            raw[10 * i + 9] = occ[i];
+        }
+        DSF_CUDA(cudaMemcpyAsync(s->d_raw.p, raw, sizeof(double) * 10 * (size_t)n, cudaMemcpyHostToDevice, e->stream));
+        AtomParams P;
+        P.n_atoms = n;
+        P.xyz_conv = s->xyz_conv;
+        std::copy(s->Minv, s->Minv + 9, P.Minv);
+        std::copy(s->A6, s->A6 + 36, P.A6);
+        atom_convert_kernel<<<(n + 127) / 128, 128, 0, e->stream>>>(
+            P, s->d_raw.as<double>(), s->d_perm.as<int>(), s->d_atom_adpk.as<int>(), s->d_multw.as<double>(),
+            s->d_xq.as<uint32_t>(), s->d_xlo.as<float>(), s->d_xd.as<double>(), s->d_adp_f.as<float>(),
+            s->d_adp_d.as<double>(), s->d_w_f.as<float>(), s->d_w_d.as<double>());
+        DSF_CUDA(cudaGetLastError());
+        s->have_atoms = true;
+    }
+    std::memcpy(pg, dtdf, sizeof(double) * 2 * (size_t)n_hkl);
+    DSF_CUDA(cudaMemcpyAsync(s->d_dtdf.p, pg, 16 * (size_t)n_hkl, cudaMemcpyHostToDevice, e->stream));
     double *base = s->d_out.as<double>();
     dsf_outputs d;
     d.f = base;
@@ -1472,24 +1603,40 @@ int dsf_calculate(dsf_structure *s, int precision, int flags, const double *dtdf
     d.d_plm = d.d_pval + n;
     d.d_kappa = d.d_plm + 25 * (size_t)n;
     d.d_kappa_prime = d.d_kappa + n;
-    DSF_CUDA(cudaMemcpyAsync(s->d_dtdf.p, dtdf, 16 * (size_t)n_hkl, cudaMemcpyHostToDevice, e->stream));
     int rc = dsf_calculate_device(s, precision, flags, s->d_dtdf.as<double>(), &d, e->stream);
     if (rc) return rc;
-    DSF_CUDA(cudaMemcpyAsync(out->f, d.f, 8 * nf, cudaMemcpyDeviceToHost, e->stream));
-    struct { double *dst; double *src; size_t n; } cp[] = {
-        {out->d_xyz, d.d_xyz, 3 * (size_t)n}, {out->d_adp, d.d_adp, 6 * (size_t)n}, {out->d_occ, d.d_occ, (size_t)n},
-        {out->d_pval, d.d_pval, (size_t)n}, {out->d_plm, d.d_plm, 25 * (size_t)n}, {out->d_kappa, d.d_kappa, (size_t)n},
-        {out->d_kappa_prime, d.d_kappa_prime, (size_t)n}};
-    for (auto &c : cp)
-        if (c.dst) DSF_CUDA(cudaMemcpyAsync(c.dst, c.src, 8 * c.n, cudaMemcpyDeviceToHost, e->stream));
-    int kerr = 0;
-    DSF_CUDA(cudaMemcpyAsync(&kerr, s->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    const bool mp = (flags & DSF_D_MULTIPOLE) != 0;
+    const size_t nback = mp ? nout : nf + 10 * (size_t)n;  // f, xyz, adp, occ (+ multipole block)
+    DSF_CUDA(cudaMemcpyAsync(po, base, sizeof(double) * nback, cudaMemcpyDeviceToHost, e->stream));
+    DSF_CUDA(cudaMemcpyAsync(pk, s->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
     DSF_CUDA(cudaStreamSynchronize(e->stream));
-    if (kerr) {
+    if (*pk) {
         cudaMemsetAsync(s->d_err.p, 0, sizeof(int), e->stream);
         return fail(e, DSF_ERR_TIMEOUT, "a shared-memory pipeline wait of the kernel ran out");
     }
+    std::memcpy(out->f, po, sizeof(double) * nf);
+    const double *q = po + nf;
+    struct { double *dst; size_t off, n; } cp[] = {
+        {out->d_xyz, 0, 3 * (size_t)n}, {out->d_adp, 3 * (size_t)n, 6 * (size_t)n},
+        {out->d_occ, 9 * (size_t)n, (size_t)n}, {out->d_pval, 10 * (size_t)n, (size_t)n},
+        {out->d_plm, 11 * (size_t)n, 25 * (size_t)n}, {out->d_kappa, 36 * (size_t)n, (size_t)n},
+        {out->d_kappa_prime, 37 * (size_t)n, (size_t)n}};
+    for (auto &c : cp)
+        if (c.dst && (c.off < 10 * (size_t)n || mp)) std::memcpy(c.dst, q + c.off, sizeof(double) * c.n);
     return DSF_OK;
+}
+
+int dsf_calculate(dsf_structure *s, int precision, int flags, const double *dtdf, const int *include,
+                  const dsf_outputs *out)
+{
+    return calculate_host(s, precision, flags, nullptr, nullptr, nullptr, dtdf, include, out);
+}
+
+int dsf_calculate_atoms(dsf_structure *s, int precision, int flags, const double *xyz, const double *adp,
+                        const double *occupancy, const double *dtdf, const int *include, const dsf_outputs *out)
+{
+    if (s && (!xyz || !occupancy)) return fail(s->eng, DSF_ERR_ARGUMENT, "xyz and occupancy are required");
+    return calculate_host(s, precision, flags, xyz, adp, occupancy, dtdf, include, out);
 }
 
 }  // extern "C"

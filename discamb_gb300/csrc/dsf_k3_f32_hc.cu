@@ -8,6 +8,9 @@ cudaError_t launch_k3_f32_hc(const DevStructure &S, const CallBuffers &C, const 
 {
     if (mp) return aniso ? dispatch_k3<float, MODEL_HC, true, true, 2, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st)
                          : dispatch_k3<float, MODEL_HC, true, false, 2, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st);
+    if (L.coset)
+        return aniso ? dispatch_coset<float, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st)
+                     : dispatch_coset<float, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st);
     return aniso ? dispatch_k3<float, MODEL_HC, false, true, 2, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st)
                  : dispatch_k3<float, MODEL_HC, false, false, 2, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st);
 }

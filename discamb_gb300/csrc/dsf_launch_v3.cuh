@@ -7,11 +7,11 @@
 
 namespace dsf {
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
 cudaError_t launch_k3(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, int n_tiles, int n_chunks,
                       size_t smem, cudaStream_t st)
 {
-    auto k = sf_grad_kernel3<R, MODEL, MP, ANISO, NSC>;
+    auto k = sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k<<<dim3(n_tiles, n_chunks), kTileAtoms, smem, st>>>(S, C, L);
@@ -32,6 +32,31 @@ cudaError_t dispatch_k3(const DevStructure &S, const CallBuffers &C, const SfLau
 {
     if (S.n_sym == N0) return launch_k3<R, MODEL, MP, ANISO, N0>(S, C, L, n_tiles, n_chunks, smem, st);
     return dispatch_k3<R, MODEL, MP, ANISO, NS...>(S, C, L, n_tiles, n_chunks, smem, st);
+}
+
+// HC without the multipole adjoint, operations in sign-diagonal cosets: the
+// class-sum kernels of the compiled (operation count, coset size) pairs; the
+// engine sets L.coset only for those pairs (coset_form_compiled)
+template <typename R, bool ANISO>
+cudaError_t dispatch_coset(const DevStructure &, const CallBuffers &, const SfLaunch &, int, int, size_t, cudaStream_t)
+{
+    return cudaErrorInvalidValue;
+}
+
+template <typename R, bool ANISO, int N0, int CS0, int... NC>
+cudaError_t dispatch_coset(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, int n_tiles, int n_chunks,
+                           size_t smem, cudaStream_t st)
+{
+    if (S.n_sym == N0 && L.coset == CS0)
+        return launch_k3<R, MODEL_HC, false, ANISO, N0, CS0>(S, C, L, n_tiles, n_chunks, smem, st);
+    return dispatch_coset<R, ANISO, NC...>(S, C, L, n_tiles, n_chunks, smem, st);
+}
+
+// (operation count, coset size) pairs with compiled class-sum kernels
+__host__ inline bool coset_form_compiled(bool fp64, int n_sym, int cs)
+{
+    if (fp64) return (n_sym == 4 && cs == 4) || (n_sym == 8 && cs == 4);
+    return (n_sym == 2 && cs == 2) || (n_sym == 4 && (cs == 4 || cs == 2)) || (n_sym == 8 && (cs == 8 || cs == 4));
 }
 
 cudaError_t launch_k3_f32_hc(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool mp, bool aniso,

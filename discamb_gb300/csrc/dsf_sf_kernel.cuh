@@ -156,17 +156,33 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 // ---------------------------------------------------------------------------
 struct SfLaunch {
     int hkl_chunk;         // reflections per block (multiple of ht)
-    int ht;                // reflections per shared-memory sub-tile (multiple of 4, divides 16)
+    int ht;                // reflections per shared-memory sub-tile (multiple of 4, divides kMaxHT)
     int tile_offset;       // first tile of this launch
     int max_types;         // largest number of types in a tile of this launch
-    int n_hkl_pad;         // padded reflection count of the tables (multiple of 16)
+    int n_hkl_pad;         // padded reflection count of the tables (multiple of kMaxHT)
     const void *rs;        // RsRec<R> [n_hkl_pad][n_sym]
     const void *tr;        // R [n_types][n_hkl_pad][8]
     const void *trm;       // R [n_types][n_hkl_pad][8] (multipole adjoint)
     const int *cont;       // [n_hkl_pad] 1: reflection = previous one + (0,0,1) (reflections in line order)
     const int *tile_lmax;  // [n_tiles] highest l of the angular sums of the tile's atoms
     int *error;            // set to 1 on a timed-out wait
+    // operations in cosets of CS: within a coset the operations differ by a
+    // sign-diagonal Cartesian map diag(+-1, +-1, +-1) of the reciprocal vector;
+    // sgn[s][c] is the sign operation s gives the harmonics of parity class
+    // c = px + 2 py + 4 pz (parities of the harmonic in x, y, z), relative to
+    // the first operation of its coset
+    int coset;             // size of the sign-diagonal cosets the operations are ordered in (0: none)
+    float sgn_f[8][8];
+    double sgn_d[8][8];
 };
+
+// parity class (px + 2 py + 4 pz) of the 25 harmonics of harmonic_polys
+// (0: 1; 1-3: y z x; 4-8: xy yz (2zz-xx-yy) xz (xx-yy); 9-15: l = 3; 16-24: l = 4)
+__host__ __device__ constexpr int harmonic_class(int q)
+{
+    constexpr int cls[25] = {0, 2, 4, 1, 3, 6, 0, 5, 0, 2, 7, 2, 4, 1, 4, 1, 3, 6, 3, 6, 0, 5, 0, 5, 0};
+    return cls[q];
+}
 
 template <typename R>
 struct StageLayout {
@@ -233,10 +249,18 @@ struct PhaseOps<double> {
 // build up.
 constexpr int kAnchorF32 = 4;
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
 __global__ void __launch_bounds__(kTileAtoms)
 sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
 {
+    // CS > 0 (HC, fixed operation count, operations in sign-diagonal cosets of
+    // CS): the angular sums are formed once per (atom, reflection, coset) by
+    // parity class from the harmonics of the coset's first operation, and each
+    // operation combines the eight class sums with its signs -- the same sums
+    // as the per-operation form
+    constexpr bool DIAG = CS > 0;
+    static_assert(!DIAG || (MODEL == MODEL_HC && NSC > 0 && NSC <= 8 && NSC % CS == 0 && !MP),
+                  "coset form: HC, compiled count <= 8");
     using R2 = typename Vec2<R>::T;
     constexpr bool F32 = sizeof(R) == 4;
     constexpr int NT = n_channels<R, MP>();
@@ -428,6 +452,30 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                     for (int q = 0; q < (ANISO ? 6 : 1); q++) { Are[q] = R(0); Aim[q] = R(0); }
                     R Ere = 0, Eim = 0, Kre = 0, Kim = 0;
                     const RsRec<R> *recs = sRs + (size_t)hl * nS;
+                    // coset form: radial-weighted class sums, even l (real part) and odd l (imaginary part)
+                    R Ec[4] = {0, 0, 0, 0}, Oc[4] = {0, 0, 0, 0};  // classes 0 3 6 5 | 2 4 1 7
+                    auto class_sums = [&](const R *y) {
+                        if constexpr (DIAG) {
+                        Oc[3] = R(0);
+                        Ec[0] = fsre + r0 * (pg[0] * y[0]) + r2 * (pg[6] * y[6] + pg[8] * y[8]);
+                        Ec[1] = r2 * (pg[4] * y[4]);
+                        Ec[2] = r2 * (pg[5] * y[5]);
+                        Ec[3] = r2 * (pg[7] * y[7]);
+                        Oc[0] = r1 * (pg[1] * y[1]);
+                        Oc[1] = r1 * (pg[2] * y[2]);
+                        Oc[2] = r1 * (pg[3] * y[3]);
+                        if (high_l) {
+                            Ec[0] += r4 * (pg[20] * y[20] + pg[22] * y[22] + pg[24] * y[24]);
+                            Ec[1] += r4 * (pg[16] * y[16] + pg[18] * y[18]);
+                            Ec[2] += r4 * (pg[17] * y[17] + pg[19] * y[19]);
+                            Ec[3] += r4 * (pg[21] * y[21] + pg[23] * y[23]);
+                            Oc[0] += r3 * (pg[9] * y[9] + pg[11] * y[11]);
+                            Oc[1] += r3 * (pg[12] * y[12] + pg[14] * y[14]);
+                            Oc[2] += r3 * (pg[13] * y[13] + pg[15] * y[15]);
+                            Oc[3] = r3 * (pg[10] * y[10]);
+                        }
+                        }
+                    };
                     auto term = [&](int s) {
                         const RsRec<R> &rec = recs[s];
                         const R h0f = rec.hf[0], h1f = rec.hf[1], h2f = rec.hf[2];
@@ -466,6 +514,17 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                             } else {
                                 const double2 tv = S.table_d[ti];
                                 fre = tv.x + anre; fim = tv.y + anim;
+                            }
+                        } else if constexpr (DIAG) {
+                            // fsph rides in the class-0 sums (sign +1 for every operation)
+                            if constexpr (F32) {
+                                fre = Ec[0] + L.sgn_f[s][3] * Ec[1] + L.sgn_f[s][6] * Ec[2] + L.sgn_f[s][5] * Ec[3];
+                                fim = fsim + L.sgn_f[s][2] * Oc[0] + L.sgn_f[s][4] * Oc[1] + L.sgn_f[s][1] * Oc[2] +
+                                      L.sgn_f[s][7] * Oc[3];
+                            } else {
+                                fre = Ec[0] + L.sgn_d[s][3] * Ec[1] + L.sgn_d[s][6] * Ec[2] + L.sgn_d[s][5] * Ec[3];
+                                fim = fsim + L.sgn_d[s][2] * Oc[0] + L.sgn_d[s][4] * Oc[1] + L.sgn_d[s][1] * Oc[2] +
+                                      L.sgn_d[s][7] * Oc[3];
                             }
                         } else if constexpr (HC) {
                             A0 = pg[0] * y[0];
@@ -517,7 +576,12 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                     };
                     if constexpr (NSC > 0) {
 #pragma unroll
-                        for (int s = 0; s < NSC; s++) term(s);
+                        for (int s = 0; s < NSC; s++) {
+                            if constexpr (DIAG) {
+                                if (s % CS == 0) class_sums(recs[s].y);
+                            }
+                            term(s);
+                        }
                     } else {
 #pragma unroll 1
                         for (int s = 0; s < nS; s++) term(s);

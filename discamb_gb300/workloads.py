@@ -230,7 +230,7 @@ def small_case(sg_symbol="P21/c", n_atoms=6, stol_max=0.5, seed=7, cell_kind=Non
                      "P21": "monoclinic", "P21/c": "monoclinic", "C2/c": "monoclinic",
                      "I2/m-like": "monoclinic"}.get(sg_symbol, "orthorhombic")
     cell = random_cell(rng, cell_kind)
-    if sg_symbol == "P43212":
+    if sg_symbol in ("P43212", "P41"):
         a = cell[0]
         cell = (a, a, cell[2], 90.0, 90.0, 90.0)
     base = ["C", "H", "N", "O", "S"]

@@ -177,6 +177,11 @@ int64_t dsf_structure_device_bytes(const dsf_structure *s);
 /* host buffers: dtdf [n_hkl][2]; include [n_atoms] (NULL = all); outputs on host */
 int dsf_calculate(dsf_structure *s, int precision, int derivative_flags, const double *dtdf,
                   const int *include, const dsf_outputs *out);
+/* the reference call shape: the atoms' current parameters (xyz [n][3], adp [n][6], occupancy [n], crystal's
+ * conventions) with dT/dF, uploaded and computed in one call (calculateStructureFactorsAndDerivatives(atoms, hkl,
+ * f, dTarget_dparam, dTarget_df, countAtomContribution), include/discamb/Scattering/SfCalculator.h:45-67) */
+int dsf_calculate_atoms(dsf_structure *s, int precision, int derivative_flags, const double *xyz, const double *adp,
+                        const double *occupancy, const double *dtdf, const int *include, const dsf_outputs *out);
 /* device buffers, asynchronous on `stream` (cudaStream_t, NULL = engine stream) */
 int dsf_calculate_device(dsf_structure *s, int precision, int derivative_flags, const double *dtdf_device,
                          const dsf_outputs *out_device, void *stream);

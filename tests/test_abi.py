@@ -30,8 +30,8 @@ def lib_path():
 
 def test_header_declares_the_boundary():
     names = declared_functions()
-    for required in ("dsf_engine_create", "dsf_structure_create_hc", "dsf_calculate", "dsf_calculate_device",
-                     "dsf_last_error"):
+    for required in ("dsf_engine_create", "dsf_structure_create_hc", "dsf_calculate", "dsf_calculate_atoms",
+                     "dsf_calculate_device", "dsf_last_error"):
         assert required in names
 
 
@@ -52,3 +52,4 @@ def test_invalid_handles_are_rejected_without_a_device(lib_path):
     assert lib.dsf_engine_create(0, None) != 0
     assert lib.dsf_structure_destroy(None) != 0
     assert lib.dsf_calculate(None, 0, 0, None, None, None) != 0
+    assert lib.dsf_calculate_atoms(None, 0, 0, None, None, None, None, None, None) != 0

@@ -121,6 +121,26 @@ def test_config2_subset_full_derivatives(engine, prec):
         assert rel_norm(r[k], o[k]) < tol, (k, rel_norm(r[k], o[k]))
 
 
+# operation orders of every class-sum kernel shape (operation count, sign-diagonal
+# coset size): P21 (2,2), P212121 (4,4), P41 (4,2), P43212 (8,4), Pbca all
+# operations (8,8); P1 and P-1(shift) keep the per-operation form
+@pytest.mark.parametrize("prec", [FP64, FP32])
+@pytest.mark.parametrize("sg,rep", [("P21", "engine"), ("P212121", "engine"), ("P41", "engine"),
+                                    ("P43212", "engine"), ("Pbca", "engine"), ("Pbca", "all"),
+                                    ("P1", "engine"), ("P-1(shift)", "all")])
+def test_sign_coset_forms_match_oracle(engine, sg, rep, prec):
+    for aniso in (False, True):
+        st = W.small_case(sg, n_atoms=9, stol_max=0.55, seed=41, aniso=aniso)
+        if rep == "all":  # no inversion shortcut: equal F only without anomalous dispersion
+            for w in st.wfns:
+                w.anomalous = 0j
+        o = O.compute(st)
+        calc = api.HcCalculator(engine, st, representation=rep)
+        r = calc.calculate(st.dtdf, precision=prec)
+        check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
+        calc.close()
+
+
 def test_fp32_against_fp64_full_config1(engine):
     st = W.config1()
     calc = api.HcCalculator(engine, st)
@@ -181,6 +201,25 @@ def test_all_atoms_excluded_gives_zero(engine):
     # and back on: the mask is per call
     r2 = calc.calculate(st.dtdf, precision=FP64)
     assert np.sum(np.abs(r2["f"])) > 0
+
+
+def test_single_call_matches_update_then_calculate(engine):
+    st = W.small_case("P212121", n_atoms=6, stol_max=0.5, seed=31)
+    calc = api.HcCalculator(engine, st)
+    xyz2 = st.xyz + 0.01
+    occ2 = 0.5 * st.occupancy
+    for prec in (FP64, api.DSF_FP32_BULK):
+        calc.update_atoms(xyz2, st.adp, occ2)
+        a = calc.calculate(st.dtdf, precision=prec)
+        calc.update_atoms(st.xyz, st.adp, st.occupancy)
+        b = calc.calculate(st.dtdf, precision=prec, atoms=(xyz2, st.adp, occ2))
+        assert np.array_equal(a["f"], b["f"]) and np.array_equal(a["d_xyz"], b["d_xyz"])
+        assert np.array_equal(a["d_occ"], b["d_occ"])
+        # the uploaded parameters stay resident for the next plain call
+        c = calc.calculate(st.dtdf, precision=prec, adp_layout="padded")
+        assert np.array_equal(a["f"], c["f"])
+        for i, v in enumerate(a["d_adp"]):
+            assert np.array_equal(c["d_adp"][i, :len(v)], v) and not np.any(c["d_adp"][i, len(v):])
 
 
 def test_reflection_set_change_and_repeat(engine):
