@@ -1463,9 +1463,9 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     L.error = s->d_err.as<int>();
     L.cont = s->d_cont.as<int>();
     L.tile_lmax = s->d_tile_lmax.as<int>();
-    // class-sum kernels: HC without the multipole adjoint, operations in sign-diagonal cosets
+    // class-sum kernels: HC, operations in sign-diagonal cosets
     L.coset = 0;
-    if (s->model == MODEL_HC && !mp && s->coset_size && coset_form_compiled(fp64, s->n_sym, s->coset_size)) {
+    if (s->model == MODEL_HC && s->coset_size && coset_form_compiled(fp64, s->n_sym, s->coset_size)) {
         L.coset = s->coset_size;
         for (int op = 0; op < s->n_sym; op++)
             for (int c = 0; c < 8; c++) {

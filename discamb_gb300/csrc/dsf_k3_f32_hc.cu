@@ -1,4 +1,5 @@
-// FP32-bulk Hansen-Coppens instantiations of sf_grad_kernel3 and the launch entry.
+// FP32-bulk Hansen-Coppens instantiations of sf_grad_kernel3 without the
+// multipole adjoint, and the launch entry.
 #include "dsf_launch_v3.cuh"
 
 namespace dsf {
@@ -6,11 +7,10 @@ namespace dsf {
 cudaError_t launch_k3_f32_hc(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool mp, bool aniso,
                              int n_tiles, int n_chunks, size_t smem, cudaStream_t st)
 {
-    if (mp) return aniso ? dispatch_k3<float, MODEL_HC, true, true, 2, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st)
-                         : dispatch_k3<float, MODEL_HC, true, false, 2, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st);
+    if (mp) return launch_k3_f32_hc_mp(S, C, L, aniso, n_tiles, n_chunks, smem, st);
     if (L.coset)
-        return aniso ? dispatch_coset<float, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st)
-                     : dispatch_coset<float, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st);
+        return aniso ? dispatch_coset<float, false, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st)
+                     : dispatch_coset<float, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st);
     return aniso ? dispatch_k3<float, MODEL_HC, false, true, 2, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st)
                  : dispatch_k3<float, MODEL_HC, false, false, 2, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st);
 }

@@ -7,11 +7,14 @@ cudaError_t launch_k3_f64(const DevStructure &S, const CallBuffers &C, const SfL
                           int n_tiles, int n_chunks, size_t smem, cudaStream_t st)
 {
     if (S.model == MODEL_HC) {
+        if (mp && L.coset)
+            return aniso ? dispatch_coset<double, true, true, 4, 4, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st)
+                         : dispatch_coset<double, true, false, 4, 4, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st);
         if (mp) return aniso ? dispatch_k3<double, MODEL_HC, true, true, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st)
                              : dispatch_k3<double, MODEL_HC, true, false, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st);
         if (L.coset)
-            return aniso ? dispatch_coset<double, true, 4, 4, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st)
-                         : dispatch_coset<double, false, 4, 4, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st);
+            return aniso ? dispatch_coset<double, false, true, 4, 4, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st)
+                         : dispatch_coset<double, false, false, 4, 4, 8, 4>(S, C, L, n_tiles, n_chunks, smem, st);
         return aniso ? dispatch_k3<double, MODEL_HC, false, true, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st)
                      : dispatch_k3<double, MODEL_HC, false, false, 4, 8>(S, C, L, n_tiles, n_chunks, smem, st);
     }

@@ -34,22 +34,22 @@ cudaError_t dispatch_k3(const DevStructure &S, const CallBuffers &C, const SfLau
     return dispatch_k3<R, MODEL, MP, ANISO, NS...>(S, C, L, n_tiles, n_chunks, smem, st);
 }
 
-// HC without the multipole adjoint, operations in sign-diagonal cosets: the
-// class-sum kernels of the compiled (operation count, coset size) pairs; the
-// engine sets L.coset only for those pairs (coset_form_compiled)
-template <typename R, bool ANISO>
+// HC, operations in sign-diagonal cosets: the class-sum kernels of the
+// compiled (operation count, coset size) pairs; the engine sets L.coset only
+// for those pairs (coset_form_compiled)
+template <typename R, bool MP, bool ANISO>
 cudaError_t dispatch_coset(const DevStructure &, const CallBuffers &, const SfLaunch &, int, int, size_t, cudaStream_t)
 {
     return cudaErrorInvalidValue;
 }
 
-template <typename R, bool ANISO, int N0, int CS0, int... NC>
+template <typename R, bool MP, bool ANISO, int N0, int CS0, int... NC>
 cudaError_t dispatch_coset(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, int n_tiles, int n_chunks,
                            size_t smem, cudaStream_t st)
 {
     if (S.n_sym == N0 && L.coset == CS0)
-        return launch_k3<R, MODEL_HC, false, ANISO, N0, CS0>(S, C, L, n_tiles, n_chunks, smem, st);
-    return dispatch_coset<R, ANISO, NC...>(S, C, L, n_tiles, n_chunks, smem, st);
+        return launch_k3<R, MODEL_HC, MP, ANISO, N0, CS0>(S, C, L, n_tiles, n_chunks, smem, st);
+    return dispatch_coset<R, MP, ANISO, NC...>(S, C, L, n_tiles, n_chunks, smem, st);
 }
 
 // (operation count, coset size) pairs with compiled class-sum kernels
@@ -61,6 +61,8 @@ __host__ inline bool coset_form_compiled(bool fp64, int n_sym, int cs)
 
 cudaError_t launch_k3_f32_hc(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool mp, bool aniso,
                              int n_tiles, int n_chunks, size_t smem, cudaStream_t st);
+cudaError_t launch_k3_f32_hc_mp(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool aniso,
+                                int n_tiles, int n_chunks, size_t smem, cudaStream_t st);
 cudaError_t launch_k3_f32_other(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool aniso,
                                 int n_tiles, int n_chunks, size_t smem, cudaStream_t st);
 cudaError_t launch_k3_f64(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool mp, bool aniso,

@@ -184,6 +184,20 @@ __host__ __device__ constexpr int harmonic_class(int q)
     return cls[q];
 }
 
+// the 16 (l, parity class) slots of the multipole adjoint's class sums: the
+// slot of harmonic q, and the parity class and l of slot k
+__host__ __device__ constexpr int harmonic_slot(int q)
+{
+    constexpr int sl[25] = {0, 1, 2, 3, 4, 5, 6, 7, 6, 8, 9, 8, 10, 11, 10, 11, 12, 13, 12, 13, 14, 15, 14, 15, 14};
+    return sl[q];
+}
+__host__ __device__ constexpr int slot_class(int k)
+{
+    constexpr int c[16] = {0, 2, 4, 1, 3, 6, 0, 5, 2, 7, 4, 1, 3, 6, 0, 5};
+    return c[k];
+}
+__host__ __device__ constexpr int slot_l(int k) { return k == 0 ? 0 : (k < 4 ? 1 : k / 4 + 1); }
+
 template <typename R>
 struct StageLayout {
     size_t rs, tr, trm, gw, h2, cont, bytes;
@@ -259,7 +273,7 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
     // operation combines the eight class sums with its signs -- the same sums
     // as the per-operation form
     constexpr bool DIAG = CS > 0;
-    static_assert(!DIAG || (MODEL == MODEL_HC && NSC > 0 && NSC <= 8 && NSC % CS == 0 && !MP),
+    static_assert(!DIAG || (MODEL == MODEL_HC && NSC > 0 && NSC <= 8 && NSC % CS == 0),
                   "coset form: HC, compiled count <= 8");
     using R2 = typename Vec2<R>::T;
     constexpr bool F32 = sizeof(R) == 4;
@@ -454,8 +468,34 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                     const RsRec<R> *recs = sRs + (size_t)hl * nS;
                     // coset form: radial-weighted class sums, even l (real part) and odd l (imaginary part)
                     R Ec[4] = {0, 0, 0, 0}, Oc[4] = {0, 0, 0, 0};  // classes 0 3 6 5 | 2 4 1 7
+                    // with the multipole adjoint: unweighted slot sums (l, class) and the
+                    // operations' signed adjoint weights per slot, folded into the P_lm
+                    // channels once per coset
+                    R Acl[DIAG && MP ? 16 : 1], QC[DIAG && MP ? 16 : 1];
+#pragma unroll
+                    for (int k = 0; k < (DIAG && MP ? 16 : 1); k++) { Acl[k] = R(0); QC[k] = R(0); }
+                    auto slot_sums = [&](const R *y) {
+                        if constexpr (DIAG && MP) {
+#pragma unroll
+                            for (int k = 0; k < 16; k++) Acl[k] = R(0);
+#pragma unroll
+                            for (int q = 0; q < 9; q++) Acl[harmonic_slot(q)] += pg[q] * y[q];
+                            if (high_l) {
+#pragma unroll
+                                for (int q = 9; q < 25; q++) Acl[harmonic_slot(q)] += pg[q] * y[q];
+                            }
+                        }
+                    };
+                    auto flush_slots = [&](const R *y) {
+                        if constexpr (DIAG && MP) {
+#pragma unroll
+                            for (int q = 0; q < 25; q++) part[CH_PLM + q] += QC[harmonic_slot(q)] * y[q];
+#pragma unroll
+                            for (int k = 0; k < 16; k++) QC[k] = R(0);
+                        }
+                    };
                     auto class_sums = [&](const R *y) {
-                        if constexpr (DIAG) {
+                        if constexpr (DIAG && !MP) {
                         Oc[3] = R(0);
                         Ec[0] = fsre + r0 * (pg[0] * y[0]) + r2 * (pg[6] * y[6] + pg[8] * y[8]);
                         Ec[1] = r2 * (pg[4] * y[4]);
@@ -515,6 +555,19 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                                 const double2 tv = S.table_d[ti];
                                 fre = tv.x + anre; fim = tv.y + anim;
                             }
+                        } else if constexpr (DIAG && MP) {
+                            const auto sg = [&](int c) -> R {
+                                if constexpr (F32) return L.sgn_f[s][c]; else return L.sgn_d[s][c];
+                            };
+                            A0 = Acl[0];
+                            A1 = sg(2) * Acl[1] + sg(4) * Acl[2] + sg(1) * Acl[3];
+                            A2 = Acl[6] + sg(3) * Acl[4] + sg(6) * Acl[5] + sg(5) * Acl[7];
+                            if (high_l) {
+                                A3 = sg(2) * Acl[8] + sg(7) * Acl[9] + sg(4) * Acl[10] + sg(1) * Acl[11];
+                                A4 = Acl[14] + sg(3) * Acl[12] + sg(6) * Acl[13] + sg(5) * Acl[15];
+                            }
+                            fre = fsre + r0 * A0 + r2 * A2 + r4 * A4;
+                            fim = fsim + r1 * A1 + r3 * A3;
                         } else if constexpr (DIAG) {
                             // fsph rides in the class-0 sums (sign +1 for every operation)
                             if constexpr (F32) {
@@ -559,15 +612,25 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                             // q_l = Re(g i^l rr_l z): even l rs_l Re(gz), odd l -rs_l Im(gz)
                             const R wre = gre * zre - gim * zim, wim = gre * zim + gim * zre;
                             const R q0 = r0 * wre, q1 = -r1 * wim, q2 = r2 * wre, q3 = -r3 * wim, q4 = r4 * wre;
-                            part[CH_PLM] += q0 * y[0];
+                            if constexpr (DIAG) {
+                                const R ql[5] = {q0, q1, q2, q3, q4};
+                                QC[0] += q0;
 #pragma unroll
-                            for (int q = 1; q < 4; q++) part[CH_PLM + q] += q1 * y[q];
+                                for (int k = 1; k < 16; k++) {
+                                    if constexpr (F32) QC[k] += L.sgn_f[s][slot_class(k)] * ql[slot_l(k)];
+                                    else QC[k] += L.sgn_d[s][slot_class(k)] * ql[slot_l(k)];
+                                }
+                            } else {
+                                part[CH_PLM] += q0 * y[0];
 #pragma unroll
-                            for (int q = 4; q < 9; q++) part[CH_PLM + q] += q2 * y[q];
+                                for (int q = 1; q < 4; q++) part[CH_PLM + q] += q1 * y[q];
 #pragma unroll
-                            for (int q = 9; q < 16; q++) part[CH_PLM + q] += q3 * y[q];
+                                for (int q = 4; q < 9; q++) part[CH_PLM + q] += q2 * y[q];
 #pragma unroll
-                            for (int q = 16; q < 25; q++) part[CH_PLM + q] += q4 * y[q];
+                                for (int q = 9; q < 16; q++) part[CH_PLM + q] += q3 * y[q];
+#pragma unroll
+                                for (int q = 16; q < 25; q++) part[CH_PLM + q] += q4 * y[q];
+                            }
                             const R dre = dr[2] * A0 + dr[4] * A2 + dr[6] * A4;
                             const R dim = dr[3] * A1 + dr[5] * A3;
                             Kre += dre * zre - dim * zim;
@@ -578,10 +641,15 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
 #pragma unroll
                         for (int s = 0; s < NSC; s++) {
                             if constexpr (DIAG) {
-                                if (s % CS == 0) class_sums(recs[s].y);
+                                if (s % CS == 0) {
+                                    if (s > 0) flush_slots(recs[s - CS].y);
+                                    class_sums(recs[s].y);
+                                    slot_sums(recs[s].y);
+                                }
                             }
                             term(s);
                         }
+                        if constexpr (DIAG) flush_slots(recs[NSC - CS].y);
                     } else {
 #pragma unroll 1
                         for (int s = 0; s < nS; s++) term(s);

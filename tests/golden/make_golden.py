@@ -31,7 +31,8 @@ from oracle import ref as R  # noqa: E402
 
 def hc_cases():
     cases = []
-    for i, sg in enumerate(["P1", "P-1", "P21", "P21/c", "P212121", "C2/c", "P43212", "P-1(shift)", "I2/m-like"]):
+    for i, sg in enumerate(["P1", "P-1", "P21", "P21/c", "P212121", "C2/c", "P43212", "P-1(shift)", "I2/m-like",
+                            "P41", "Pbca"]):
         st = W.small_case(sg, n_atoms=5, stol_max=0.55, seed=100 + i, improper_lcs=True)
         cases.append((f"hc_{sg.replace('/', '_').replace('(', '_').replace(')', '')}", st))
     st = W.config0(seed=0)

@@ -213,13 +213,16 @@ def test_single_call_matches_update_then_calculate(engine):
         a = calc.calculate(st.dtdf, precision=prec)
         calc.update_atoms(st.xyz, st.adp, st.occupancy)
         b = calc.calculate(st.dtdf, precision=prec, atoms=(xyz2, st.adp, occ2))
-        assert np.array_equal(a["f"], b["f"]) and np.array_equal(a["d_xyz"], b["d_xyz"])
-        assert np.array_equal(a["d_occ"], b["d_occ"])
+        # equal up to the order of the FP64 atomic sums across blocks
+        assert rel_f(b["f"], a["f"]) < 1e-13
+        for k in ("d_xyz", "d_adp", "d_occ"):
+            assert rel_norm(b[k], a[k]) < 1e-13, k
         # the uploaded parameters stay resident for the next plain call
         c = calc.calculate(st.dtdf, precision=prec, adp_layout="padded")
-        assert np.array_equal(a["f"], c["f"])
+        assert rel_f(c["f"], a["f"]) < 1e-13
         for i, v in enumerate(a["d_adp"]):
-            assert np.array_equal(c["d_adp"][i, :len(v)], v) and not np.any(c["d_adp"][i, len(v):])
+            assert np.allclose(c["d_adp"][i, :len(v)], v, rtol=1e-12, atol=1e-9 * np.abs(v).max())
+            assert not np.any(c["d_adp"][i, len(v):])
 
 
 def test_reflection_set_change_and_repeat(engine):
