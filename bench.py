@@ -40,9 +40,20 @@ sys.path.insert(0, REPO)
 
 import numpy as np  # noqa: E402
 
-TRAFFIC_KEY = "sf_grad_kernel3<float,HC,0,ISO,4>@config1"
-FLOPS_PER_TERM_CONFIG1 = 94  # phase 6 + multipole forward 60 + 1 + f*e*T 8 + accumulate 4 + adjoint 6 + xyz 6 + B 2 + occ 1
-WORKLOAD = "config1: HC multipoles l<=4, 5000 atoms (150 types), P212121, 54704 hkl d>=1.5A, iso B, dF/d(xyz,B,occ)"
+# algorithmic flops per term (FMA = 2; sincos and exp counted apart):
+#   config1: phase 6 + multipole forward 60 + 1 + f*e*T 8 + accumulate 4 + adjoint 6 + xyz 6 + B 2 + occ 1 = 94
+#   config2: forward 91 (with the aniso exponent 12) + full adjoint 104 (xyz 6, U 12, occ 1, Pv 6, kappa 4,
+#            kappa' 14, Plm 55, p 6) = 195
+WORKLOADS = {
+    "config1": dict(seed=1, multipoles=False, flops=94, fp64_frac=1.0, cpu_frac=0.25,
+                    traffic_key="sf_grad_kernel3<float,HC,0,ISO,4>@config1",
+                    desc="config1: HC multipoles l<=4, 5000 atoms (150 types), P212121, 54704 hkl d>=1.5A, iso B, "
+                         "dF/d(xyz,B,occ)"),
+    "config2": dict(seed=2, multipoles=True, flops=195, fp64_frac=0.05, cpu_frac=0.002,
+                    traffic_key="sf_grad_kernel3<float,HC,MP,ANISO,8>@config2",
+                    desc="config2: HC multipoles l<=4, 50000 atoms (300 types), P43212, all hkl d>=1.2A, aniso U "
+                         "(H iso), dF/d(xyz,U,occ,Pv,Plm,kappa,kappa')"),
+}
 
 
 def dist_env():
@@ -106,12 +117,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def kernel_traffic():
+def kernel_traffic(key):
     """DRAM bytes per launch of the FP32 kernel on this workload, from the
     committed ncu summary (dram__bytes_read.sum + dram__bytes_write.sum)."""
     try:
         with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "ncu_traffic.json")) as fh:
-            rec = json.load(fh).get(TRAFFIC_KEY)
+            rec = json.load(fh).get(key)
         return rec["dram_bytes_per_launch"] if rec else None
     except (OSError, ValueError, KeyError):
         return None
@@ -134,13 +145,13 @@ def fp32_peak_tflops(device):
     return out.value
 
 
-def cpu_baseline(st, sample_frac, threads):
+def cpu_baseline(st, sample_frac, threads, multipoles=False):
     """The reference engine's algorithm on the host cores (oracle port)."""
     from oracle import oracle as O
     m = max(1, int(st.n_hkl * sample_frac))
     sel = np.arange(m)
     t0 = time.perf_counter()
-    O.compute(st, hkl_subset=sel, n_threads=threads)
+    O.compute(st, hkl_subset=sel, n_threads=threads, multipoles=multipoles)
     dt = time.perf_counter() - t0
     terms = st.n_atoms * st.sg.point_group_order * m
     return terms / dt, dt, m
@@ -151,12 +162,13 @@ def run_reference(args):
     if rank != 0:
         return 0
     from discamb_gb300 import workloads as W
-    st = W.config1()
+    wl = WORKLOADS[args.workload]
+    st = getattr(W, args.workload)(seed=wl["seed"])
     threads = os.cpu_count() or 1
-    frac = args.reference_sample
+    frac = args.reference_sample if args.workload == "config1" else wl["cpu_frac"]
     vals = []
     for i in range(args.warmup + args.steps):
-        v, dt, m = cpu_baseline(st, frac, threads)
+        v, dt, m = cpu_baseline(st, frac, threads, multipoles=wl["multipoles"])
         if i >= args.warmup:
             vals.append((v, dt))
     value = statistics.median(v for v, _ in vals)
@@ -165,9 +177,9 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "sample": f"first {frac:.0%} of the reflections per step"},
+            "config": {"workload": wl["desc"], "sample": f"first {frac:.1%} of the reflections per step"},
             "cpu_baseline": {"value": value, "unit": "terms/s", "cores": threads, "kind": "port",
-                             "sample": f"config1 atoms x first {int(st.n_hkl * frac)} reflections per step"},
+                             "sample": f"{args.workload} atoms x first {int(st.n_hkl * frac)} reflections per step"},
             "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -183,7 +195,9 @@ def run_gpu(args):
     torch.cuda.set_device(device)
     from discamb_gb300 import api, build, workloads as W
     build.build()
-    st = W.config1(seed=1 + rank)
+    wl = WORKLOADS[args.workload]
+    st = getattr(W, args.workload)(seed=wl["seed"] + rank)
+    mpd = wl["multipoles"]
     eng = api.Engine(device)
     calc = api.HcCalculator(eng, st)
     n_hkl, n = st.n_hkl, st.n_atoms
@@ -196,19 +210,22 @@ def run_gpu(args):
     assert sptr != 0
     dtdf = torch.tensor(np.stack([st.dtdf.real, st.dtdf.imag], 1), dtype=torch.float64, device=dev).contiguous()
     f = torch.empty(n_hkl, 2, dtype=torch.float64, device=dev)
-    g = {k: torch.empty(n, w, dtype=torch.float64, device=dev) for k, w in (("d_xyz", 3), ("d_adp", 6), ("d_occ", 1))}
-    outs = {"f": f.data_ptr(), "d_xyz": g["d_xyz"].data_ptr(), "d_adp": g["d_adp"].data_ptr(),
-            "d_occ": g["d_occ"].data_ptr()}
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    widths = [("d_xyz", 3), ("d_adp", 6), ("d_occ", 1)]
+    if mpd:
+        widths += [("d_pval", 1), ("d_plm", 25), ("d_kappa", 1), ("d_kappa_prime", 1)]
+    g = {k: torch.empty(n, w, dtype=torch.float64, device=dev) for k, w in widths}
+    outs = {"f": f.data_ptr(), **{k: v.data_ptr() for k, v in g.items()}}
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > L2 (129 MB)
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    def timed_device(prec, steps, warmup):
+    def timed_device(prec, steps, warmup, calc_=calc, dtdf_=dtdf, outs_=outs):
         for _ in range(warmup):
-            calc.calculate_device(dtdf.data_ptr(), outs, precision=prec, stream=sptr)
+            flush.zero_()
+            calc_.calculate_device(dtdf_.data_ptr(), outs_, precision=prec, multipoles=mpd, stream=sptr)
         torch.cuda.synchronize(dev)
         barrier()
         torch.cuda.synchronize(dev)
@@ -219,11 +236,11 @@ def run_gpu(args):
         for i in range(steps):
             flush.zero_()
             ev[i][0].record(stream)
-            calc.calculate_device(dtdf.data_ptr(), outs, precision=prec, stream=sptr)
+            calc_.calculate_device(dtdf_.data_ptr(), outs_, precision=prec, multipoles=mpd, stream=sptr)
             ev[i][1].record(stream)
-            launches += calc.last_launch_count()
+            launches += calc_.last_launch_count()
             stream.synchronize()
-            kern.append(calc.last_kernel_ms())
+            kern.append(calc_.last_kernel_ms())
         torch.cuda.synchronize(dev)
         barrier()
         torch.cuda.synchronize(dev)
@@ -234,24 +251,39 @@ def run_gpu(args):
     with ClockSampler(device) as clk:
         ms32, kern32, launches32, wall32 = timed_device(api.DSF_FP32_BULK, args.steps, args.warmup)
     clocks = clk.summary()
-    ms64, kern64, _, _ = timed_device(api.DSF_FP64, max(2, min(args.steps, 3)), 1)
+    # the plain FP64 form, on the whole reflection set or on a leading fraction of it
+    frac64 = wl["fp64_frac"]
+    if frac64 < 1.0:
+        m64 = max(16, int(n_hkl * frac64))
+        calc.set_hkl(st.hkl[:m64])
+        ms64, kern64, _, _ = timed_device(api.DSF_FP64, 2, 1, dtdf_=dtdf[:m64].contiguous())
+        calc.set_hkl(st.hkl)
+        terms64 = terms * m64 / n_hkl
+    else:
+        ms64, kern64, _, _ = timed_device(api.DSF_FP64, max(2, min(args.steps, 3)), 1)
+        terms64 = terms
 
     # end to end through the reference-shaped host call (atoms + dT/dF in, F and
     # derivatives out); the library stages through its own pinned buffer
     xyz_h = st.xyz.copy()
     adp_h = st.adp_array()
     occ_h = st.occupancy.copy()
+
+    def host_call():
+        return calc.calculate(st.dtdf, precision=api.DSF_FP32_BULK, atoms=(xyz_h, adp_h, occ_h),
+                              adp_layout="padded", multipoles=mpd)
+
     for _ in range(args.warmup):
-        r = calc.calculate(st.dtdf, precision=api.DSF_FP32_BULK, atoms=(xyz_h, adp_h, occ_h), adp_layout="padded")
+        host_call()
     e2e = []
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        r = calc.calculate(st.dtdf, precision=api.DSF_FP32_BULK, atoms=(xyz_h, adp_h, occ_h), adp_layout="padded")
+        host_call()
         e2e.append(time.perf_counter() - t0)
     h2d = 80 * n + 16 * n_hkl
-    d2h = 16 * n_hkl + (3 + 6 + 1) * 8 * n
+    d2h = 16 * n_hkl + sum(w for _, w in widths) * 8 * n
 
     step32 = statistics.mean(ms32)
     step64 = statistics.mean(ms64)
@@ -265,29 +297,31 @@ def run_gpu(args):
     value = world * terms / (step32 * 1e-3)
     if rank != 0:
         return 0
-    achieved = FLOPS_PER_TERM_CONFIG1 * terms / (k32 * 1e-3) * 1e-12
+    achieved = wl["flops"] * terms / (k32 * 1e-3) * 1e-12
     peak = fp32_peak_tflops(device)
-    cpu_v, cpu_dt, cpu_m = cpu_baseline(st, args.cpu_sample, os.cpu_count() or 1)
+    cpu_v, cpu_dt, cpu_m = cpu_baseline(st, wl["cpu_frac"], os.cpu_count() or 1, multipoles=mpd)
     mp = measured_peaks()
     line = {
         "metric": "atom*symop*hkl terms/s (SF+grad)", "value": value, "unit": "terms/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step32, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk (integer phase reduction, f64 accumulation)",
         "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "terms_per_step": terms, "l2": "flushed (256 MB write) between timed steps",
+        "config": {"workload": wl["desc"], "terms_per_step": terms, "l2": "flushed (256 MB write) between timed steps",
                    "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
-        "fp64": {"value": world * terms / (step64 * 1e-3), "ms_per_step": step64,
-                 "kernel_ms": statistics.mean(kern64), "fp32_over_fp64": step64 / step32},
+        "fp64": {"value": world * terms64 / (step64 * 1e-3), "ms_per_step": step64,
+                 "kernel_ms": statistics.mean(kern64),
+                 "fp32_over_fp64": (terms / step32) / (terms64 / step64),
+                 "sample": "all reflections" if frac64 >= 1.0 else f"first {frac64:.0%} of the reflections"},
         "e2e": {"value": world * terms / (e2e_ms * 1e-3), "unit": "terms/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": kernel_traffic(),
+                     "frac": achieved / peak if peak else None, "traffic": kernel_traffic(wl["traffic_key"]),
                      "peak_source": "FP32 FMA throughput probe measured in this run (MEASURED_PEAKS.json lists "
                                     "HBM and bf16 tensor peaks only)",
-                     "flops_per_term": FLOPS_PER_TERM_CONFIG1, "kernel_ms": k32,
+                     "flops_per_term": wl["flops"], "kernel_ms": k32,
                      "hbm_peak_gbs_measured": mp.get("hbm_gbs")},
         "cpu_baseline": {"value": cpu_v, "unit": "terms/s", "cores": os.cpu_count() or 1, "kind": "port",
-                         "sample": f"config1 atoms x first {cpu_m} reflections, one call ({cpu_dt:.1f} s)"},
+                         "sample": f"{args.workload} atoms x first {cpu_m} reflections, one call ({cpu_dt:.1f} s)"},
         "gpu_launches": launches32,
         "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
         "wall_s_timed_region": wall32,
@@ -304,6 +338,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-sample", type=float, default=0.25)
     ap.add_argument("--reference-sample", type=float, default=0.1)
     args = ap.parse_args()

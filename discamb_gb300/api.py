@@ -106,10 +106,19 @@ def library():
         L.dsf_calculate_atoms.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), _P(C.c_double),
                                           _P(C.c_double), _P(C.c_double), _P(C.c_int), _P(_Out)]
         L.dsf_calculate_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, _P(_Out), C.c_void_p]
+        L.dsf_calculate_batch_device.argtypes = [_P(C.c_void_p), C.c_int, C.c_int, C.c_int, _P(C.c_void_p),
+                                                 _P(_Out), C.c_void_p]
+        L.dsf_calculate_batch.argtypes = [_P(C.c_void_p), C.c_int, C.c_int, C.c_int, _P(C.c_void_p),
+                                          _P(C.c_void_p), _P(_Out)]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
     return _lib
+
+
+def _flags(derivatives, multipoles):
+    return (DSF_D_XYZ if "xyz" in derivatives else 0) | (DSF_D_ADP if "adp" in derivatives else 0) | \
+        (DSF_D_OCC if "occ" in derivatives else 0) | (DSF_D_MULTIPOLE if multipoles else 0)
 
 
 def _d(a):
@@ -137,6 +146,46 @@ class Engine:
         if rc != 0:
             msg = self.lib.dsf_last_error(self.h)
             raise DsfError(f"{what}: status {rc}: {msg.decode() if msg else ''}")
+
+    def calculate_batch(self, calcs, dtdfs, precision=DSF_FP32_BULK, derivatives=("xyz", "adp", "occ"),
+                        multipoles=False, includes=None):
+        """Several calculators of this engine in one submission
+        (dsf_calculate_batch): host dT/dF per calculator, the resident atoms;
+        returns one result dict per calculator (padded [n][6] ADP layout)."""
+        n = len(calcs)
+        flags = _flags(derivatives, multipoles)
+        hs = (C.c_void_p * n)(*[c.h.value for c in calcs])
+        keep, gp, ip = [], (C.c_void_p * n)(), (C.c_void_p * n)()
+        outs = (_Out * n)()
+        res = []
+        for i, c in enumerate(calcs):
+            g = np.ascontiguousarray(dtdfs[i], dtype=np.complex128).view(np.float64)
+            keep.append(g)
+            gp[i] = g.ctypes.data
+            if includes is not None and includes[i] is not None:
+                inc = np.ascontiguousarray(includes[i], dtype=np.int32)
+                keep.append(inc)
+                ip[i] = inc.ctypes.data
+            r = c._out_arrays(multipoles)
+            res.append(r)
+            c._fill_out(outs[i], r, multipoles)
+        self.check(self.lib.dsf_calculate_batch(hs, n, int(precision), flags, gp,
+                                                ip if includes is not None else None, outs), "calculate_batch")
+        return [c._result(r, multipoles, "padded") for c, r in zip(calcs, res)]
+
+    def calculate_batch_device(self, calcs, dtdf_ptrs, outputs, precision=DSF_FP32_BULK,
+                               derivatives=("xyz", "adp", "occ"), multipoles=False, stream=0):
+        """Device-resident batch (dsf_calculate_batch_device): dtdf_ptrs[i]
+        and outputs[i] (dict of device pointers) per calculator."""
+        n = len(calcs)
+        hs = (C.c_void_p * n)(*[c.h.value for c in calcs])
+        gp = (C.c_void_p * n)(*[int(p) for p in dtdf_ptrs])
+        outs = (_Out * n)()
+        for i, o in enumerate(outputs):
+            for k, v in o.items():
+                setattr(outs[i], k, v)
+        self.check(self.lib.dsf_calculate_batch_device(hs, n, int(precision), _flags(derivatives, multipoles), gp,
+                                                       outs, C.c_void_p(stream)), "calculate_batch_device")
 
     def close(self):
         """Destroys the engine after every structure created on it."""
@@ -271,6 +320,35 @@ class _Calculator:
         (x1, p1), (x2, p2), (x3, p3) = self._atom_arrays(xyz, adp, occupancy)
         self.engine.check(self.lib.dsf_structure_update_atoms(self.h, p1, p2, p3), "update_atoms")
 
+    def _out_arrays(self, multipoles):
+        n, m = self.n_atoms, self.n_hkl
+        r = dict(f=np.zeros(2 * m), d_xyz=np.zeros(3 * n), d_adp=np.zeros(6 * n), d_occ=np.zeros(n))
+        if multipoles:
+            r.update(d_pval=np.zeros(n), d_plm=np.zeros(25 * n), d_kappa=np.zeros(n), d_kappa_prime=np.zeros(n))
+        return r
+
+    @staticmethod
+    def _fill_out(o, r, multipoles):
+        o.f = r["f"].ctypes.data
+        o.d_xyz, o.d_adp, o.d_occ = r["d_xyz"].ctypes.data, r["d_adp"].ctypes.data, r["d_occ"].ctypes.data
+        if multipoles:
+            o.d_pval, o.d_plm = r["d_pval"].ctypes.data, r["d_plm"].ctypes.data
+            o.d_kappa, o.d_kappa_prime = r["d_kappa"].ctypes.data, r["d_kappa_prime"].ctypes.data
+
+    def _result(self, r, multipoles, adp_layout):
+        n = self.n_atoms
+        da = r["d_adp"].reshape(n, 6)
+        if adp_layout == "padded":
+            d_adp = da
+        else:
+            nadp = self._n_adp
+            d_adp = [da[i, :nadp[i]] for i in range(n)]
+        out = dict(f=r["f"].view(np.complex128), d_xyz=r["d_xyz"].reshape(n, 3), d_adp=d_adp, d_occ=r["d_occ"])
+        if multipoles:
+            out.update(d_pval=r["d_pval"], d_plm=r["d_plm"].reshape(n, 25), d_kappa=r["d_kappa"],
+                       d_kappa_p=r["d_kappa_prime"])
+        return out
+
     def calculate(self, dtdf, precision=DSF_FP64, derivatives=("xyz", "adp", "occ"), multipoles=False,
                   include=None, atoms=None, adp_layout="list"):
         """F and dT/dparam in the crystal's conventions (host buffers).
@@ -279,18 +357,11 @@ class _Calculator:
         adp_layout "list": d_adp[i] holds the atom's own ADP components (the
         reference's adp_derivatives); "padded": one [n][6] array, zero past
         each atom's component count."""
-        n, m = self.n_atoms, self.n_hkl
-        flags = (DSF_D_XYZ if "xyz" in derivatives else 0) | (DSF_D_ADP if "adp" in derivatives else 0) | \
-                (DSF_D_OCC if "occ" in derivatives else 0) | (DSF_D_MULTIPOLE if multipoles else 0)
+        flags = _flags(derivatives, multipoles)
         g = np.ascontiguousarray(dtdf, dtype=np.complex128).view(np.float64)
-        f = np.zeros(2 * m)
-        dx, da, do = np.zeros(3 * n), np.zeros(6 * n), np.zeros(n)
-        dpv, dplm, dk, dkp = np.zeros(n), np.zeros(25 * n), np.zeros(n), np.zeros(n)
+        r = self._out_arrays(multipoles)
         o = _Out()
-        o.f = f.ctypes.data
-        o.d_xyz, o.d_adp, o.d_occ = dx.ctypes.data, da.ctypes.data, do.ctypes.data
-        if multipoles:
-            o.d_pval, o.d_plm, o.d_kappa, o.d_kappa_prime = dpv.ctypes.data, dplm.ctypes.data, dk.ctypes.data, dkp.ctypes.data
+        self._fill_out(o, r, multipoles)
         inc = None
         if include is not None:
             incarr, inc = _i(np.asarray(include, dtype=np.int32))
@@ -301,16 +372,7 @@ class _Calculator:
             (x1, p1), (x2, p2), (x3, p3) = self._atom_arrays(*atoms)
             self.engine.check(self.lib.dsf_calculate_atoms(self.h, int(precision), flags, p1, p2, p3, gp, inc,
                                                            C.byref(o)), "calculate")
-        da = da.reshape(n, 6)
-        if adp_layout == "padded":
-            d_adp = da
-        else:
-            nadp = self._n_adp
-            d_adp = [da[i, :nadp[i]] for i in range(n)]
-        out = dict(f=f.view(np.complex128), d_xyz=dx.reshape(n, 3), d_adp=d_adp, d_occ=do)
-        if multipoles:
-            out.update(d_pval=dpv, d_plm=dplm.reshape(n, 25), d_kappa=dk, d_kappa_p=dkp)
-        return out
+        return self._result(r, multipoles, adp_layout)
 
     def calculate_structure_factors_and_derivatives(self, xyz, adp, occupancy, hkl, dtdf, include=None,
                                                     precision=DSF_FP64, multipoles=False):
@@ -337,8 +399,7 @@ class _Calculator:
                          multipoles=False, stream=0):
         """Device-resident call: dtdf_ptr = device pointer to [n_hkl][2]
         doubles, outputs = dict of device pointers (f required)."""
-        flags = (DSF_D_XYZ if "xyz" in derivatives else 0) | (DSF_D_ADP if "adp" in derivatives else 0) | \
-                (DSF_D_OCC if "occ" in derivatives else 0) | (DSF_D_MULTIPOLE if multipoles else 0)
+        flags = _flags(derivatives, multipoles)
         o = _Out()
         for k, v in outputs.items():
             setattr(o, k, v)

@@ -23,19 +23,18 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
 
 namespace dsf {
-struct SfLaunch;
 cudaError_t launch_rs_prep(const DevStructure &S, int n_hkl_pad, void *rs_f, void *rs_d, cudaStream_t st);
 cudaError_t launch_tr_prep(const DevStructure &S, int n_hkl_pad, void *tr_f, void *tr_d, void *trm_f, void *trm_d,
                            bool mp, cudaStream_t st);
 size_t rs_record_bytes(bool fp64);
 size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types);
-cudaError_t launch_sf3(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool fp64, bool mp, bool aniso,
-                       int n_tiles, int n_chunks, cudaStream_t st);
+cudaError_t launch_sf3(const K3Args &A, int model, bool fp64, bool mp, bool aniso);
 cudaError_t launch_sf_grad(const DevStructure &S, const CallBuffers &C, bool fp64, bool mp, int hkl_chunk, int ht,
                            cudaStream_t st);
 size_t sf_grad_smem_bytes(bool fp64, int ht, int n_sym);
@@ -110,16 +109,6 @@ int fail(dsf_engine *e, int code, const std::string &msg)
 {
     if (e) e->err = msg;
     return code;
-}
-
-void mat3_mul(const double *a, const double *b, double *c)
-{
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) {
-            double s = 0;
-            for (int k = 0; k < 3; k++) s += a[3 * i + k] * b[3 * k + j];
-            c[3 * i + j] = s;
-        }
 }
 
 bool mat_inverse(const double *a, double *inv, int n)
@@ -1423,39 +1412,46 @@ double dsf_last_kernel_ms(dsf_structure *s)
     return (double)ms;
 }
 
-int dsf_calculate_device(dsf_structure *s, int precision, int flags, const double *dtdf_device,
-                         const dsf_outputs *out, void *stream)
+// ---------------------------------------------------------------------------
+// one call, in phases: checks, adjoint weights + zeroed accumulators, the SF
+// kernel launches (one per ADP kind), the F and derivative epilogues
+// ---------------------------------------------------------------------------
+static int call_check(dsf_structure *s, int precision, int flags, const double *dtdf_device, const dsf_outputs *out)
 {
-    if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
     if (!s->have_hkl) return fail(e, DSF_ERR_STATE, "no reflections set");
     if (!s->have_atoms) return fail(e, DSF_ERR_STATE, "atomic parameters not uploaded");
     if (!out || !out->f || !dtdf_device) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
     if (precision != DSF_FP64 && precision != DSF_FP32_BULK) return fail(e, DSF_ERR_ARGUMENT, "unknown precision");
-    cudaSetDevice(e->device);
-    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
-    const bool fp64 = precision == DSF_FP64;
     const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
-    const int n_hkl = s->n_hkl, n = s->n_atoms;
-    int launches = 0;
-    gw_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, reinterpret_cast<const double2 *>(dtdf_device),
-                                                   s->d_hmult.as<double>(), s->d_cinv.as<double2>(), s->centro_mode,
-                                                   s->d_gw_d.as<double2>(), s->d_gw_f.as<float2>(),
-                                                   s->d_hperm.as<int>());
-    launches++;
-    DSF_CUDA(cudaGetLastError());
-    DSF_CUDA(cudaMemsetAsync(s->d_facc.p, 0, 16 * (size_t)n_hkl, st));
-    DSF_CUDA(cudaMemsetAsync(s->d_gacc.p, 0, sizeof(double) * kNch * (size_t)n, st));
     if (mp && !s->trm_valid) {
         int rc = build_radial_tables(s, true);
         if (rc) return rc;
     }
-    CallBuffers C;
+    return DSF_OK;
+}
+
+static int call_pre(dsf_structure *s, const double *dtdf_device, cudaStream_t st)
+{
+    dsf_engine *e = s->eng;
+    const int n_hkl = s->n_hkl;
+    gw_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, reinterpret_cast<const double2 *>(dtdf_device),
+                                                   s->d_hmult.as<double>(), s->d_cinv.as<double2>(), s->centro_mode,
+                                                   s->d_gw_d.as<double2>(), s->d_gw_f.as<float2>(),
+                                                   s->d_hperm.as<int>());
+    DSF_CUDA(cudaGetLastError());
+    DSF_CUDA(cudaMemsetAsync(s->d_facc.p, 0, 16 * (size_t)n_hkl, st));
+    DSF_CUDA(cudaMemsetAsync(s->d_gacc.p, 0, sizeof(double) * kNch * (size_t)s->n_atoms, st));
+    return DSF_OK;
+}
+
+static void call_buffers(dsf_structure *s, bool fp64, CallBuffers &C, SfLaunch &L, SignTable &G)
+{
     C.gw_d = s->d_gw_d.as<double2>();
     C.gw_f = s->d_gw_f.as<float2>();
     C.f_acc = s->d_facc.as<double2>();
     C.g_acc = s->d_gacc.as<double>();
-    SfLaunch L{};
+    L = SfLaunch{};
     L.n_hkl_pad = s->n_hkl_pad;
     L.rs = fp64 ? s->d_rs_d.p : s->d_rs_f.p;
     L.tr = fp64 ? s->d_tr_d.p : s->d_tr_f.p;
@@ -1465,6 +1461,7 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     L.tile_lmax = s->d_tile_lmax.as<int>();
     // class-sum kernels: HC, operations in sign-diagonal cosets
     L.coset = 0;
+    std::memset(&G, 0, sizeof(G));
     if (s->model == MODEL_HC && s->coset_size && coset_form_compiled(fp64, s->n_sym, s->coset_size)) {
         L.coset = s->coset_size;
         for (int op = 0; op < s->n_sym; op++)
@@ -1472,41 +1469,44 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
                 int sg = 1;
                 for (int i = 0; i < 3; i++)
                     if ((c >> i) & 1) sg *= s->sym_sign[3 * op + i];
-                L.sgn_f[op][c] = (float)sg;
-                L.sgn_d[op][c] = (double)sg;
+                G.f[op][c] = (float)sg;
+                G.d[op][c] = (double)sg;
             }
     }
-    if (!s->ev_begin) {
-        DSF_CUDA(cudaEventCreate(&s->ev_begin));
-        DSF_CUDA(cudaEventCreate(&s->ev_end));
-    }
-    DSF_CUDA(cudaEventRecord(s->ev_begin, st));
-    // one launch per ADP kind (tiles [0, n_tiles_plain) without anisotropic ADPs)
-    const int ranges[2][2] = {{0, s->n_tiles_plain}, {s->n_tiles_plain, s->n_tiles}};
-    for (int kind = 0; kind < 2; kind++) {
-        const int t0 = ranges[kind][0], nt = ranges[kind][1] - ranges[kind][0];
-        if (nt <= 0) continue;
-        L.tile_offset = t0;
-        L.max_types = kind ? s->max_types_aniso : s->max_types_plain;
-        // reflections per sub-tile from the shared-memory budget (several blocks per SM)
-        int ht = kMaxHT;
-        const size_t budget = std::min<size_t>(e->max_smem, fp64 ? 200 * 1024 : 100 * 1024);
-        while (ht > 4 && sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > budget) ht /= 2;
-        if (sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > e->max_smem)
-            return fail(e, DSF_ERR_UNSUPPORTED, "shared-memory tile does not fit this device");
-        L.ht = ht;
-        // reflection chunks so the grid covers the SMs several times
-        const int target = std::max(1, e->n_sm) * 8;
-        const int n_chunks0 = std::max(1, target / nt);
-        int chunk = (n_hkl + n_chunks0 - 1) / n_chunks0;
-        chunk = std::max(chunk, 4 * ht);
-        chunk = (chunk + ht - 1) / ht * ht;
-        L.hkl_chunk = chunk;
-        const int n_chunks = (n_hkl + chunk - 1) / chunk;
-        DSF_CUDA(launch_sf3(s->dev, C, L, fp64, mp, kind == 1, nt, n_chunks, st));
-        launches++;
-    }
-    DSF_CUDA(cudaEventRecord(s->ev_end, st));
+}
+
+// launch shape of the tiles of one ADP kind: reflections per sub-tile from the
+// shared-memory budget (several blocks per SM), reflection chunks of about
+// `block_terms` atom x reflection pairs per block (at least four sub-tiles)
+static int kind_shape(dsf_structure *s, int kind, bool fp64, bool mp, double block_terms, SfLaunch &L, int &nt,
+                      int &n_chunks, size_t &smem)
+{
+    dsf_engine *e = s->eng;
+    const int t0 = kind ? s->n_tiles_plain : 0, t1 = kind ? s->n_tiles : s->n_tiles_plain;
+    nt = t1 - t0;
+    n_chunks = 0;
+    if (nt <= 0) return DSF_OK;
+    L.tile_offset = t0;
+    L.max_types = kind ? s->max_types_aniso : s->max_types_plain;
+    int ht = kMaxHT;
+    const size_t budget = std::min<size_t>(e->max_smem, fp64 ? 200 * 1024 : 100 * 1024);
+    while (ht > 4 && sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > budget) ht /= 2;
+    smem = sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types);
+    if (smem > e->max_smem) return fail(e, DSF_ERR_UNSUPPORTED, "shared-memory tile does not fit this device");
+    L.ht = ht;
+    int chunk = (int)std::min<double>(s->n_hkl, std::max(1.0, block_terms / kTileAtoms));
+    chunk = std::max(chunk, 4 * ht);
+    chunk = (chunk + ht - 1) / ht * ht;
+    L.hkl_chunk = chunk;
+    n_chunks = (s->n_hkl + chunk - 1) / chunk;
+    return DSF_OK;
+}
+
+static int call_post(dsf_structure *s, int flags, const dsf_outputs *out, cudaStream_t st, int &launches)
+{
+    dsf_engine *e = s->eng;
+    const int n_hkl = s->n_hkl, n = s->n_atoms;
+    const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
     f_epilogue_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, s->d_facc.as<double2>(), s->d_hmult.as<double>(),
                                                            s->d_cinv.as<double2>(), s->centro_mode, out->f,
                                                            s->d_hperm.as<int>());
@@ -1529,14 +1529,198 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         launches++;
         DSF_CUDA(cudaGetLastError());
     }
+    return DSF_OK;
+}
+
+int dsf_calculate_device(dsf_structure *s, int precision, int flags, const double *dtdf_device,
+                         const dsf_outputs *out, void *stream)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    int rc = call_check(s, precision, flags, dtdf_device, out);
+    if (rc) return rc;
+    cudaSetDevice(e->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    const bool fp64 = precision == DSF_FP64;
+    const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
+    if ((rc = call_pre(s, dtdf_device, st))) return rc;
+    int launches = 1;
+    CallBuffers C;
+    SfLaunch L;
+    SignTable G;
+    call_buffers(s, fp64, C, L, G);
+    if (!s->ev_begin) {
+        DSF_CUDA(cudaEventCreate(&s->ev_begin));
+        DSF_CUDA(cudaEventCreate(&s->ev_end));
+    }
+    DSF_CUDA(cudaEventRecord(s->ev_begin, st));
+    // one launch per ADP kind (tiles [0, n_tiles_plain) without anisotropic ADPs); the
+    // reflection chunks make the grid cover the SMs about eight times
+    for (int kind = 0; kind < 2; kind++) {
+        int nt, n_chunks;
+        size_t smem;
+        const int ntk = kind ? s->n_tiles - s->n_tiles_plain : s->n_tiles_plain;
+        const int n_chunks0 = std::max(1, std::max(1, e->n_sm) * 8 / std::max(1, ntk));
+        const double block_terms = (double)kTileAtoms * ((s->n_hkl + n_chunks0 - 1) / n_chunks0);
+        if ((rc = kind_shape(s, kind, fp64, mp, block_terms, L, nt, n_chunks, smem))) return rc;
+        if (nt <= 0) continue;
+        K3Args A;
+        A.S = &s->dev;
+        A.C = &C;
+        A.L = &L;
+        A.G = &G;
+        A.n_sym = s->n_sym;
+        A.coset = L.coset;
+        A.n_tiles = nt;
+        A.n_chunks = n_chunks;
+        A.smem = smem;
+        A.st = st;
+        DSF_CUDA(launch_sf3(A, s->model, fp64, mp, kind == 1));
+        launches++;
+    }
+    DSF_CUDA(cudaEventRecord(s->ev_end, st));
+    if ((rc = call_post(s, flags, out, st, launches))) return rc;
     s->last_launches = launches;
     return DSF_OK;
 }
 
-// host-buffer call: optional atom upload, dT/dF upload, the device calculation,
-// read-back; staged through one pinned buffer per structure, one stream sync
-static int calculate_host(dsf_structure *s, int precision, int flags, const double *xyz, const double *adp,
-                          const double *occ, const double *dtdf, const int *include, const dsf_outputs *out)
+// Many structures of one engine in one submission: the FP32 SF kernels of all
+// structures without the multipole adjoint run as batched launches (one per
+// kernel shape and sign table, up to kBatchItems structures each); the rest
+// (FP64, multipole adjoint) launch per structure.  Adjoint weights and
+// epilogues launch per structure.
+int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int precision, int flags,
+                               const double *const *dtdf_device, const dsf_outputs *out_device, void *stream)
+{
+    if (!structures || n < 1 || !dtdf_device || !out_device) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = structures[0] ? structures[0]->eng : nullptr;
+    if (!e) return DSF_ERR_ARGUMENT;
+    for (int i = 0; i < n; i++) {
+        if (!structures[i] || structures[i]->eng != e)
+            return fail(e, DSF_ERR_ARGUMENT, "batch structures must belong to one engine");
+        int rc = call_check(structures[i], precision, flags, dtdf_device[i], &out_device[i]);
+        if (rc) return rc;
+    }
+    cudaSetDevice(e->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    const bool fp64 = precision == DSF_FP64;
+    int launches = 0, rc;
+    for (int i = 0; i < n; i++) {
+        if ((rc = call_pre(structures[i], dtdf_device[i], st))) return rc;
+        launches++;
+    }
+    // work per block so that the whole batch covers the SMs about eight times
+    double total = 0;
+    for (int i = 0; i < n; i++) total += (double)structures[i]->n_atoms * structures[i]->n_hkl;
+    const double block_terms = std::max<double>(kTileAtoms * 64.0, total / (std::max(1, e->n_sm) * 8.0));
+    // group the batched items by kernel shape and sign table
+    struct Group {
+        int model, aniso, n_sym, coset;
+        SignTable G;
+        size_t smem = 0;
+        std::vector<SfBatchItem> items;
+    };
+    std::vector<Group> groups;
+    for (int i = 0; i < n; i++) {
+        dsf_structure *s = structures[i];
+        const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
+        CallBuffers C;
+        SfLaunch L;
+        SignTable G;
+        call_buffers(s, fp64, C, L, G);
+        for (int kind = 0; kind < 2; kind++) {
+            int nt, n_chunks;
+            size_t smem;
+            if ((rc = kind_shape(s, kind, fp64, mp, block_terms, L, nt, n_chunks, smem))) return rc;
+            if (nt <= 0) continue;
+            if (fp64 || mp) {  // per-structure launch
+                K3Args A;
+                A.S = &s->dev;
+                A.C = &C;
+                A.L = &L;
+                A.G = &G;
+                A.n_sym = s->n_sym;
+                A.coset = L.coset;
+                A.n_tiles = nt;
+                A.n_chunks = n_chunks;
+                A.smem = smem;
+                A.st = st;
+                DSF_CUDA(launch_sf3(A, s->model, fp64, mp, kind == 1));
+                launches++;
+                continue;
+            }
+            Group *g = nullptr;
+            for (auto &x : groups)
+                if (x.model == s->model && x.aniso == kind && x.n_sym == s->n_sym && x.coset == L.coset &&
+                    (L.coset == 0 || std::memcmp(&x.G, &G, sizeof(G)) == 0)) {
+                    g = &x;
+                    break;
+                }
+            if (!g) {
+                groups.emplace_back();
+                g = &groups.back();
+                g->model = s->model;
+                g->aniso = kind;
+                g->n_sym = s->n_sym;
+                g->coset = L.coset;
+                g->G = G;
+            }
+            SfBatchItem it;
+            it.S = s->dev;
+            it.C = C;
+            it.L = L;
+            it.n_tiles = nt;
+            g->items.push_back(it);
+            g->smem = std::max(g->smem, smem);
+        }
+    }
+    static SfBatch B;  // host staging of the launch parameters (copied at launch)
+    static std::mutex mtx;
+    std::lock_guard<std::mutex> lock(mtx);
+    for (auto &g : groups)
+        for (size_t b0 = 0; b0 < g.items.size(); b0 += kBatchItems) {
+            const int m = (int)std::min<size_t>(kBatchItems, g.items.size() - b0);
+            B.n = m;
+            int blocks = 0;
+            for (int k = 0; k < m; k++) {
+                B.item[k] = g.items[b0 + k];
+                B.block_begin[k] = blocks;
+                const SfLaunch &L = B.item[k].L;
+                const int n_chunks = (B.item[k].S.n_hkl + L.hkl_chunk - 1) / L.hkl_chunk;
+                blocks += B.item[k].n_tiles * n_chunks;
+            }
+            B.block_begin[m] = blocks;
+            K3Args A;
+            A.B = &B;
+            A.G = &g.G;
+            A.n_sym = g.n_sym;
+            A.coset = g.coset;
+            A.blocks = blocks;
+            A.smem = g.smem;
+            A.st = st;
+            DSF_CUDA(launch_k3b_f32(A, g.model, g.aniso == 1));
+            launches++;
+        }
+    for (int i = 0; i < n; i++)
+        if ((rc = call_post(structures[i], flags, &out_device[i], st, launches))) return rc;
+    for (int i = 0; i < n; i++) structures[i]->last_launches = launches;
+    return DSF_OK;
+}
+
+// host-buffer calls, staged through one pinned buffer per structure:
+// host_stage enqueues the inclusion mask, the optional atom upload and dT/dF
+// on the engine stream; host_readback enqueues F, the derivatives and the
+// error flag back; host_finish (after the stream sync) checks the flag and
+// copies the results out
+struct HostCall {
+    dsf_outputs d;      // device output block
+    double *po = nullptr;
+    int *pk = nullptr;
+    size_t nf = 0, nout = 0;
+};
+
+static int host_stage(dsf_structure *s, const double *xyz, const double *adp, const double *occ,
+                      const double *dtdf, const int *include, const dsf_outputs *out, HostCall &hc)
 {
     if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
@@ -1568,7 +1752,6 @@ static int calculate_host(dsf_structure *s, int precision, int flags, const doub
         s->pinned_bytes = stage_bytes;
     }
     double *raw = (double *)s->pinned, *pg = raw + 10 * (size_t)n, *po = pg + 2 * (size_t)n_hkl;
-    int *pk = (int *)(po + nout);
     if (xyz) {
         for (int i = 0; i < n; i++) {
             for (int j = 0; j < 3; j++) {
@@ -1594,7 +1777,7 @@ static int calculate_host(dsf_structure *s, int precision, int flags, const doub
     std::memcpy(pg, dtdf, sizeof(double) * 2 * (size_t)n_hkl);
     DSF_CUDA(cudaMemcpyAsync(s->d_dtdf.p, pg, 16 * (size_t)n_hkl, cudaMemcpyHostToDevice, e->stream));
     double *base = s->d_out.as<double>();
-    dsf_outputs d;
+    dsf_outputs &d = hc.d;
     d.f = base;
     d.d_xyz = base + nf;
     d.d_adp = d.d_xyz + 3 * (size_t)n;
@@ -1603,19 +1786,34 @@ static int calculate_host(dsf_structure *s, int precision, int flags, const doub
     d.d_plm = d.d_pval + n;
     d.d_kappa = d.d_plm + 25 * (size_t)n;
     d.d_kappa_prime = d.d_kappa + n;
-    int rc = dsf_calculate_device(s, precision, flags, s->d_dtdf.as<double>(), &d, e->stream);
-    if (rc) return rc;
+    hc.po = po;
+    hc.pk = (int *)(po + nout);
+    hc.nf = nf;
+    hc.nout = nout;
+    return DSF_OK;
+}
+
+static int host_readback(dsf_structure *s, int flags, HostCall &hc)
+{
+    dsf_engine *e = s->eng;
     const bool mp = (flags & DSF_D_MULTIPOLE) != 0;
-    const size_t nback = mp ? nout : nf + 10 * (size_t)n;  // f, xyz, adp, occ (+ multipole block)
-    DSF_CUDA(cudaMemcpyAsync(po, base, sizeof(double) * nback, cudaMemcpyDeviceToHost, e->stream));
-    DSF_CUDA(cudaMemcpyAsync(pk, s->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
-    DSF_CUDA(cudaStreamSynchronize(e->stream));
-    if (*pk) {
+    const size_t nback = mp ? hc.nout : hc.nf + 10 * (size_t)s->n_atoms;  // f, xyz, adp, occ (+ multipole block)
+    DSF_CUDA(cudaMemcpyAsync(hc.po, hc.d.f, sizeof(double) * nback, cudaMemcpyDeviceToHost, e->stream));
+    DSF_CUDA(cudaMemcpyAsync(hc.pk, s->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    return DSF_OK;
+}
+
+static int host_finish(dsf_structure *s, int flags, const HostCall &hc, const dsf_outputs *out)
+{
+    dsf_engine *e = s->eng;
+    const int n = s->n_atoms;
+    const bool mp = (flags & DSF_D_MULTIPOLE) != 0;
+    if (*hc.pk) {
         cudaMemsetAsync(s->d_err.p, 0, sizeof(int), e->stream);
         return fail(e, DSF_ERR_TIMEOUT, "a shared-memory pipeline wait of the kernel ran out");
     }
-    std::memcpy(out->f, po, sizeof(double) * nf);
-    const double *q = po + nf;
+    std::memcpy(out->f, hc.po, sizeof(double) * hc.nf);
+    const double *q = hc.po + hc.nf;
     struct { double *dst; size_t off, n; } cp[] = {
         {out->d_xyz, 0, 3 * (size_t)n}, {out->d_adp, 3 * (size_t)n, 6 * (size_t)n},
         {out->d_occ, 9 * (size_t)n, (size_t)n}, {out->d_pval, 10 * (size_t)n, (size_t)n},
@@ -1623,6 +1821,46 @@ static int calculate_host(dsf_structure *s, int precision, int flags, const doub
         {out->d_kappa_prime, 37 * (size_t)n, (size_t)n}};
     for (auto &c : cp)
         if (c.dst && (c.off < 10 * (size_t)n || mp)) std::memcpy(c.dst, q + c.off, sizeof(double) * c.n);
+    return DSF_OK;
+}
+
+static int calculate_host(dsf_structure *s, int precision, int flags, const double *xyz, const double *adp,
+                          const double *occ, const double *dtdf, const int *include, const dsf_outputs *out)
+{
+    HostCall hc;
+    int rc = host_stage(s, xyz, adp, occ, dtdf, include, out, hc);
+    if (rc) return rc;
+    dsf_engine *e = s->eng;
+    if ((rc = dsf_calculate_device(s, precision, flags, s->d_dtdf.as<double>(), &hc.d, e->stream))) return rc;
+    if ((rc = host_readback(s, flags, hc))) return rc;
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    return host_finish(s, flags, hc, out);
+}
+
+int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int flags,
+                        const double *const *dtdf, const int *const *include, const dsf_outputs *out)
+{
+    if (!structures || n < 1 || !dtdf || !out || !structures[0]) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = structures[0]->eng;
+    std::vector<HostCall> hc(n);
+    std::vector<dsf_outputs> d(n);
+    std::vector<const double *> g(n);
+    for (int i = 0; i < n; i++) {
+        if (!structures[i] || structures[i]->eng != e)
+            return fail(e, DSF_ERR_ARGUMENT, "batch structures must belong to one engine");
+        int rc = host_stage(structures[i], nullptr, nullptr, nullptr, dtdf[i], include ? include[i] : nullptr,
+                            &out[i], hc[i]);
+        if (rc) return rc;
+        d[i] = hc[i].d;
+        g[i] = structures[i]->d_dtdf.as<double>();
+    }
+    int rc = dsf_calculate_batch_device(structures, n, precision, flags, g.data(), d.data(), e->stream);
+    if (rc) return rc;
+    for (int i = 0; i < n; i++)
+        if ((rc = host_readback(structures[i], flags, hc[i]))) return rc;
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    for (int i = 0; i < n; i++)
+        if ((rc = host_finish(structures[i], flags, hc[i], &out[i]))) return rc;
     return DSF_OK;
 }
 

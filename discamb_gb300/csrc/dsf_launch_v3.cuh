@@ -1,55 +1,73 @@
-// Launch helpers of sf_grad_kernel3: one instantiation per (precision, model,
-// multipole adjoint, ADP kind, symmetry-operation count); counts other than the
-// compiled ones use the runtime loop.  The instantiations are spread over
-// three translation units so they compile in parallel.
+// Launch helpers of sf_grad_kernel3 / sf_grad_batch3: one instantiation per
+// (precision, model, multipole adjoint, ADP kind, symmetry-operation count,
+// coset size); counts other than the compiled ones use the runtime loop.  The
+// instantiations are spread over several translation units so they compile in
+// parallel; the batched form exists for the FP32 kernels without the multipole
+// adjoint (dsf_k3b_f32.cu).
 #pragma once
 #include "dsf_sf_kernel.cuh"
 
 namespace dsf {
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
-cudaError_t launch_k3(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, int n_tiles, int n_chunks,
-                      size_t smem, cudaStream_t st)
+// everything a launch needs: one structure (S, C, L, grid n_tiles x n_chunks)
+// or a batch (B, grid of `blocks`)
+struct K3Args {
+    const DevStructure *S = nullptr;
+    const CallBuffers *C = nullptr;
+    const SfLaunch *L = nullptr;
+    const SignTable *G = nullptr;
+    const SfBatch *B = nullptr;
+    int n_sym = 0, coset = 0;
+    int n_tiles = 0, n_chunks = 0, blocks = 0;
+    size_t smem = 0;
+    cudaStream_t st = nullptr;
+};
+
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+cudaError_t launch_k3(const K3Args &A)
 {
-    auto k = sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    k<<<dim3(n_tiles, n_chunks), kTileAtoms, smem, st>>>(S, C, L);
+    if constexpr (BATCH) {
+        auto k = sf_grad_batch3<R, MODEL, MP, ANISO, NSC, CS>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A.smem);
+        if (e != cudaSuccess) return e;
+        k<<<A.blocks, kTileAtoms, A.smem, A.st>>>(*A.B, *A.G);
+    } else {
+        auto k = sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A.smem);
+        if (e != cudaSuccess) return e;
+        k<<<dim3(A.n_tiles, A.n_chunks), kTileAtoms, A.smem, A.st>>>(*A.S, *A.C, *A.L, *A.G);
+    }
     return cudaGetLastError();
 }
 
 // compiled operation counts first, runtime count last
-template <typename R, int MODEL, bool MP, bool ANISO>
-cudaError_t dispatch_k3(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, int n_tiles, int n_chunks,
-                        size_t smem, cudaStream_t st)
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO>
+cudaError_t dispatch_k3(const K3Args &A)
 {
-    return launch_k3<R, MODEL, MP, ANISO, 0>(S, C, L, n_tiles, n_chunks, smem, st);
+    return launch_k3<BATCH, R, MODEL, MP, ANISO, 0>(A);
 }
 
-template <typename R, int MODEL, bool MP, bool ANISO, int N0, int... NS>
-cudaError_t dispatch_k3(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, int n_tiles, int n_chunks,
-                        size_t smem, cudaStream_t st)
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, int N0, int... NS>
+cudaError_t dispatch_k3(const K3Args &A)
 {
-    if (S.n_sym == N0) return launch_k3<R, MODEL, MP, ANISO, N0>(S, C, L, n_tiles, n_chunks, smem, st);
-    return dispatch_k3<R, MODEL, MP, ANISO, NS...>(S, C, L, n_tiles, n_chunks, smem, st);
+    if (A.n_sym == N0) return launch_k3<BATCH, R, MODEL, MP, ANISO, N0>(A);
+    return dispatch_k3<BATCH, R, MODEL, MP, ANISO, NS...>(A);
 }
 
 // HC, operations in sign-diagonal cosets: the class-sum kernels of the
 // compiled (operation count, coset size) pairs; the engine sets L.coset only
 // for those pairs (coset_form_compiled)
-template <typename R, bool MP, bool ANISO>
-cudaError_t dispatch_coset(const DevStructure &, const CallBuffers &, const SfLaunch &, int, int, size_t, cudaStream_t)
+template <bool BATCH, typename R, bool MP, bool ANISO>
+cudaError_t dispatch_coset(const K3Args &)
 {
     return cudaErrorInvalidValue;
 }
 
-template <typename R, bool MP, bool ANISO, int N0, int CS0, int... NC>
-cudaError_t dispatch_coset(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, int n_tiles, int n_chunks,
-                           size_t smem, cudaStream_t st)
+template <bool BATCH, typename R, bool MP, bool ANISO, int N0, int CS0, int... NC>
+cudaError_t dispatch_coset(const K3Args &A)
 {
-    if (S.n_sym == N0 && L.coset == CS0)
-        return launch_k3<R, MODEL_HC, MP, ANISO, N0, CS0>(S, C, L, n_tiles, n_chunks, smem, st);
-    return dispatch_coset<R, MP, ANISO, NC...>(S, C, L, n_tiles, n_chunks, smem, st);
+    if (A.n_sym == N0 && A.coset == CS0) return launch_k3<BATCH, R, MODEL_HC, MP, ANISO, N0, CS0>(A);
+    return dispatch_coset<BATCH, R, MP, ANISO, NC...>(A);
 }
 
 // (operation count, coset size) pairs with compiled class-sum kernels
@@ -59,13 +77,11 @@ __host__ inline bool coset_form_compiled(bool fp64, int n_sym, int cs)
     return (n_sym == 2 && cs == 2) || (n_sym == 4 && (cs == 4 || cs == 2)) || (n_sym == 8 && (cs == 8 || cs == 4));
 }
 
-cudaError_t launch_k3_f32_hc(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool mp, bool aniso,
-                             int n_tiles, int n_chunks, size_t smem, cudaStream_t st);
-cudaError_t launch_k3_f32_hc_mp(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool aniso,
-                                int n_tiles, int n_chunks, size_t smem, cudaStream_t st);
-cudaError_t launch_k3_f32_other(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool aniso,
-                                int n_tiles, int n_chunks, size_t smem, cudaStream_t st);
-cudaError_t launch_k3_f64(const DevStructure &S, const CallBuffers &C, const SfLaunch &L, bool mp, bool aniso,
-                          int n_tiles, int n_chunks, size_t smem, cudaStream_t st);
+// per-translation-unit entries (model, multipole adjoint and ADP kind resolved at run time)
+cudaError_t launch_k3_f32_hc(const K3Args &A, bool mp, bool aniso);
+cudaError_t launch_k3_f32_hc_mp(const K3Args &A, bool aniso);
+cudaError_t launch_k3_f32_other(const K3Args &A, int model, bool aniso);
+cudaError_t launch_k3_f64(const K3Args &A, int model, bool mp, bool aniso);
+cudaError_t launch_k3b_f32(const K3Args &A, int model, bool aniso);
 
 }  // namespace dsf

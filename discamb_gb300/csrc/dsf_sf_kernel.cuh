@@ -166,14 +166,33 @@ struct SfLaunch {
     const int *cont;       // [n_hkl_pad] 1: reflection = previous one + (0,0,1) (reflections in line order)
     const int *tile_lmax;  // [n_tiles] highest l of the angular sums of the tile's atoms
     int *error;            // set to 1 on a timed-out wait
-    // operations in cosets of CS: within a coset the operations differ by a
-    // sign-diagonal Cartesian map diag(+-1, +-1, +-1) of the reciprocal vector;
-    // sgn[s][c] is the sign operation s gives the harmonics of parity class
-    // c = px + 2 py + 4 pz (parities of the harmonic in x, y, z), relative to
-    // the first operation of its coset
     int coset;             // size of the sign-diagonal cosets the operations are ordered in (0: none)
-    float sgn_f[8][8];
-    double sgn_d[8][8];
+};
+
+// Operations in cosets of CS: within a coset the operations differ by a
+// sign-diagonal Cartesian map diag(+-1, +-1, +-1) of the reciprocal vector.
+// f[s][c] (d[s][c]) is the sign operation s gives the harmonics of parity
+// class c = px + 2 py + 4 pz (parities of the harmonic in x, y, z), relative to
+// the first operation of its coset.  A kernel parameter of its own: the hot
+// loop reads it as immediate constant-bank operands.
+struct SignTable {
+    float f[8][8];
+    double d[8][8];
+};
+
+// structures of one batched launch (sf_grad_batch3): kernel-parameter space
+// holds up to kBatchItems (structure, ADP kind) items
+constexpr int kBatchItems = 48;
+struct SfBatchItem {
+    DevStructure S;
+    CallBuffers C;
+    SfLaunch L;
+    int n_tiles;  // tiles of this item (blocks = n_tiles x chunks)
+};
+struct SfBatch {
+    int n;
+    int block_begin[kBatchItems + 1];  // first block of each item; [n] = total
+    SfBatchItem item[kBatchItems];
 };
 
 // parity class (px + 2 py + 4 pz) of the 25 harmonics of harmonic_polys
@@ -263,9 +282,9 @@ struct PhaseOps<double> {
 // build up.
 constexpr int kAnchorF32 = 4;
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
-__global__ void __launch_bounds__(kTileAtoms)
-sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS>
+__device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBuffers &C, const SfLaunch &L,
+                                             const SignTable &G, const int tile_rel, const int chunk)
 {
     // CS > 0 (HC, fixed operation count, operations in sign-diagonal cosets of
     // CS): the angular sums are formed once per (atom, reflection, coset) by
@@ -286,8 +305,8 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nS = NSC > 0 ? NSC : S.n_sym;
     const int ht = L.ht;
-    const int tile = L.tile_offset + blockIdx.x;
-    const int h_begin = blockIdx.y * L.hkl_chunk;
+    const int tile = L.tile_offset + tile_rel;
+    const int h_begin = chunk * L.hkl_chunk;
     const int h_end = min(S.n_hkl, h_begin + L.hkl_chunk);
     if (h_begin >= h_end) return;
     const int a_begin = S.tile_begin[tile], a_end = S.tile_begin[tile + 1];
@@ -557,7 +576,7 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                             }
                         } else if constexpr (DIAG && MP) {
                             const auto sg = [&](int c) -> R {
-                                if constexpr (F32) return L.sgn_f[s][c]; else return L.sgn_d[s][c];
+                                if constexpr (F32) return G.f[s][c]; else return G.d[s][c];
                             };
                             A0 = Acl[0];
                             A1 = sg(2) * Acl[1] + sg(4) * Acl[2] + sg(1) * Acl[3];
@@ -571,13 +590,13 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                         } else if constexpr (DIAG) {
                             // fsph rides in the class-0 sums (sign +1 for every operation)
                             if constexpr (F32) {
-                                fre = Ec[0] + L.sgn_f[s][3] * Ec[1] + L.sgn_f[s][6] * Ec[2] + L.sgn_f[s][5] * Ec[3];
-                                fim = fsim + L.sgn_f[s][2] * Oc[0] + L.sgn_f[s][4] * Oc[1] + L.sgn_f[s][1] * Oc[2] +
-                                      L.sgn_f[s][7] * Oc[3];
+                                fre = Ec[0] + G.f[s][3] * Ec[1] + G.f[s][6] * Ec[2] + G.f[s][5] * Ec[3];
+                                fim = fsim + G.f[s][2] * Oc[0] + G.f[s][4] * Oc[1] + G.f[s][1] * Oc[2] +
+                                      G.f[s][7] * Oc[3];
                             } else {
-                                fre = Ec[0] + L.sgn_d[s][3] * Ec[1] + L.sgn_d[s][6] * Ec[2] + L.sgn_d[s][5] * Ec[3];
-                                fim = fsim + L.sgn_d[s][2] * Oc[0] + L.sgn_d[s][4] * Oc[1] + L.sgn_d[s][1] * Oc[2] +
-                                      L.sgn_d[s][7] * Oc[3];
+                                fre = Ec[0] + G.d[s][3] * Ec[1] + G.d[s][6] * Ec[2] + G.d[s][5] * Ec[3];
+                                fim = fsim + G.d[s][2] * Oc[0] + G.d[s][4] * Oc[1] + G.d[s][1] * Oc[2] +
+                                      G.d[s][7] * Oc[3];
                             }
                         } else if constexpr (HC) {
                             A0 = pg[0] * y[0];
@@ -617,8 +636,8 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
                                 QC[0] += q0;
 #pragma unroll
                                 for (int k = 1; k < 16; k++) {
-                                    if constexpr (F32) QC[k] += L.sgn_f[s][slot_class(k)] * ql[slot_l(k)];
-                                    else QC[k] += L.sgn_d[s][slot_class(k)] * ql[slot_l(k)];
+                                    if constexpr (F32) QC[k] += G.f[s][slot_class(k)] * ql[slot_l(k)];
+                                    else QC[k] += G.d[s][slot_class(k)] * ql[slot_l(k)];
                                 }
                             } else {
                                 part[CH_PLM] += q0 * y[0];
@@ -748,6 +767,32 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L)
             for (int q = CH_PV; q < NT; q++) atomicAdd(G + q, total(q));
         }
     }
+}
+
+// one structure: block (tile, reflection chunk)
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+__global__ void __launch_bounds__(kTileAtoms)
+sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
+{
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(S, C, L, G, blockIdx.x, blockIdx.y);
+}
+
+// many structures of one kernel shape (and one sign table) in one launch: the
+// block's item is the last with block_begin <= blockIdx.x
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+__global__ void __launch_bounds__(kTileAtoms)
+sf_grad_batch3(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
+{
+    const int b = blockIdx.x;
+    int lo = 0, hi = B.n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (B.block_begin[mid] <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const SfBatchItem &it = B.item[lo];
+    const int lb = b - B.block_begin[lo];
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(it.S, it.C, it.L, G, lb % it.n_tiles, lb / it.n_tiles);
 }
 
 }  // namespace dsf

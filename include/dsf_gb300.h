@@ -185,6 +185,16 @@ int dsf_calculate_atoms(dsf_structure *s, int precision, int derivative_flags, c
 /* device buffers, asynchronous on `stream` (cudaStream_t, NULL = engine stream) */
 int dsf_calculate_device(dsf_structure *s, int precision, int derivative_flags, const double *dtdf_device,
                          const dsf_outputs *out_device, void *stream);
+/* n structures of one engine in one submission (device buffers per structure, asynchronous on `stream`): the
+ * FP32 structure-factor kernels of structures without the multipole adjoint run as batched launches, one per
+ * kernel shape.  The same results as n dsf_calculate_device calls; the reference has no batched call (one
+ * calculator per structure, SfCalculator.h:45-67, called in turn by its callers). */
+int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int precision, int derivative_flags,
+                               const double *const *dtdf_device, const dsf_outputs *out_device, void *stream);
+/* the same with host buffers (dtdf[i] [n_hkl_i][2], include[i] NULL = all atoms, outputs on the host); one
+ * stream synchronisation for the whole batch */
+int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int derivative_flags,
+                        const double *const *dtdf, const int *const *include, const dsf_outputs *out);
 
 /* number of kernel launches issued by the last calculation (for accounting) */
 int dsf_last_launch_count(const dsf_structure *s);

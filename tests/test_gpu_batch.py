@@ -1,0 +1,128 @@
+"""Batched submission (dsf_calculate_batch / dsf_calculate_batch_device):
+many structures of one engine give the same results as one call each.
+
+FP64: equal to the single calls up to the order of the FP64 atomic sums.
+FP32: the batch chooses its own reflection chunks (and so its own line
+re-anchoring points), so it is compared with the oracle at the FP32 bar
+(sum|dF|/sum|F| <= 1e-6, per-class derivative norm error <= 1e-5)."""
+import numpy as np
+import pytest
+
+from conftest import rel_f, rel_norm
+from discamb_gb300 import api, workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FP64, FP32 = api.DSF_FP64, api.DSF_FP32_BULK
+
+
+def mixed_set():
+    """HC structures of every kernel shape (operation count, coset form,
+    ADP kind), an IAM and a tabulated structure."""
+    cases = []
+    for i, sg in enumerate(["P1", "P-1", "P21", "P21/c", "P212121", "C2/c", "P41", "P43212", "Pbca"]):
+        cases.append(("hc", W.small_case(sg, n_atoms=5 + i, stol_max=0.5, seed=300 + i, aniso=bool(i % 2))))
+    return cases
+
+
+def iam_case():
+    st = W.small_case("P21/c", n_atoms=7, stol_max=0.5, seed=351)
+    ntype = int(st.atom_type.max()) + 1
+    rng = np.random.default_rng(5)
+    iam = dict(ngauss=np.full(ntype, 4, np.int32), a=rng.uniform(0.5, 3, (ntype, 5)),
+               b=rng.uniform(0.5, 30, (ntype, 5)), c=rng.uniform(0, 0.5, ntype))
+    return st, iam
+
+
+def table_case():
+    st = W.small_case("P212121", n_atoms=6, stol_max=0.45, seed=352)
+    rot, _ = api.all_ops_mod_centering(st.sg)
+    rng = np.random.default_rng(6)
+    t = rng.normal(size=(st.n_hkl, len(rot), st.n_atoms)) + 1j * rng.normal(size=(st.n_hkl, len(rot), st.n_atoms))
+    return st, t
+
+
+def make_calcs(engine):
+    calcs, oracles = [], []
+    for kind, st in mixed_set():
+        calcs.append(api.HcCalculator(engine, st))
+        oracles.append(lambda st=st, mp=False: O.compute(st, multipoles=mp))
+    st, iam = iam_case()
+    calcs.append(api.IamCalculator(engine, st, iam))
+    oracles.append(lambda st=st, iam=iam, mp=False: O.compute(st, model="iam", iam=iam))
+    st, t = table_case()
+    calcs.append(api.TabulatedCalculator(engine, st, t))
+    oracles.append(lambda st=st, t=t, mp=False: O.compute(st, model="table", table=t))
+    return calcs, oracles
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_batch_matches_single_calls(engine, prec):
+    calcs, oracles = make_calcs(engine)
+    dtdfs = [c.st.dtdf for c in calcs]
+    batch = engine.calculate_batch(calcs, dtdfs, precision=prec)
+    for c, o, b in zip(calcs, oracles, batch):
+        if prec == FP64:
+            a = c.calculate(c.st.dtdf, precision=prec, adp_layout="padded")
+            assert rel_f(b["f"], a["f"]) < 1e-12
+            for k in ("d_xyz", "d_adp", "d_occ"):
+                assert rel_norm(b[k], a[k]) < 1e-12, k
+        else:
+            ref = o()
+            nadp = c.st.n_adp()
+            adp = [b["d_adp"][i, :nadp[i]] for i in range(c.n_atoms)]
+            assert rel_f(b["f"], ref["f"]) < 1e-6
+            assert rel_norm(b["d_xyz"], ref["d_xyz"]) < 1e-5
+            assert rel_norm(adp, ref["d_adp"]) < 1e-5
+            assert rel_norm(b["d_occ"], ref["d_occ"]) < 1e-5
+    for c in calcs:
+        c.close()
+
+
+def test_batch_with_multipole_adjoint_and_repeats(engine):
+    # HC structures with the multipole adjoint launch per structure inside the batch
+    sts = [W.small_case(sg, n_atoms=6, stol_max=0.5, seed=360 + i) for i, sg in enumerate(["P21/c", "P212121", "P1"])]
+    calcs = [api.HcCalculator(engine, st) for st in sts]
+    for rep in range(2):
+        batch = engine.calculate_batch(calcs, [st.dtdf for st in sts], precision=FP32, multipoles=True)
+        for st, b in zip(sts, batch):
+            o = O.compute(st, multipoles=True)
+            assert rel_f(b["f"], o["f"]) < 1e-6
+            for k in ("d_pval", "d_plm", "d_kappa", "d_kappa_p"):
+                assert rel_norm(b[k], o[k]) < 1e-5, k
+    for c in calcs:
+        c.close()
+
+
+def test_batch_larger_than_one_launch(engine):
+    # more structures of one kernel shape than one batched launch holds (48)
+    sts = [W.small_case("P21/c", n_atoms=3, stol_max=0.3, seed=400 + i) for i in range(53)]
+    calcs = [api.HcCalculator(engine, st) for st in sts]
+    batch = engine.calculate_batch(calcs, [st.dtdf for st in sts], precision=FP64)
+    for c, st, b in zip(calcs, sts, batch):
+        a = c.calculate(st.dtdf, precision=FP64)
+        assert rel_f(b["f"], a["f"]) < 1e-12
+        assert rel_norm(b["d_xyz"], a["d_xyz"]) < 1e-12
+    # FP32: all 53 in batched launches (two of them)
+    batch = engine.calculate_batch(calcs, [st.dtdf for st in sts], precision=FP32)
+    for st, b in zip(sts[::13], batch[::13]):
+        o = O.compute(st)
+        assert rel_f(b["f"], o["f"]) < 1e-6
+        assert rel_norm(b["d_xyz"], o["d_xyz"]) < 1e-5
+    for c in calcs:
+        c.close()
+
+
+def test_batch_rejects_foreign_structures(engine):
+    st = W.small_case("P21", n_atoms=3, stol_max=0.3, seed=450)
+    other = api.Engine(0)
+    try:
+        a = api.HcCalculator(engine, st)
+        b = api.HcCalculator(other, st)
+        with pytest.raises(api.DsfError):
+            engine.calculate_batch([a, b], [st.dtdf, st.dtdf])
+        a.close()
+        b.close()
+    finally:
+        other.close()
