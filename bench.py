@@ -49,6 +49,9 @@ WORKLOADS = {
                     traffic_key="sf_grad_kernel3<float,HC,0,ISO,4>@config1",
                     desc="config1: HC multipoles l<=4, 5000 atoms (150 types), P212121, 54704 hkl d>=1.5A, iso B, "
                          "dF/d(xyz,B,occ)"),
+    "config4": dict(seed=4, desc="config4: 256 crystals, P21/c, tabulated complex64 form factors per (atom, h'), "
+                                 "atoms log-uniform 10-2000, hkl log-uniform 2k-100k, aniso U (H iso), "
+                                 "dF/d(xyz,U,occ); one batched submission per step"),
     "config2": dict(seed=2, multipoles=True, flops=195, fp64_frac=0.05, cpu_frac=0.002,
                     traffic_key="sf_grad_kernel3<float,HC,MP,ANISO,8>@config2",
                     desc="config2: HC multipoles l<=4, 50000 atoms (300 types), P43212, all hkl d>=1.2A, aniso U "
@@ -180,6 +183,186 @@ def run_reference(args):
             "config": {"workload": wl["desc"], "sample": f"first {frac:.1%} of the reflections per step"},
             "cpu_baseline": {"value": value, "unit": "terms/s", "cores": threads, "kind": "port",
                              "sample": f"{args.workload} atoms x first {int(st.n_hkl * frac)} reflections per step"},
+            "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def config4_batch(args, eng, dev, api, W, torch):
+    """The config4 crystals on the device: structures created from tables
+    drawn on the device (f0 (1 + 0.05 CN(0,1)) per (h, operation, atom)),
+    plus per-crystal dT/dF and output buffers."""
+    specs = W.config4_specs(args.c4_crystals, seed=WORKLOADS["config4"]["seed"])
+    calcs, sts, dtdf, outs, tables_small = [], [], [], [], {}
+    for i, (na, nh) in enumerate(specs):
+        st = W.config4_crystal(na, nh, seed=4000 + i)
+        f0e, el = W.config4_f0_elements(st, W.config4_stol(st))
+        f0 = torch.tensor(f0e, dtype=torch.float32, device=dev)[:, torch.tensor(el, device=dev)]  # [nh, na]
+        gen = torch.Generator(device=dev)
+        gen.manual_seed(4000 + i)
+        noise = torch.randn((st.n_hkl, 4, st.n_atoms, 2), generator=gen, device=dev) * (0.05 / math.sqrt(2.0))
+        table = torch.empty_like(noise)
+        table[..., 0] = f0[:, None, :] * (1.0 + noise[..., 0])
+        table[..., 1] = f0[:, None, :] * noise[..., 1]
+        del noise
+        torch.cuda.synchronize(dev)  # the engine gathers the table on its own stream
+        calcs.append(api.TabulatedCalculator(eng, st, table_device=table.data_ptr()))
+        if st.n_atoms * st.n_hkl <= 4e6:
+            tables_small[i] = table
+        del table
+        sts.append(st)
+        dtdf.append(torch.tensor(np.stack([st.dtdf.real, st.dtdf.imag], 1), dtype=torch.float64,
+                                 device=dev).contiguous())
+        o = {"f": torch.empty(st.n_hkl, 2, dtype=torch.float64, device=dev)}
+        for k, w in (("d_xyz", 3), ("d_adp", 6), ("d_occ", 1)):
+            o[k] = torch.empty(st.n_atoms, w, dtype=torch.float64, device=dev)
+        outs.append(o)
+    return specs, calcs, sts, dtdf, outs, tables_small
+
+
+def run_config4(args):
+    import torch
+    from discamb_gb300 import api, build, workloads as W
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_config4_reference(args)
+    device = local if world > 1 else 0
+    torch.cuda.set_device(device)
+    build.build()
+    dev = torch.device("cuda", device)
+    eng = api.Engine(device)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    sptr = stream.cuda_stream
+    t_setup = time.perf_counter()
+    specs, calcs, sts, dtdf, outs, small = config4_batch(args, eng, dev, api, W, torch)
+    torch.cuda.synchronize(dev)
+    t_setup = time.perf_counter() - t_setup
+    terms = sum(st.n_atoms * 4 * st.n_hkl for st in sts)
+    table_bytes = 8 * terms
+    io_bytes = sum(32 * st.n_hkl + 8 * 10 * st.n_atoms for st in sts)  # dT/dF in, F out, per-atom outputs
+    ptrs = [d.data_ptr() for d in dtdf]
+    optrs = [{k: v.data_ptr() for k, v in o.items()} for o in outs]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        eng.calculate_batch_device(calcs, ptrs, optrs, precision=api.DSF_FP32_BULK, stream=sptr)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(device) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    launches = calcs[0].last_launch_count()
+    ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    # FP64 form of the same batch (per-structure launches)
+    ev64 = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    eng.calculate_batch_device(calcs, ptrs, optrs, precision=api.DSF_FP64, stream=sptr)
+    ev64[0].record(stream)
+    eng.calculate_batch_device(calcs, ptrs, optrs, precision=api.DSF_FP64, stream=sptr)
+    ev64[1].record(stream)
+    torch.cuda.synchronize(dev)
+    ms64 = ev64[0].elapsed_time(ev64[1])
+    # end to end: host dT/dF in, host F and derivatives out, one submission
+    hd = [st.dtdf for st in sts]
+    for _ in range(2):
+        eng.calculate_batch(calcs, hd, precision=api.DSF_FP32_BULK)
+    e2e = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        eng.calculate_batch(calcs, hd, precision=api.DSF_FP32_BULK)
+        e2e.append(time.perf_counter() - t0)
+    e2e_ms = statistics.mean(e2e) * 1e3
+    mp = measured_peaks()
+    peak = mp.get("hbm_gbs")
+    achieved = (table_bytes + io_bytes) / (ms * 1e-3) * 1e-9
+    # CPU: the generic engine with a tabulated form factor, one thread, on the small crystals
+    from oracle import oracle as O
+    t_cpu, cpu_terms, used = 0.0, 0, []
+    for i in sorted(small, key=lambda j: sts[j].n_atoms * sts[j].n_hkl):
+        st = sts[i]
+        tb = small[i].cpu().numpy()
+        t = tb[..., 0] + 1j * tb[..., 1]
+        t0 = time.perf_counter()
+        O.compute(st, model="table", table=t, n_threads=1)
+        t_cpu += time.perf_counter() - t0
+        cpu_terms += st.n_atoms * 4 * st.n_hkl
+        used.append(i)
+        if t_cpu > 10.0:
+            break
+    line = {
+        "metric": "atom*symop*hkl terms/s (SF+grad)", "value": terms / (ms * 1e-3), "unit": "terms/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk (complex64 table, f64 accumulation)",
+        "data": "synthetic (seeded; tables drawn on the device)",
+        "config": {"workload": WORKLOADS["config4"]["desc"], "crystals": len(sts), "terms_per_step": terms,
+                   "table_bytes": table_bytes, "setup_s": t_setup,
+                   "l2": "inputs larger than L2 (tables); 256 MB flush between steps"},
+        "fp64": {"value": terms / (ms64 * 1e-3), "ms_per_step": ms64, "fp32_over_fp64": ms64 / ms},
+        "e2e": {"value": terms / (e2e_ms * 1e-3), "unit": "terms/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": sum(16 * st.n_hkl for st in sts),
+                "d2h_bytes_per_step": sum(16 * st.n_hkl + 80 * st.n_atoms for st in sts)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "bytes_per_step": table_bytes + io_bytes, "timed": "whole batched step (CUDA events)"},
+        "cpu_baseline": {"value": cpu_terms / t_cpu if t_cpu else None, "unit": "terms/s", "cores": 1,
+                         "kind": "port",
+                         "sample": f"{len(used)} smallest crystals, generic engine with the table, one thread "
+                                   f"({t_cpu:.1f} s)"},
+        "gpu_launches": launches,
+        "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+        "wall_s_timed_region": wall,
+    }
+    print(json.dumps(line))
+    for c in calcs:
+        c.close()
+    eng.close()
+    return 0
+
+
+def run_config4_reference(args):
+    """The generic engine with tabulated form factors on the host, one
+    thread (the reference's tabulated path is serial), on the smallest
+    crystals of the batch, tables drawn on the host."""
+    from discamb_gb300 import workloads as W
+    from oracle import oracle as O
+    specs = W.config4_specs(args.c4_crystals, seed=WORKLOADS["config4"]["seed"])
+    order = sorted(range(len(specs)), key=lambda i: specs[i][0] * specs[i][1])
+    vals, times = [], []
+    for rep in range(args.warmup + args.steps):
+        t_cpu, terms = 0.0, 0
+        for i in order:
+            st = W.config4_crystal(*specs[i], seed=4000 + i)
+            t = W.config4_table(st, np.random.default_rng(4000 + i))
+            t0 = time.perf_counter()
+            O.compute(st, model="table", table=t, n_threads=1)
+            t_cpu += time.perf_counter() - t0
+            terms += st.n_atoms * 4 * st.n_hkl
+            if t_cpu > 3.0:
+                break
+        if rep >= args.warmup:
+            vals.append(terms / t_cpu)
+            times.append(t_cpu)
+    value = statistics.median(vals)
+    line = {"metric": "atom*symop*hkl terms/s (SF+grad)", "value": value, "unit": "terms/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(times) * 1e3,
+            "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference", "config": {"workload": WORKLOADS["config4"]["desc"],
+                                            "sample": "smallest crystals, about 3 s of work per step"},
+            "cpu_baseline": {"value": value, "unit": "terms/s", "cores": 1, "kind": "port",
+                             "sample": "smallest crystals of the batch, one thread"},
             "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -339,11 +522,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS))
+    ap.add_argument("--c4-crystals", type=int, default=256)
     ap.add_argument("--cpu-sample", type=float, default=0.25)
     ap.add_argument("--reference-sample", type=float, default=0.1)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload == "config4":
+        return run_config4(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -94,6 +94,8 @@ def library():
         L.dsf_structure_create_iam.argtypes = [C.c_void_p, _P(_Sym), _P(_Iam), _P(_Atoms), _P(C.c_void_p)]
         L.dsf_structure_create_tabulated.argtypes = [C.c_void_p, _P(_Sym), _P(_Atoms), C.c_int, _P(C.c_int),
                                                      _P(C.c_double), C.c_int, _P(C.c_void_p)]
+        L.dsf_structure_create_tabulated_device.argtypes = [C.c_void_p, _P(_Sym), _P(_Atoms), C.c_int, _P(C.c_int),
+                                                            C.c_void_p, C.c_int, _P(C.c_void_p)]
         L.dsf_structure_destroy.argtypes = [C.c_void_p]
         L.dsf_structure_set_hkl.argtypes = [C.c_void_p, C.c_int, _P(C.c_int)]
         L.dsf_structure_update_atoms.argtypes = [C.c_void_p, _P(C.c_double), _P(C.c_double), _P(C.c_double)]
@@ -468,16 +470,24 @@ class TabulatedCalculator(_Calculator):
     """Tabulated complex form factors per (reflection, operation, atom) over
     all operations modulo centering."""
 
-    def __init__(self, engine, st, table, fp32_table=False):
+    def __init__(self, engine, st, table=None, fp32_table=False, table_device=None, table_device_fp64=False):
+        """table: host complex [n_hkl][n_ops][n_atoms]; or table_device: a
+        device pointer to the same layout (complex64, or complex128 with
+        table_device_fp64), gathered on the device (FP32 table)."""
         super().__init__(engine, st)
         sym, k1 = symmetry_desc(st, "all")
         atoms, k3 = _atoms_desc(st, lcs=False)
-        t = np.asarray(table)
-        tt = np.ascontiguousarray(np.stack([t.real, t.imag], -1).reshape(-1), dtype=np.float64)
         x, p = _i(np.asarray(st.hkl).reshape(-1))
-        engine.check(self.lib.dsf_structure_create_tabulated(engine.h, C.byref(sym), C.byref(atoms), len(st.hkl), p,
-                                                             tt.ctypes.data_as(_P(C.c_double)), int(fp32_table),
-                                                             C.byref(self.h)), "create_tabulated")
+        if table_device is not None:
+            engine.check(self.lib.dsf_structure_create_tabulated_device(
+                engine.h, C.byref(sym), C.byref(atoms), len(st.hkl), p, C.c_void_p(int(table_device)),
+                int(table_device_fp64), C.byref(self.h)), "create_tabulated_device")
+        else:
+            t = np.asarray(table)
+            tt = np.ascontiguousarray(np.stack([t.real, t.imag], -1).reshape(-1), dtype=np.float64)
+            engine.check(self.lib.dsf_structure_create_tabulated(engine.h, C.byref(sym), C.byref(atoms), len(st.hkl),
+                                                                 p, tt.ctypes.data_as(_P(C.c_double)),
+                                                                 int(fp32_table), C.byref(self.h)), "create_tabulated")
         self.n_hkl = len(st.hkl)
         self.update_atoms(st.xyz, st.adp, st.occupancy)
 

@@ -75,8 +75,10 @@ struct DevStructure {
     const int4 *hkl;             // [n_hkl] (h,k,l,0)
     const double *h2;            // |h_cart|^2
     const float *h2f;
-    const float2 *table_f;       // tabulated model: [n_hkl][n_sym][n_atoms]
+    const float2 *table_f;       // tabulated model: [n_hkl_pad][n_sym][table_stride]
     const double2 *table_d;
+    int table_stride;            // columns per (reflection, operation) row: even
+    int table_split, table_shift;  // column of sorted atom a: a + (a >= split ? shift : 0) (even tile starts)
     const int *atom_orig;        // sorted -> original atom index
     const int *atom_plm_lmax;    // highest l of the atom's P_lm parameters (-1: none)
 };

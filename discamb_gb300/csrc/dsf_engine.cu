@@ -33,7 +33,7 @@ cudaError_t launch_rs_prep(const DevStructure &S, int n_hkl_pad, void *rs_f, voi
 cudaError_t launch_tr_prep(const DevStructure &S, int n_hkl_pad, void *tr_f, void *tr_d, void *trm_f, void *trm_d,
                            bool mp, cudaStream_t st);
 size_t rs_record_bytes(bool fp64);
-size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types);
+size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types, bool table);
 cudaError_t launch_sf3(const K3Args &A, int model, bool fp64, bool mp, bool aniso);
 cudaError_t launch_sf_grad(const DevStructure &S, const CallBuffers &C, bool fp64, bool mp, int hkl_chunk, int ht,
                            cudaStream_t st);
@@ -184,6 +184,9 @@ struct dsf_structure {
     // vector; sym_sign: that map's signs relative to the coset's first operation
     int coset_size = 0;
     std::vector<int> sym_sign;  // [n_sym][3]
+    // tabulated model: column of sorted atom a = a + (a >= table_split ? table_shift : 0), table_stride
+    // columns per row (even), so every tile's columns start on a 16-byte boundary
+    int table_stride = 0, table_split = 0, table_shift = 0;
     std::vector<int> perm;  // sorted -> original
     std::vector<int> tile_begin, tile_ntypes, tile_types;
     // host model copies
@@ -882,6 +885,9 @@ void refresh_dev(dsf_structure *s)
     d.h2f = s->d_h2f.as<float>();
     d.table_f = s->d_table_f.as<float2>();
     d.table_d = s->d_table_d.as<double2>();
+    d.table_stride = s->table_stride;
+    d.table_split = s->table_split;
+    d.table_shift = s->table_shift;
     d.atom_orig = s->d_perm.as<int>();
     d.atom_plm_lmax = s->d_plm_lmax.as<int>();
 }
@@ -1149,6 +1155,24 @@ int dsf_structure_create_iam(dsf_engine *e, const dsf_symmetry *sym, const dsf_i
 
 int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl);
 
+// column layout of the tabulated model (see dsf_structure::table_stride)
+static void table_columns(dsf_structure *s)
+{
+    int n_plain = 0;
+    while (n_plain < s->n_atoms && s->adpk[s->perm[n_plain]] != 6) n_plain++;
+    s->table_split = n_plain;
+    s->table_shift = n_plain % 2;
+    s->table_stride = (s->n_atoms + s->table_shift + 1) / 2 * 2;
+}
+
+// column c -> sorted atom index, or -1 for a padding column
+__host__ __device__ inline int table_column_atom(int c, int split, int shift, int n_atoms)
+{
+    if (c < split) return c;
+    const int a = c - shift;
+    return (a >= split && a < n_atoms) ? a : -1;
+}
+
 int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms, int n_hkl,
                                    const int *hkl, const double *table, int table_fp32, dsf_structure **out)
 {
@@ -1182,21 +1206,112 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
             if (hkl[3 * x + j] != hkl[3 * y + j]) return hkl[3 * x + j] < hkl[3 * y + j];
         return false;
     });
-    const size_t row = (size_t)s->n_sym * s->n_atoms;  // complex values per reflection
+    // columns in the engine's (sorted) atom order, padded so every tile starts on a 16-byte boundary
+    table_columns(s);
+    const int nA = s->n_atoms, nS = s->n_sym, stride = s->table_stride;
+    const size_t row = (size_t)nS * stride;  // complex values per reflection
     std::vector<float> tf(2 * row * n_pad, 0.0f);
+    std::vector<double> td(table_fp32 ? 0 : 2 * row * n_pad, 0.0);
     for (int i = 0; i < n_hkl; i++)
-        for (size_t q = 0; q < 2 * row; q++) tf[2 * row * i + q] = (float)table[2 * row * order[i] + q];
+        for (int op = 0; op < nS; op++)
+            for (int c = 0; c < stride; c++) {
+                const int a = table_column_atom(c, s->table_split, s->table_shift, nA);
+                if (a < 0) continue;
+                const size_t j = 2 * (((size_t)order[i] * nS + op) * nA + s->perm[a]);
+                const size_t k = 2 * (row * i + (size_t)op * stride + c);
+                tf[k] = (float)table[j];
+                tf[k + 1] = (float)table[j + 1];
+                if (!table_fp32) {
+                    td[k] = table[j];
+                    td[k + 1] = table[j + 1];
+                }
+            }
     if ((rc = upload(e, s->d_table_f, tf.data(), tf.size()))) return bail(rc);
-    if (!table_fp32) {
-        std::vector<double> td(2 * row * n_pad, 0.0);
-        for (int i = 0; i < n_hkl; i++)
-            for (size_t q = 0; q < 2 * row; q++) td[2 * row * i + q] = table[2 * row * order[i] + q];
-        if ((rc = upload(e, s->d_table_d, td.data(), td.size()))) return bail(rc);
-    } else {
-        // the plain form reads the FP32 values widened
-        std::vector<double> td(tf.begin(), tf.end());
-        if ((rc = upload(e, s->d_table_d, td.data(), td.size()))) return bail(rc);
+    // an FP32 table is read widened by the plain form (no FP64 copy)
+    if (!table_fp32 && (rc = upload(e, s->d_table_d, td.data(), td.size()))) return bail(rc);
+    if ((rc = finish_create(e, s))) return bail(rc);
+    s->eng->live_structures++;
+    if ((rc = dsf_structure_set_hkl(s, n_hkl, hkl))) { s->eng->live_structures--; return bail(rc); }
+    *out = s;
+    return DSF_OK;
+}
+
+// gathers a caller's [n_hkl][n_sym][n_atoms] complex table (complex64 or
+// complex128, the caller's reflection and atom order) into the engine's
+// line-ordered, padded complex64 table with columns in the engine's atom
+// order; rows past n_hkl are zero
+__global__ void table_gather_kernel(int n_pad, int n_hkl, int n_sym, int n_atoms, int stride, int split, int shift,
+                                    const int *order, const int *perm, const void *src, int src_fp64, float2 *dst)
+{
+    const size_t row = (size_t)n_sym * stride, total = (size_t)n_pad * row;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t r = i / row, q = i - r * row;
+        const int op = (int)(q / stride), c = (int)(q - (size_t)op * stride);
+        const int a = table_column_atom(c, split, shift, n_atoms);
+        float2 v = make_float2(0.f, 0.f);
+        if (r < (size_t)n_hkl && a >= 0) {
+            const size_t j = ((size_t)order[r] * n_sym + op) * n_atoms + perm[a];
+            if (src_fp64) {
+                const double2 d = reinterpret_cast<const double2 *>(src)[j];
+                v = make_float2((float)d.x, (float)d.y);
+            } else {
+                v = reinterpret_cast<const float2 *>(src)[j];
+            }
+        }
+        dst[i] = v;
     }
+}
+
+int dsf_structure_create_tabulated_device(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms, int n_hkl,
+                                          const int *hkl, const void *table_device, int table_fp64,
+                                          dsf_structure **out)
+{
+    dsf_structure *s = nullptr;
+    int rc = create_common(e, sym, atoms, MODEL_TABLE, out, &s);
+    if (rc) return rc;
+    auto bail = [&](int code) { delete s; return code; };
+    if (!table_device || n_hkl < 1 || !hkl)
+        return bail(fail(e, DSF_ERR_ARGUMENT, "tabulated model needs a table and reflections"));
+    s->n_types = 1;
+    s->trad.assign(1, TypeHost{});
+    s->trad[0].lmax_used = -1;
+    if ((rc = build_tiles(s, false))) return bail(rc);
+    std::vector<double> z(25 * (size_t)s->n_atoms, 0.0);
+    std::vector<float> zf(25 * (size_t)s->n_atoms, 0.0f);
+    if ((rc = upload(e, s->d_pg_d, z.data(), z.size()))) return bail(rc);
+    if ((rc = upload(e, s->d_pg_f, zf.data(), zf.size()))) return bail(rc);
+    s->dmat.assign(165 * (size_t)s->n_atoms, 0.0);
+    if ((rc = upload(e, s->d_dmat, s->dmat.data(), s->dmat.size()))) return bail(rc);
+    {
+        std::vector<int> lmx(s->n_atoms, -1), tl(s->n_tiles, -1);
+        if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return bail(rc);
+        if ((rc = upload(e, s->d_tile_lmax, tl.data(), tl.size()))) return bail(rc);
+    }
+    // the engine's line order, as dsf_structure_set_hkl orders the reflections
+    const int n_pad = (n_hkl + kMaxHT - 1) / kMaxHT * kMaxHT;
+    std::vector<int> order(n_hkl);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        for (int j = 0; j < 3; j++)
+            if (hkl[3 * x + j] != hkl[3 * y + j]) return hkl[3 * x + j] < hkl[3 * y + j];
+        return false;
+    });
+    DevBuf d_order;
+    if ((rc = upload(e, d_order, order.data(), order.size()))) return bail(rc);
+    table_columns(s);
+    const size_t row = (size_t)s->n_sym * s->table_stride;
+    cudaError_t ce = s->d_table_f.alloc(sizeof(float2) * row * n_pad);
+    if (ce != cudaSuccess) {
+        d_order.release();
+        return bail(fail(e, DSF_ERR_MEMORY, "table allocation failed"));
+    }
+    table_gather_kernel<<<std::max(1, e->n_sm) * 8, 256, 0, e->stream>>>(
+        n_pad, n_hkl, s->n_sym, s->n_atoms, s->table_stride, s->table_split, s->table_shift, d_order.as<int>(),
+        s->d_perm.as<int>(), table_device, table_fp64, s->d_table_f.as<float2>());
+    ce = cudaGetLastError();
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    d_order.release();
+    if (ce != cudaSuccess) return bail(fail(e, DSF_ERR_CUDA, cudaGetErrorString(ce)));
     if ((rc = finish_create(e, s))) return bail(rc);
     s->eng->live_structures++;
     if ((rc = dsf_structure_set_hkl(s, n_hkl, hkl))) { s->eng->live_structures--; return bail(rc); }
@@ -1489,9 +1604,12 @@ static int kind_shape(dsf_structure *s, int kind, bool fp64, bool mp, double blo
     L.tile_offset = t0;
     L.max_types = kind ? s->max_types_aniso : s->max_types_plain;
     int ht = kMaxHT;
-    const size_t budget = std::min<size_t>(e->max_smem, fp64 ? 200 * 1024 : 100 * 1024);
-    while (ht > 4 && sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types) > budget) ht /= 2;
-    smem = sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types);
+    size_t budget = std::min<size_t>(e->max_smem, fp64 ? 200 * 1024 : 100 * 1024);
+    const bool table = s->model == MODEL_TABLE;
+    // the staged FP32 table dominates the stage: a smaller budget keeps four blocks per SM
+    if (table && !fp64) budget = std::min<size_t>(budget, 64 * 1024);
+    while (ht > 4 && sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types, table) > budget) ht /= 2;
+    smem = sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types, table);
     if (smem > e->max_smem) return fail(e, DSF_ERR_UNSUPPORTED, "shared-memory tile does not fit this device");
     L.ht = ht;
     int chunk = (int)std::min<double>(s->n_hkl, std::max(1.0, block_terms / kTileAtoms));
@@ -1609,11 +1727,9 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
         if ((rc = call_pre(structures[i], dtdf_device[i], st))) return rc;
         launches++;
     }
-    // work per block so that the whole batch covers the SMs about eight times
-    double total = 0;
-    for (int i = 0; i < n; i++) total += (double)structures[i]->n_atoms * structures[i]->n_hkl;
-    const double block_terms = std::max<double>(kTileAtoms * 64.0, total / (std::max(1, e->n_sm) * 8.0));
-    // group the batched items by kernel shape and sign table
+    // group the batched items by kernel shape and sign table; the reflection
+    // chunks are chosen per launch (below) so that each launch covers the SMs
+    // about eight times
     struct Group {
         int model, aniso, n_sym, coset;
         SignTable G;
@@ -1631,7 +1747,11 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
         for (int kind = 0; kind < 2; kind++) {
             int nt, n_chunks;
             size_t smem;
-            if ((rc = kind_shape(s, kind, fp64, mp, block_terms, L, nt, n_chunks, smem))) return rc;
+            // per-structure launches size their chunks as dsf_calculate_device does
+            const int ntk = kind ? s->n_tiles - s->n_tiles_plain : s->n_tiles_plain;
+            const int n_chunks0 = std::max(1, std::max(1, e->n_sm) * 8 / std::max(1, ntk));
+            const double own_terms = (double)kTileAtoms * ((s->n_hkl + n_chunks0 - 1) / n_chunks0);
+            if ((rc = kind_shape(s, kind, fp64, mp, own_terms, L, nt, n_chunks, smem))) return rc;
             if (nt <= 0) continue;
             if (fp64 || mp) {  // per-structure launch
                 K3Args A;
@@ -1681,13 +1801,24 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
         for (size_t b0 = 0; b0 < g.items.size(); b0 += kBatchItems) {
             const int m = (int)std::min<size_t>(kBatchItems, g.items.size() - b0);
             B.n = m;
+            // atom x reflection pairs per block for this launch: about eight blocks per SM
+            double pairs = 0;
+            for (int k = 0; k < m; k++) {
+                const SfBatchItem &it = g.items[b0 + k];
+                pairs += (double)it.n_tiles * kTileAtoms * it.S.n_hkl;
+            }
+            const double block_terms = std::max<double>(kTileAtoms * 64.0, pairs / (std::max(1, e->n_sm) * 8.0));
             int blocks = 0;
             for (int k = 0; k < m; k++) {
                 B.item[k] = g.items[b0 + k];
+                SfLaunch &L = B.item[k].L;
+                const int n_hkl = B.item[k].S.n_hkl, ht = L.ht;
+                int chunk = (int)std::min<double>(n_hkl, std::max(1.0, block_terms / kTileAtoms));
+                chunk = std::max(chunk, 4 * ht);
+                chunk = (chunk + ht - 1) / ht * ht;
+                L.hkl_chunk = chunk;
                 B.block_begin[k] = blocks;
-                const SfLaunch &L = B.item[k].L;
-                const int n_chunks = (B.item[k].S.n_hkl + L.hkl_chunk - 1) / L.hkl_chunk;
-                blocks += B.item[k].n_tiles * n_chunks;
+                blocks += B.item[k].n_tiles * ((n_hkl + chunk - 1) / chunk);
             }
             B.block_begin[m] = blocks;
             K3Args A;

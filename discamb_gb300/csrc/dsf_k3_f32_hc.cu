@@ -14,10 +14,10 @@ cudaError_t launch_k3_f32_hc(const K3Args &A, bool mp, bool aniso)
                  : dispatch_k3<false, float, MODEL_HC, false, false, 2, 4, 8>(A);
 }
 
-size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types)
+size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types, bool table)
 {
     if (fp64) return mp ? sf_smem_bytes<double, true>(ht, n_sym, max_types) : sf_smem_bytes<double, false>(ht, n_sym, max_types);
-    return mp ? sf_smem_bytes<float, true>(ht, n_sym, max_types) : sf_smem_bytes<float, false>(ht, n_sym, max_types);
+    return mp ? sf_smem_bytes<float, true>(ht, n_sym, max_types) : sf_smem_bytes<float, false>(ht, n_sym, max_types, table);
 }
 
 cudaError_t launch_sf3(const K3Args &A, int model, bool fp64, bool mp, bool aniso)

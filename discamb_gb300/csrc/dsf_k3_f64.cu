@@ -18,10 +18,10 @@ cudaError_t launch_k3_f64(const K3Args &A, int model, bool mp, bool aniso)
                      : dispatch_k3<false, double, MODEL_HC, false, false, 4, 8>(A);
     }
     if (model == MODEL_IAM)
-        return aniso ? dispatch_k3<false, double, MODEL_IAM, false, true>(A)
-                     : dispatch_k3<false, double, MODEL_IAM, false, false>(A);
-    return aniso ? dispatch_k3<false, double, MODEL_TABLE, false, true>(A)
-                 : dispatch_k3<false, double, MODEL_TABLE, false, false>(A);
+        return aniso ? dispatch_k3<false, double, MODEL_IAM, false, true, 4>(A)
+                     : dispatch_k3<false, double, MODEL_IAM, false, false, 4>(A);
+    return aniso ? dispatch_k3<false, double, MODEL_TABLE, false, true, 4>(A)
+                 : dispatch_k3<false, double, MODEL_TABLE, false, false, 4>(A);
 }
 
 }  // namespace dsf

@@ -219,10 +219,12 @@ __host__ __device__ constexpr int slot_l(int k) { return k == 0 ? 0 : (k < 4 ? 1
 
 template <typename R>
 struct StageLayout {
-    size_t rs, tr, trm, gw, h2, cont, bytes;
-    __host__ __device__ StageLayout(int ht, int ns, int max_types, bool mp)
+    size_t rs, tr, trm, gw, h2, cont, tab, bytes;
+    // tab: FP32 tabulated model, the tile's form factors [ht][ns][kTileAtoms] (complex64)
+    __host__ __device__ StageLayout(int ht, int ns, int max_types, bool mp, bool table = false)
     {
-        rs = 0;
+        tab = 0;
+        rs = (table && sizeof(R) == 4) ? sizeof(float2) * (size_t)ht * ns * kTileAtoms : 0;
         tr = rs + sizeof(RsRec<R>) * (size_t)ht * ns;
         trm = tr + sizeof(R) * 8 * (size_t)ht * max_types;
         gw = trm + (mp ? sizeof(R) * 8 * (size_t)ht * max_types : 0);
@@ -237,9 +239,9 @@ template <typename R, bool MP>
 __host__ __device__ constexpr int n_channels() { return MP ? 38 : 10; }
 
 template <typename R, bool MP>
-__host__ __device__ inline size_t sf_smem_bytes(int ht, int ns, int max_types)
+__host__ __device__ inline size_t sf_smem_bytes(int ht, int ns, int max_types, bool table = false)
 {
-    StageLayout<R> L(ht, ns, max_types, MP);
+    StageLayout<R> L(ht, ns, max_types, MP, table);
     size_t b = 64;                                                        // barriers
     b += 2 * L.bytes;                                                     // two stages
     b += sizeof(R) * 2 * (size_t)(kTileAtoms / 32) * ht;                  // warp partials of F
@@ -316,7 +318,8 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 
     // shared memory carve-up
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);  // [2]
-    const StageLayout<R> SL(ht, nS, L.max_types, MP);
+    const StageLayout<R> SL(ht, nS, L.max_types, MP, TABLE);
+    constexpr bool TAB_SMEM = TABLE && F32;  // form factors staged by bulk copies
     unsigned char *stage0 = smem_raw + 64;
     R2 *sF = reinterpret_cast<R2 *>(stage0 + 2 * SL.bytes);           // [kWarps][ht]
     R *sTot = reinterpret_cast<R *>(sF + kWarps * ht);                 // [NT][kTileAtoms]
@@ -353,10 +356,21 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
         unsigned char *st = stage0 + buf * SL.bytes;
         const uint32_t rs_bytes = (uint32_t)(sizeof(RsRec<R>) * ht * nS);
         const uint32_t tr_bytes = (uint32_t)(sizeof(R) * 8 * ht);
+        // the tile's columns of the table: 16-byte aligned (even first column, even row stride)
+        const int tab_col0 = a_begin + (a_begin >= S.table_split ? S.table_shift : 0);
+        const uint32_t tab_bytes = (uint32_t)((sizeof(float2) * (a_end - a_begin) + 15) & ~(size_t)15);
         const uint32_t bytes = rs_bytes + (uint32_t)(2 * sizeof(R) * ht) + (uint32_t)(sizeof(R) * ht) +
-                               (uint32_t)(sizeof(int) * ht) + (TABLE ? 0u : tr_bytes * nT * (MP ? 2u : 1u));
+                               (uint32_t)(sizeof(int) * ht) + (TABLE ? 0u : tr_bytes * nT * (MP ? 2u : 1u)) +
+                               (TAB_SMEM ? tab_bytes * (uint32_t)(ht * nS) : 0u);
         fence_proxy_async();
         mbar_expect_tx(&bar[buf], bytes);
+        if constexpr (TAB_SMEM) {
+            for (int q = 0; q < ht * nS; q++) {
+                const size_t row = (size_t)(h0 + q / nS) * nS + (q % nS);
+                bulk_copy(st + SL.tab + sizeof(float2) * kTileAtoms * (size_t)q,
+                          S.table_f + row * S.table_stride + tab_col0, tab_bytes, &bar[buf]);
+            }
+        }
         bulk_copy(st + SL.rs, rs_g + (size_t)h0 * nS, rs_bytes, &bar[buf]);
         if constexpr (!TABLE) {
             for (int t = 0; t < nT; t++) {
@@ -428,7 +442,6 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             }
         }
     }
-    const int a_orig = have ? S.atom_orig[a] : 0;
 
     if (tid == 0) issue(0, h_begin);
     uint32_t parity[2] = {0u, 0u};
@@ -565,13 +578,23 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         R A0 = 0, A1 = 0, A2 = 0, A3 = 0, A4 = 0;
                         const R *y = rec.y;
                         if constexpr (TABLE) {
-                            // the table holds n_hkl_pad rows (zero past the last reflection)
-                            const size_t ti = ((size_t)(h0 + hl) * nS + s) * S.n_atoms + a_orig;
+                            // the table holds n_hkl_pad rows (zero past the last reflection), columns in
+                            // the engine's atom order (consecutive lanes read consecutive values)
                             if constexpr (F32) {
-                                const float2 tv = S.table_f[ti];
+                                const float2 tv = reinterpret_cast<const float2 *>(st + SL.tab)[
+                                    (size_t)(hl * nS + s) * kTileAtoms + tid];
                                 fre = tv.x + anre; fim = tv.y + anim;
                             } else {
-                                const double2 tv = S.table_d[ti];
+                                const int col = a + (a >= S.table_split ? S.table_shift : 0);
+                                const size_t ti = ((size_t)(h0 + hl) * nS + s) * S.table_stride + (have ? col : 0);
+                                // an FP32-only table is read widened
+                                double2 tv;
+                                if (S.table_d) {
+                                    tv = S.table_d[ti];
+                                } else {
+                                    const float2 t1 = S.table_f[ti];
+                                    tv = make_double2(t1.x, t1.y);
+                                }
                                 fre = tv.x + anre; fim = tv.y + anim;
                             }
                         } else if constexpr (DIAG && MP) {

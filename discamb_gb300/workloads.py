@@ -10,7 +10,8 @@ five benchmark configurations
   d >= 1.5 A, isotropic B ~ U(10,40), 150 shared types;
 * ``config2``: 50,000 atoms, P4_3 2_1 2, 120x120x140 A, d >= 1.2 A,
   anisotropic non-H, 300 types, full derivative set;
-* ``config4``: tabulated form factors (see ``tabulated_batch``);
+* ``config4``: a batch of crystals with tabulated form factors
+  (``config4_specs`` / ``config4_crystal`` / ``config4_f0``);
 
 and small cases used by the tests.  Synthetic wavefunctions: every element
 gets a core and a valence orbital of two Slater functions each (hydrogen: a
@@ -237,3 +238,80 @@ def small_case(sg_symbol="P21/c", n_atoms=6, stol_max=0.5, seed=7, cell_kind=Non
     elements = [base[i % len(base)] for i in range(n_atoms)]
     return build_structure(cell=cell, sg_symbol=sg_symbol, elements=elements, rng=rng,
                            stol_max=stol_max, name=f"small-{sg_symbol}", **kw)
+
+
+# ---------------------------------------------------------------------------
+# config 4: a batch of crystals with tabulated form factors
+# ---------------------------------------------------------------------------
+def config4_specs(n_crystals=256, seed=4):
+    """(n_atoms, n_hkl) per crystal: atoms log-uniform in [10, 2000], reflections
+    log-uniform in [2000, 100000]."""
+    rng = np.random.default_rng(seed)
+    atoms = np.exp(rng.uniform(math.log(10), math.log(2000), n_crystals)).astype(int)
+    hkl = np.exp(rng.uniform(math.log(2000), math.log(100000), n_crystals)).astype(int)
+    return [(int(a), int(h)) for a, h in zip(atoms, hkl)]
+
+
+def config4_crystal(n_atoms, n_hkl, seed):
+    """One crystal of the batch: P2_1/c, anisotropic ADPs (hydrogen isotropic),
+    a cell of about 18 A^3 per atom, and the n_hkl unique reflections of lowest
+    resolution (a complete sphere in sin(theta)/lambda, trimmed to n_hkl)."""
+    rng = np.random.default_rng(seed)
+    sg = space_group("P21/c")
+    vol = 18.0 * n_atoms * sg.n_total
+    beta = rng.uniform(95, 110)
+    ratios = rng.uniform(0.8, 1.25, 3)
+    edge = (vol / (np.prod(ratios) * math.sin(math.radians(beta)))) ** (1 / 3)
+    cell = (edge * ratios[0], edge * ratios[1], edge * ratios[2], 90.0, beta, 90.0)
+    # unique reflections ~ (4 pi / 3) V / d^3 / 4 for Laue class 2/m; ask for 30% more, keep the n_hkl lowest
+    d = (4.0 * math.pi / 3.0 * vol / (4.0 * n_hkl * 1.3)) ** (1 / 3)
+    while True:
+        hkl = unique_hkl(cell, sg, d_min=d)
+        if len(hkl) >= n_hkl:
+            break
+        d *= 0.9
+    b = frac_to_cart_matrix(cell)
+    binv = np.linalg.inv(b).T  # reciprocal basis
+    s2 = np.sum((np.asarray(hkl, dtype=np.float64) @ binv.T) ** 2, axis=1)
+    hkl = np.asarray(hkl)[np.argsort(s2, kind="stable")[:n_hkl]]
+    elements = [("C", "N", "O", "H")[i] for i in rng.choice(4, n_atoms, p=[0.35, 0.1, 0.1, 0.45])]
+    return build_structure(cell=cell, sg_symbol="P21/c", elements=elements, rng=rng, n_types=4, hkl=hkl,
+                           aniso=True, l_max=0, name=f"config4-{seed}")
+
+
+# per-element spherical f0(s) = Z sum_i w_i exp(-b_i s^2), s = sin(theta)/lambda, weights summing to one
+# (Z electrons at s = 0, falling off like the core + valence densities above)
+_F0 = {"H": (1, (0.5, 0.3, 0.2), (10.0, 25.0, 3.0)),
+       "C": (6, (0.4, 0.3, 0.3), (20.0, 8.0, 0.5)),
+       "N": (7, (0.4, 0.3, 0.3), (16.0, 6.5, 0.4)),
+       "O": (8, (0.4, 0.3, 0.3), (13.0, 5.0, 0.3))}
+
+
+def config4_f0_elements(st, s):
+    """f0 per (reflection, element) at sin(theta)/lambda s [n_hkl], and the
+    element index of every atom."""
+    labels = sorted({st.wfns[w].label for w in st.atom_wfn})
+    s2 = np.asarray(s, dtype=np.float64) ** 2
+    f0 = np.zeros((len(s2), len(labels)))
+    for j, e in enumerate(labels):
+        z, ww, bb = _F0.get(e, _F0["C"])
+        f0[:, j] = z * sum(wi * np.exp(-bi * s2) for wi, bi in zip(ww, bb))
+    idx = {e: j for j, e in enumerate(labels)}
+    return f0, np.array([idx[st.wfns[w].label] for w in st.atom_wfn], dtype=np.int64)
+
+
+def config4_stol(st):
+    """sin(theta)/lambda of every reflection of a crystal."""
+    b = frac_to_cart_matrix(st.cell)
+    binv = np.linalg.inv(b).T
+    return 0.5 * np.linalg.norm(np.asarray(st.hkl, dtype=np.float64) @ binv.T, axis=1)
+
+
+def config4_table(st, rng, n_ops=4):
+    """A host table [n_hkl][n_ops][n_atoms] (complex128): f0 (1 + 0.05 CN(0, 1))
+    (the tests' small crystals; the benchmark draws the same on the device)."""
+    f0e, el = config4_f0_elements(st, config4_stol(st))
+    f0 = f0e[:, el][:, None, :]
+    shape = (st.n_hkl, n_ops, st.n_atoms)
+    noise = (rng.normal(size=shape) + 1j * rng.normal(size=shape)) * (0.05 / math.sqrt(2.0))
+    return f0 * (1.0 + noise)

@@ -162,6 +162,13 @@ int dsf_structure_create_iam(dsf_engine *e, const dsf_symmetry *sym, const dsf_i
 int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms,
                                    int n_hkl, const int *hkl, const double *table, int table_fp32,
                                    dsf_structure **out);
+/* the same from a device table (the caller's buffer on the engine's device, complex64 when table_fp64 = 0,
+ * else complex128; [n_hkl][n_symops][n_atoms] in the order of hkl): gathered on the device into the engine's
+ * complex64 table, so tables larger than host memory never cross the host.  The caller may free its buffer when
+ * the call returns.  The reference's table lives in a host std::map (ConstFormFactorCalculationsManager.cpp:9-15). */
+int dsf_structure_create_tabulated_device(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms,
+                                          int n_hkl, const int *hkl, const void *table_device, int table_fp64,
+                                          dsf_structure **out);
 int dsf_structure_destroy(dsf_structure *s);
 
 int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl);

@@ -126,3 +126,61 @@ def test_batch_rejects_foreign_structures(engine):
         b.close()
     finally:
         other.close()
+
+
+def test_device_table_matches_host_table_and_oracle(engine):
+    torch = pytest.importorskip("torch")
+    for i, (na, nh) in enumerate([(12, 2100), (40, 2500), (7, 3000)]):
+        st = W.config4_crystal(na, nh, seed=5000 + i)
+        t = W.config4_table(st, np.random.default_rng(5000 + i))
+        dev = torch.device("cuda", 0)
+        tt = torch.tensor(np.stack([t.real, t.imag], -1), dtype=torch.float32, device=dev).contiguous()
+        torch.cuda.synchronize()  # the engine gathers the table on its own stream
+        a = api.TabulatedCalculator(engine, st, table_device=tt.data_ptr())
+        del tt
+        torch.cuda.synchronize()
+        b = api.TabulatedCalculator(engine, st, table=t.astype(np.complex64), fp32_table=True)
+        for prec in (FP32, FP64):
+            ra = a.calculate(st.dtdf, precision=prec)
+            rb = b.calculate(st.dtdf, precision=prec)
+            assert rel_f(ra["f"], rb["f"]) < 1e-13
+            assert rel_norm(ra["d_xyz"], rb["d_xyz"]) < 1e-12
+        o = O.compute(st, model="table", table=t.astype(np.complex64).astype(np.complex128))
+        r = a.calculate(st.dtdf, precision=FP32)
+        assert rel_f(r["f"], o["f"]) < 1e-6
+        assert rel_norm(r["d_xyz"], o["d_xyz"]) < 1e-5 and rel_norm(r["d_adp"], o["d_adp"]) < 1e-5
+        # the FP64 form reads the complex64 table widened: FP64 accuracy on those values
+        r = a.calculate(st.dtdf, precision=FP64)
+        assert rel_f(r["f"], o["f"]) < 1e-10
+        a.close()
+        b.close()
+
+
+def test_tabulated_batch_device_path(engine):
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", 0)
+    calcs, sts, tabs = [], [], []
+    for i, (na, nh) in enumerate([(12, 2100), (40, 2500), (7, 3000), (25, 2200)]):
+        st = W.config4_crystal(na, nh, seed=5100 + i)
+        t = W.config4_table(st, np.random.default_rng(5100 + i)).astype(np.complex64)
+        tt = torch.tensor(np.stack([t.real, t.imag], -1), dtype=torch.float32, device=dev).contiguous()
+        torch.cuda.synchronize()
+        calcs.append(api.TabulatedCalculator(engine, st, table_device=tt.data_ptr()))
+        sts.append(st)
+        tabs.append(t.astype(np.complex128))
+    dt = [torch.tensor(np.stack([st.dtdf.real, st.dtdf.imag], 1), dtype=torch.float64, device=dev) for st in sts]
+    outs = [{"f": torch.zeros(st.n_hkl, 2, dtype=torch.float64, device=dev),
+             "d_xyz": torch.zeros(st.n_atoms, 3, dtype=torch.float64, device=dev)} for st in sts]
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.synchronize()
+    engine.calculate_batch_device(calcs, [d.data_ptr() for d in dt],
+                                  [{k: v.data_ptr() for k, v in o.items()} for o in outs],
+                                  precision=FP32, derivatives=("xyz",), stream=stream.cuda_stream)
+    stream.synchronize()
+    for st, t, o in zip(sts, tabs, outs):
+        ref = O.compute(st, model="table", table=t)
+        f = o["f"].cpu().numpy()
+        assert rel_f(f[:, 0] + 1j * f[:, 1], ref["f"]) < 1e-6
+        assert rel_norm(o["d_xyz"].cpu().numpy(), ref["d_xyz"]) < 1e-5
+    for c in calcs:
+        c.close()
