@@ -52,6 +52,10 @@ WORKLOADS = {
     "config4": dict(seed=4, desc="config4: 256 crystals, P21/c, tabulated complex64 form factors per (atom, h'), "
                                  "atoms log-uniform 10-2000, hkl log-uniform 2k-100k, aniso U (H iso), "
                                  "dF/d(xyz,U,occ); one batched submission per step"),
+    "config3": dict(seed=3, desc="config3: served stream, Poisson arrivals at 200 req/s, 400 structures x 5 "
+                                 "least-squares cycles (xyz sigma 0.01 A, U sigma 5%), atoms log-uniform 20-20000, "
+                                 "hkl log-uniform 1k-300k, P1/P-1/P21/P21c/P212121/C2c, HC l<=4, aniso U, "
+                                 "dF/d(xyz,U,occ)"),
     "config2": dict(seed=2, multipoles=True, flops=195, fp64_frac=0.05, cpu_frac=0.002,
                     traffic_key="sf_grad_kernel3<float,HC,MP,ANISO,8>@config2",
                     desc="config2: HC multipoles l<=4, 50000 atoms (300 types), P43212, all hkl d>=1.2A, aniso U "
@@ -218,6 +222,167 @@ def config4_batch(args, eng, dev, api, W, torch):
             o[k] = torch.empty(st.n_atoms, w, dtype=torch.float64, device=dev)
         outs.append(o)
     return specs, calcs, sts, dtdf, outs, tables_small
+
+
+def _perturbed_cycle(st, rng):
+    """One least-squares cycle's parameters: xyz moved by N(0, 0.01 A) per
+    Cartesian axis (as fractional shifts), U scaled by N(1, 0.05)."""
+    lengths = np.asarray(st.cell[:3])
+    xyz = st.xyz + rng.normal(scale=0.01, size=st.xyz.shape) / lengths
+    adp = st.adp_array() * (1.0 + rng.normal(scale=0.05, size=(st.n_atoms, 6)))
+    return xyz, adp, st.occupancy
+
+
+def run_config3(args):
+    import multiprocessing as mp
+    from discamb_gb300 import workloads as W
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    specs = W.config3_specs(args.c3_structures, seed=WORKLOADS["config3"]["seed"])
+    t_gen = time.perf_counter()
+    # structures are generated in a process pool before any CUDA use (spawn: no inherited CUDA state)
+    with mp.get_context("spawn").Pool(max(1, min(16, os.cpu_count() or 1))) as pool:
+        sts = pool.starmap(W.config3_structure, [(a, h, g, 3000 + i) for i, (a, h, g) in enumerate(specs)])
+    t_gen = time.perf_counter() - t_gen
+    # request r is least-squares cycle r // n of structure r % n: every structure's five cycles are spread
+    # over the stream (a client submits its next cycle after solving the previous one)
+    n_st = len(sts)
+    n_req = 5 * n_st
+    rng = np.random.default_rng(33)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.c3_rate, n_req))
+    cycles = [_perturbed_cycle(sts[r % n_st], rng) for r in range(n_req)]
+    terms = [st.n_atoms * st.sg.point_group_order * st.n_hkl for st in sts]
+    if args.impl == "reference":
+        return run_config3_reference(args, sts, terms)
+    import torch
+    from discamb_gb300 import api, build, serve
+    torch.cuda.set_device(0)
+    build.build()
+    eng = api.Engine(0)
+    budget = int(args.c3_hbm_gb * (1 << 30))
+    launches = [0]
+    run_batch = serve.batch_executor(eng, precision=api.DSF_FP32_BULK)
+
+    def executor(calcs, batch):
+        out = run_batch(calcs, batch)
+        launches[0] += calcs[0].last_launch_count()
+        return out
+
+    srv = serve.SfServer(executor, budget, max_batch=48)
+    admit_ms = []
+
+    def factory(st):
+        t0 = time.perf_counter()
+        c = api.HcCalculator(eng, st, upload_atoms=False)  # every request brings its cycle's atoms
+        admit_ms.append((time.perf_counter() - t0) * 1e3)
+        return c
+
+    for i, st in enumerate(sts):
+        srv.add_structure(i, lambda st=st: factory(st),
+                          serve.estimate_device_bytes(st.n_atoms, st.n_hkl, len(st.sg.subset_rot),
+                                                      len(st.types)))
+    # warm-up: kernel modules and first-call costs, on structures outside the stream
+    warm = [W.small_case(g, n_atoms=40, stol_max=0.6, seed=900 + j) for j, g in enumerate(W.CONFIG3_GROUPS)]
+    for j, st in enumerate(warm):
+        srv.add_structure(("warm", j), lambda st=st: api.HcCalculator(eng, st), 1 << 24)
+    for rep in range(args.warmup):
+        ws = [srv.submit(serve.Request(key=("warm", j), xyz=st.xyz, adp=st.adp_array(), occupancy=st.occupancy,
+                                       dtdf=st.dtdf)) for j, st in enumerate(warm)]
+        while srv.step():
+            pass
+        assert all(w.done.is_set() and w.error is None for w in ws)
+    for j in range(len(warm)):
+        srv.retire(("warm", j))
+    srv.rounds, srv.batch_sizes, srv.admissions = 0, [], 0
+    admit_ms.clear()
+    launches[0] = 0
+    reqs = []
+    with ClockSampler(0) as clk:
+        srv.start()
+        t0 = time.perf_counter()
+        for r in range(n_req):
+            dt = t0 + arrivals[r] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            xyz, adp, occ = cycles[r]
+            k = r % n_st
+            reqs.append(srv.submit(serve.Request(key=k, xyz=xyz, adp=adp, occupancy=occ, dtdf=sts[k].dtdf)))
+            if r // n_st == 4:
+                srv.retire(k)
+        for q in reqs:
+            q.done.wait()
+        t_end = time.perf_counter()
+        srv.stop()
+    clocks = clk.summary()
+    errors = [q.error for q in reqs if q.error]
+    lat = np.array([q.latency for q in reqs]) * 1e3
+    total_terms = sum(terms[r % n_st] for r in range(n_req))
+    span = max(q.t_done for q in reqs) - min(q.t_submit for q in reqs)
+    value = total_terms / span
+    line = {
+        "metric": "atom*symop*hkl terms/s (SF+grad)", "value": value, "unit": "terms/s", "n_gpus": 1,
+        "steps": 1, "warmup": args.warmup, "ms_per_step": span * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk (integer phase reduction, f64 accumulation)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOADS["config3"]["desc"], "structures": len(sts), "requests": n_req,
+                   "offered_req_per_s": args.c3_rate, "hbm_budget_gb": args.c3_hbm_gb,
+                   "generation_s": t_gen, "terms_served": total_terms,
+                   "step": "the whole served stream (arrival of the first request to completion of the last)"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                       "p99": float(np.percentile(lat, 99)), "mean": float(lat.mean()), "max": float(lat.max())},
+        "served": {"req_per_s": n_req / span, "rounds": srv.rounds,
+                   "mean_batch": float(np.mean(srv.batch_sizes)) if srv.batch_sizes else 0.0,
+                   "max_batch": max(srv.batch_sizes) if srv.batch_sizes else 0, "admissions": srv.admissions,
+                   "evictions": srv.evictions, "errors": len(errors),
+                   "admission_ms": {"p50": float(np.percentile(admit_ms, 50)) if admit_ms else None,
+                                    "max": float(max(admit_ms)) if admit_ms else None}},
+        "e2e": {"value": value, "unit": "terms/s",
+                "h2d_bytes_per_step": int(sum(16 * sts[r % n_st].n_hkl + 80 * sts[r % n_st].n_atoms
+                                              for r in range(n_req))),
+                "d2h_bytes_per_step": int(sum(16 * sts[r % n_st].n_hkl + 80 * sts[r % n_st].n_atoms
+                                              for r in range(n_req)))},
+        "gpu_launches": launches[0],
+        "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+        "wall_s_timed_region": t_end - t0,
+    }
+    print(json.dumps(line))
+    srv.close()
+    eng.close()
+    return 0
+
+
+def run_config3_reference(args, sts, terms):
+    """The reference engine's algorithm (oracle port, all host threads) on a
+    bounded sample of the served requests: the smallest structures' cycles."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    order = sorted(range(len(sts)), key=lambda i: terms[i])
+    vals, times = [], []
+    for rep in range(args.warmup + args.steps):
+        t_cpu, done = 0.0, 0
+        for i in order:
+            t0 = time.perf_counter()
+            O.compute(sts[i], n_threads=threads)
+            t_cpu += time.perf_counter() - t0
+            done += terms[i]
+            if t_cpu > 3.0:
+                break
+        if rep >= args.warmup:
+            vals.append(done / t_cpu)
+            times.append(t_cpu)
+    value = statistics.median(vals)
+    line = {"metric": "atom*symop*hkl terms/s (SF+grad)", "value": value, "unit": "terms/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.median(times) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": WORKLOADS["config3"]["desc"],
+                       "sample": "the smallest structures' requests, about 3 s of work per step"},
+            "cpu_baseline": {"value": value, "unit": "terms/s", "cores": threads, "kind": "port",
+                             "sample": "smallest served structures, all host threads"},
+            "e2e": {"value": value, "unit": "terms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
 
 
 def run_config4(args):
@@ -523,6 +688,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS))
     ap.add_argument("--c4-crystals", type=int, default=256)
+    ap.add_argument("--c3-structures", type=int, default=400)
+    ap.add_argument("--c3-rate", type=float, default=200.0)
+    ap.add_argument("--c3-hbm-gb", type=float, default=160.0)
     ap.add_argument("--cpu-sample", type=float, default=0.25)
     ap.add_argument("--reference-sample", type=float, default=0.1)
     args = ap.parse_args()
@@ -530,6 +698,8 @@ def main():
         args.warmup = 3
     if args.workload == "config4":
         return run_config4(args)
+    if args.workload == "config3":
+        return run_config3(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -112,6 +112,9 @@ def library():
                                                  _P(_Out), C.c_void_p]
         L.dsf_calculate_batch.argtypes = [_P(C.c_void_p), C.c_int, C.c_int, C.c_int, _P(C.c_void_p),
                                           _P(C.c_void_p), _P(_Out)]
+        L.dsf_calculate_batch_atoms.argtypes = [_P(C.c_void_p), C.c_int, C.c_int, C.c_int, _P(C.c_void_p),
+                                                _P(C.c_void_p), _P(C.c_void_p), _P(C.c_void_p), _P(C.c_void_p),
+                                                _P(_Out)]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
@@ -150,17 +153,23 @@ class Engine:
             raise DsfError(f"{what}: status {rc}: {msg.decode() if msg else ''}")
 
     def calculate_batch(self, calcs, dtdfs, precision=DSF_FP32_BULK, derivatives=("xyz", "adp", "occ"),
-                        multipoles=False, includes=None):
+                        multipoles=False, includes=None, atoms=None):
         """Several calculators of this engine in one submission
-        (dsf_calculate_batch): host dT/dF per calculator, the resident atoms;
+        (dsf_calculate_batch_atoms): host dT/dF per calculator; atoms[i] =
+        (xyz, adp, occupancy) of this call or None (the resident ones);
         returns one result dict per calculator (padded [n][6] ADP layout)."""
         n = len(calcs)
         flags = _flags(derivatives, multipoles)
         hs = (C.c_void_p * n)(*[c.h.value for c in calcs])
         keep, gp, ip = [], (C.c_void_p * n)(), (C.c_void_p * n)()
+        xp, ap, op = (C.c_void_p * n)(), (C.c_void_p * n)(), (C.c_void_p * n)()
         outs = (_Out * n)()
         res = []
         for i, c in enumerate(calcs):
+            if atoms is not None and atoms[i] is not None:
+                (x1, p1), (x2, p2), (x3, p3) = c._atom_arrays(*atoms[i])
+                keep += [x1, x2, x3]
+                xp[i], ap[i], op[i] = x1.ctypes.data, x2.ctypes.data, x3.ctypes.data
             g = np.ascontiguousarray(dtdfs[i], dtype=np.complex128).view(np.float64)
             keep.append(g)
             gp[i] = g.ctypes.data
@@ -171,8 +180,9 @@ class Engine:
             r = c._out_arrays(multipoles)
             res.append(r)
             c._fill_out(outs[i], r, multipoles)
-        self.check(self.lib.dsf_calculate_batch(hs, n, int(precision), flags, gp,
-                                                ip if includes is not None else None, outs), "calculate_batch")
+        self.check(self.lib.dsf_calculate_batch_atoms(hs, n, int(precision), flags, xp, ap, op, gp,
+                                                      ip if includes is not None else None, outs),
+                   "calculate_batch")
         return [c._result(r, multipoles, "padded") for c, r in zip(calcs, res)]
 
     def calculate_batch_device(self, calcs, dtdf_ptrs, outputs, precision=DSF_FP32_BULK,
@@ -424,7 +434,7 @@ class HcCalculator(_Calculator):
     """Hansen-Coppens structure factors; symmetry as the HC CPU engine
     (subset + inversion + centering multipliers) by default."""
 
-    def __init__(self, engine, st, representation="engine"):
+    def __init__(self, engine, st, representation="engine", upload_atoms=True):
         super().__init__(engine, st)
         sym, k1 = symmetry_desc(st, representation)
         model, k2 = _hc_desc(st)
@@ -432,7 +442,8 @@ class HcCalculator(_Calculator):
         engine.check(self.lib.dsf_structure_create_hc(engine.h, C.byref(sym), C.byref(model), C.byref(atoms),
                                                       C.byref(self.h)), "create_hc")
         self.set_hkl(st.hkl)
-        self.update_atoms(st.xyz, st.adp, st.occupancy)
+        if upload_atoms:  # else the first call brings the atoms (calculate(..., atoms=...))
+            self.update_atoms(st.xyz, st.adp, st.occupancy)
 
     def update_types(self, plm=None, pval=None, kappa=None, kappa_prime=None):
         ps = [None if v is None else _d(np.asarray(v).reshape(-1)) for v in (plm, pval, kappa, kappa_prime)]

@@ -19,6 +19,7 @@
 #include "dsf_launch_v3.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +34,9 @@ cudaError_t launch_rs_prep(const DevStructure &S, int n_hkl_pad, void *rs_f, voi
 cudaError_t launch_tr_prep(const DevStructure &S, int n_hkl_pad, void *tr_f, void *tr_d, void *trm_f, void *trm_d,
                            bool mp, cudaStream_t st);
 size_t rs_record_bytes(bool fp64);
+cudaError_t launch_global_plm(int n, int K, const int *perm, const int *atom_type, const double *lcs,
+                              const double *type_plm, const int *type_lmax, const double *fit, double *dmat,
+                              double *pg_d, float *pg_f, cudaStream_t st);
 size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types, bool table);
 cudaError_t launch_sf3(const K3Args &A, int model, bool fp64, bool mp, bool aniso);
 cudaError_t launch_sf_grad(const DevStructure &S, const CallBuffers &C, bool fp64, bool mp, int hkl_chunk, int ht,
@@ -56,13 +60,18 @@ struct TypeHost {
 };
 }  // namespace
 
+// One engine serves calculations on `stream` (or a caller's stream) and
+// structure set-up (uploads, table builds) on `setup`, so a thread may create
+// structures while another runs calculations on the engine's other structures.
 struct dsf_engine {
     int device = 0;
-    int live_structures = 0;
+    std::atomic<int> live_structures{0};
     cudaStream_t stream = nullptr;
+    cudaStream_t setup = nullptr;
+    std::mutex setup_mtx;  // one-time device tables
     int n_sm = 0;
     size_t max_smem = 0;
-    std::string err;
+    double *d_rotfit = nullptr;  // rotation-block fit (pinv blocks + sample directions) on this device
 };
 
 namespace {
@@ -105,9 +114,13 @@ struct Status {
         }                                                                                           \
     } while (0)
 
+// the last error message of the calling thread (each thread sees its own calls' errors)
+thread_local std::string tl_err;
+
 int fail(dsf_engine *e, int code, const std::string &msg)
 {
-    if (e) e->err = msg;
+    (void)e;
+    tl_err = msg;
     return code;
 }
 
@@ -203,10 +216,12 @@ struct dsf_structure {
         d_active, d_xq, d_xlo, d_xd, d_adp_f, d_adp_d, d_w_f, d_w_d, d_anom_f, d_anom_d, d_pg_f, d_pg_d, d_types,
         d_types_f, d_tcoeff, d_texp, d_tpow, d_texp_f, d_tpre_f, d_hkl, d_h2, d_h2f, d_hmult, d_cinv, d_table_f, d_table_d, d_perm, d_multw, d_dmat,
         d_raw, d_dtdf, d_gw_d, d_gw_f, d_facc, d_gacc, d_out, d_plm_lmax,
-        d_rs_f, d_rs_d, d_tr_f, d_tr_d, d_trm_f, d_trm_d, d_err, d_hperm, d_cont, d_tile_lmax;
+        d_rs_f, d_rs_d, d_tr_f, d_tr_d, d_trm_f, d_trm_d, d_err, d_hperm, d_cont, d_tile_lmax,
+        d_lcs, d_type_plm, d_type_lmax, d_atom_type0;
     std::vector<int> hperm;  // line-ordered reflection -> caller's index
     int n_hkl_pad = 0;
-    bool tr_valid = false, trm_valid = false;
+    // resident tables per precision (0: FP32, 1: FP64), built when a call first needs them
+    bool rs_ok[2] = {false, false}, tr_ok[2] = {false, false}, trm_ok[2] = {false, false};
     int n_tiles_plain = 0;   // tiles [0, n_tiles_plain) hold atoms without anisotropic ADPs
     int max_types_plain = 1, max_types_aniso = 1;
     std::vector<uint8_t> active_host;
@@ -226,11 +241,12 @@ namespace {
 
 // g = conj(dT/dF) * centering multiplier; effective weight of the
 // centrosymmetric forms: 2 Re g (inversion at origin), g + conj(g c_inv) (shifted)
-__global__ void gw_kernel(int n, const double2 *dtdf, const double *mult, const double2 *cinv, int centro,
-                          double2 *gw_d, float2 *gw_f, const int *perm)
+// adjoint weight of reflection i (engine line order): g = conj(dT/dF) x centering
+// multiplier, folded with the inversion centre (2 Re g at the origin,
+// g + conj(g c_inv) away from it)
+__device__ __forceinline__ void gw_one(int i, const double2 *dtdf, const double *mult, const double2 *cinv,
+                                       int centro, double2 *gw_d, float2 *gw_f, const int *perm)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     const double m = mult[i];
     const int o = perm ? perm[i] : i;
     double gre = dtdf[o].x * m, gim = -dtdf[o].y * m;
@@ -247,18 +263,23 @@ __global__ void gw_kernel(int n, const double2 *dtdf, const double *mult, const 
     gw_f[i] = make_float2((float)gre, (float)gim);
 }
 
-__global__ void f_epilogue_kernel(int n, const double2 *facc, const double *mult, const double2 *cinv, int centro,
-                                  double *f_out, const int *perm)
+__global__ void gw_kernel(int n, const double2 *dtdf, const double *mult, const double2 *cinv, int centro,
+                          double2 *gw_d, float2 *gw_f, const int *perm)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i < n) gw_one(i, dtdf, mult, cinv, centro, gw_d, gw_f, perm);
+}
+
+// F of reflection i: the accumulated U, the inversion centre and the centering multiplier
+__device__ __forceinline__ void f_epilogue_one(int i, const double2 *facc, const double *mult, const double2 *cinv,
+                                               int centro, double *f_out, const int *perm)
+{
     double2 F = facc[i];
     if (centro == 1) {
         F.x = 2.0 * F.x;
         F.y = 0.0;
     } else if (centro == 2) {
         const double2 c = cinv[i];
-        // F + c conj(F)
         const double re = F.x + (c.x * F.x + c.y * F.y);
         const double im = F.y + (c.y * F.x - c.x * F.y);
         F.x = re;
@@ -269,6 +290,13 @@ __global__ void f_epilogue_kernel(int n, const double2 *facc, const double *mult
     f_out[2 * o + 1] = F.y * mult[i];
 }
 
+__global__ void f_epilogue_kernel(int n, const double2 *facc, const double *mult, const double2 *cinv, int centro,
+                                  double *f_out, const int *perm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) f_epilogue_one(i, facc, mult, cinv, centro, f_out, perm);
+}
+
 struct GradParams {
     int n_atoms;
     int xyz_conv;   // 0 frac, 1 cart
@@ -277,14 +305,13 @@ struct GradParams {
     int want_xyz, want_adp, want_occ, want_mp;
 };
 
-__global__ void grad_epilogue_kernel(GradParams P, const double *g_acc, const int *perm, const int *adpk,
-                                     const double *w, const double *mult_w, const double *dmat,
-                                     const int *plm_lmax, double *d_xyz,
-                                     double *d_adp, double *d_occ, double *d_pval, double *d_plm, double *d_kappa,
-                                     double *d_kappa_p)
+// derivatives of atom a (engine order) in the crystal's conventions, original atom order
+__device__ __forceinline__ void grad_epilogue_one(int a, const GradParams &P, const double *g_acc, const int *perm,
+                                                  const int *adpk, const double *w, const double *mult_w,
+                                                  const double *dmat, const int *plm_lmax, double *d_xyz,
+                                                  double *d_adp, double *d_occ, double *d_pval, double *d_plm,
+                                                  double *d_kappa, double *d_kappa_p)
 {
-    const int a = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a >= P.n_atoms) return;
     const int o = perm[a];
     const double *G = g_acc + (size_t)a * kNch;
     const double wa = w[a];
@@ -329,6 +356,72 @@ __global__ void grad_epilogue_kernel(GradParams P, const double *g_acc, const in
             }
         }
     }
+}
+
+__global__ void grad_epilogue_kernel(GradParams P, const double *g_acc, const int *perm, const int *adpk,
+                                     const double *w, const double *mult_w, const double *dmat,
+                                     const int *plm_lmax, double *d_xyz,
+                                     double *d_adp, double *d_occ, double *d_pval, double *d_plm, double *d_kappa,
+                                     double *d_kappa_p)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a < P.n_atoms)
+        grad_epilogue_one(a, P, g_acc, perm, adpk, w, mult_w, dmat, plm_lmax, d_xyz, d_adp, d_occ, d_pval, d_plm,
+                          d_kappa, d_kappa_p);
+}
+
+// the per-structure work of a batched submission before and after the SF
+// kernels, for up to kPrePostItems structures per launch (kernel-parameter
+// space): block row blockIdx.y is one structure, grid-stride over its
+// reflections and atoms
+constexpr int kPrePostItems = 40;
+struct PrePostItem {
+    int n_hkl, n_atoms, centro;
+    const double2 *dtdf;
+    const double *mult;
+    const double2 *cinv;
+    const int *hperm;
+    double2 *gw_d;
+    float2 *gw_f;
+    double2 *facc;
+    double *gacc;
+    double *f_out;
+    GradParams P;
+    int want_grad;
+    const int *perm, *adpk, *plm_lmax;
+    const double *w, *mult_w, *dmat;
+    dsf_outputs out;
+};
+struct PrePostBatch {
+    int n;
+    PrePostItem item[kPrePostItems];
+};
+static_assert(sizeof(PrePostBatch) <= 32000, "kernel parameters hold at most 32764 bytes");
+static_assert(sizeof(dsf::SfBatch) <= 32000, "kernel parameters hold at most 32764 bytes");
+
+__global__ void batch_pre_kernel(const __grid_constant__ PrePostBatch B)
+{
+    const PrePostItem &it = B.item[blockIdx.y];
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < it.n_hkl; i += stride) {
+        gw_one(i, it.dtdf, it.mult, it.cinv, it.centro, it.gw_d, it.gw_f, it.hperm);
+        it.facc[i] = make_double2(0.0, 0.0);
+    }
+    const int ng = it.n_atoms * kNch;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ng; i += stride) it.gacc[i] = 0.0;
+}
+
+__global__ void batch_post_kernel(const __grid_constant__ PrePostBatch B)
+{
+    const PrePostItem &it = B.item[blockIdx.y];
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < it.n_hkl; i += stride)
+        f_epilogue_one(i, it.facc, it.mult, it.cinv, it.centro, it.f_out, it.hperm);
+    if (!it.want_grad) return;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < it.n_atoms; a += stride)
+        grad_epilogue_one(a, it.P, it.gacc, it.perm, it.adpk, it.w, it.mult_w, it.dmat, it.plm_lmax, it.out.d_xyz,
+                          it.out.d_adp, it.out.d_occ, it.out.d_pval, it.out.d_plm, it.out.d_kappa,
+                          it.out.d_kappa_prime);
 }
 
 struct AtomParams {
@@ -561,37 +654,11 @@ const RotationFit &rotation_fit()
 }
 
 // D_l with d_l(L^T u) = D_l d_l(u); stored row-major per l (165 doubles)
-void rotation_blocks(const double *L, double *D)
-{
-    const RotationFit &F = rotation_fit();
-    const int K = RotationFit::K;
-    std::vector<double> Bk(K * 25);
-    for (int k = 0; k < K; k++) {
-        double v[3];
-        for (int j = 0; j < 3; j++) v[j] = L[0 + j] * F.u[k][0] + L[3 + j] * F.u[k][1] + L[6 + j] * F.u[k][2];
-        double p[25];
-        harmonic_polys<double>(v[0], v[1], v[2], p);
-        for (int q = 0; q < 25; q++) Bk[k * 25 + q] = p[q] * kDensityNormHost[q];
-    }
-    int off = 0;
-    for (int l = 0; l <= 4; l++) {
-        const int n = 2 * l + 1;
-        // D^T = pinv * B_l  ->  D[i][j] = (pinv B)[j][i]
-        for (int i = 0; i < n; i++)
-            for (int j = 0; j < n; j++) {
-                double s = 0;
-                for (int k = 0; k < K; k++) s += F.pinv[l][j * K + k] * Bk[k * 25 + l * l + i];
-                D[off + i * n + j] = s;
-            }
-        off += n * n;
-    }
-}
-
 template <typename T>
 int upload(dsf_engine *e, DevBuf &b, const T *src, size_t n)
 {
     DSF_CUDA(b.alloc(sizeof(T) * std::max<size_t>(n, 1)));
-    if (n) DSF_CUDA(cudaMemcpyAsync(b.p, src, sizeof(T) * n, cudaMemcpyHostToDevice, e->stream));
+    if (n) DSF_CUDA(cudaMemcpyAsync(b.p, src, sizeof(T) * n, cudaMemcpyHostToDevice, e->setup));
     return DSF_OK;
 }
 
@@ -599,30 +666,31 @@ int compute_global_plm(dsf_structure *s)
 {
     dsf_engine *e = s->eng;
     const int n = s->n_atoms;
-    std::vector<double> pg(25 * (size_t)n, 0.0);
-    std::vector<float> pgf(25 * (size_t)n, 0.0f);
-    s->dmat.assign(165 * (size_t)n, 0.0);
-    for (int a = 0; a < n; a++) {
-        const int o = s->perm[a];
-        const int t = s->atom_type[o];
-        double *D = s->dmat.data() + 165 * (size_t)a;
-        rotation_blocks(s->lcs.data() + 9 * (size_t)o, D);
-        const int lmax = s->trad[t].lmax_used;
-        int off = 0;
-        for (int l = 0; l <= 4; l++) {
-            const int nl = 2 * l + 1;
-            if (l <= lmax) {
-                const double *P = s->type_plm.data() + 25 * (size_t)t + l * l;
-                for (int j = 0; j < nl; j++) {
-                    double v = 0;
-                    for (int i = 0; i < nl; i++) v += D[off + i * nl + j] * P[i];  // P_glob = D^T P
-                    pg[25 * (size_t)a + l * l + j] = v;
-                    pgf[25 * (size_t)a + l * l + j] = (float)v;
-                }
-            }
-            off += nl * nl;
-        }
+    int rc;
+    const int K = RotationFit::K;
+    std::lock_guard<std::mutex> lock(e->setup_mtx);
+    if (!e->d_rotfit) {
+        const RotationFit &F = rotation_fit();
+        std::vector<double> fit(25 * (size_t)K + 3 * (size_t)K);
+        for (int l = 0; l <= 4; l++) std::copy(F.pinv[l].begin(), F.pinv[l].end(), fit.begin() + (size_t)K * l * l);
+        for (int k = 0; k < K; k++)
+            for (int j = 0; j < 3; j++) fit[25 * (size_t)K + 3 * k + j] = F.u[k][j];
+        DSF_CUDA(cudaMalloc(&e->d_rotfit, sizeof(double) * fit.size()));
+        DSF_CUDA(cudaMemcpy(e->d_rotfit, fit.data(), sizeof(double) * fit.size(), cudaMemcpyHostToDevice));
     }
+    std::vector<int> tlmax(std::max(1, s->n_types));
+    for (int t = 0; t < s->n_types; t++) tlmax[t] = s->trad[t].lmax_used;
+    std::vector<int> atype(s->atom_type.begin(), s->atom_type.end());
+    if ((rc = upload(e, s->d_lcs, s->lcs.data(), s->lcs.size()))) return rc;
+    if ((rc = upload(e, s->d_type_plm, s->type_plm.data(), s->type_plm.size()))) return rc;
+    if ((rc = upload(e, s->d_type_lmax, tlmax.data(), tlmax.size()))) return rc;
+    if ((rc = upload(e, s->d_atom_type0, atype.data(), atype.size()))) return rc;
+    DSF_CUDA(s->d_dmat.alloc(sizeof(double) * 165 * (size_t)n));
+    DSF_CUDA(s->d_pg_d.alloc(sizeof(double) * 25 * (size_t)n));
+    DSF_CUDA(s->d_pg_f.alloc(sizeof(float) * 25 * (size_t)n));
+    DSF_CUDA(launch_global_plm(n, K, s->d_perm.as<int>(), s->d_atom_type0.as<int>(), s->d_lcs.as<double>(),
+                               s->d_type_plm.as<double>(), s->d_type_lmax.as<int>(), e->d_rotfit,
+                               s->d_dmat.as<double>(), s->d_pg_d.as<double>(), s->d_pg_f.as<float>(), e->setup));
     std::vector<int> lmx(n);
     for (int a = 0; a < n; a++) {
         const int t = s->atom_type[s->perm[a]];
@@ -633,12 +701,8 @@ int compute_global_plm(dsf_structure *s)
     for (int t = 0; t < s->n_tiles; t++)
         for (int a = s->tile_begin[t]; a < s->tile_begin[t + 1]; a++)
             tl[t] = std::max(tl[t], s->trad[s->atom_type[s->perm[a]]].lmax_used);
-    int rc;
     if ((rc = upload(e, s->d_tile_lmax, tl.data(), tl.size()))) return rc;
     if ((rc = upload(e, s->d_plm_lmax, lmx.data(), lmx.size()))) return rc;
-    if ((rc = upload(e, s->d_pg_d, pg.data(), pg.size()))) return rc;
-    if ((rc = upload(e, s->d_pg_f, pgf.data(), pgf.size()))) return rc;
-    if ((rc = upload(e, s->d_dmat, s->dmat.data(), s->dmat.size()))) return rc;
     return DSF_OK;
 }
 
@@ -776,22 +840,38 @@ int build_tiles(dsf_structure *s, bool by_type)
 void refresh_dev(dsf_structure *s);
 
 // resident per-(type, reflection) radial tables; mp = the multipole-adjoint table
-int build_radial_tables(dsf_structure *s, bool mp)
+// builds the tables a call of one precision needs: reflection-operation records,
+// radial terms, and (with the multipole adjoint) their kappa derivatives
+int ensure_tables(dsf_structure *s, bool fp64, bool mp)
 {
     dsf_engine *e = s->eng;
     if (!s->have_hkl) return DSF_OK;
+    const int p = fp64 ? 1 : 0;
+    const size_t esz = fp64 ? sizeof(double) : sizeof(float);
     const size_t row = 8 * (size_t)s->n_hkl_pad * std::max(1, s->n_types);
-    if (!mp) {
-        DSF_CUDA(s->d_tr_f.alloc(sizeof(float) * row));
-        DSF_CUDA(s->d_tr_d.alloc(sizeof(double) * row));
-        DSF_CUDA(launch_tr_prep(s->dev, s->n_hkl_pad, s->d_tr_f.p, s->d_tr_d.p, nullptr, nullptr, false, e->stream));
-        s->tr_valid = true;
-    } else {
-        DSF_CUDA(s->d_trm_f.alloc(sizeof(float) * row));
-        DSF_CUDA(s->d_trm_d.alloc(sizeof(double) * row));
-        DSF_CUDA(launch_tr_prep(s->dev, s->n_hkl_pad, nullptr, nullptr, s->d_trm_f.p, s->d_trm_d.p, true, e->stream));
-        s->trm_valid = true;
+    const bool built = !s->rs_ok[p] || !s->tr_ok[p] || (mp && !s->trm_ok[p]);
+    if (!s->rs_ok[p]) {
+        DevBuf &rs = fp64 ? s->d_rs_d : s->d_rs_f;
+        DSF_CUDA(rs.alloc(rs_record_bytes(fp64) * (size_t)s->n_hkl_pad * s->n_sym));
+        DSF_CUDA(launch_rs_prep(s->dev, s->n_hkl_pad, fp64 ? nullptr : rs.p, fp64 ? rs.p : nullptr, e->setup));
+        s->rs_ok[p] = true;
     }
+    if (!s->tr_ok[p]) {
+        DevBuf &tr = fp64 ? s->d_tr_d : s->d_tr_f;
+        DSF_CUDA(tr.alloc(esz * row));
+        DSF_CUDA(launch_tr_prep(s->dev, s->n_hkl_pad, fp64 ? nullptr : tr.p, fp64 ? tr.p : nullptr, nullptr,
+                                nullptr, false, e->setup));
+        s->tr_ok[p] = true;
+    }
+    if (mp && !s->trm_ok[p]) {
+        DevBuf &trm = fp64 ? s->d_trm_d : s->d_trm_f;
+        DSF_CUDA(trm.alloc(esz * row));
+        DSF_CUDA(launch_tr_prep(s->dev, s->n_hkl_pad, nullptr, nullptr, fp64 ? nullptr : trm.p,
+                                fp64 ? trm.p : nullptr, true, e->setup));
+        s->trm_ok[p] = true;
+    }
+    // the calls that read the tables may run on another stream
+    if (built) DSF_CUDA(cudaStreamSynchronize(e->setup));
     return DSF_OK;
 }
 
@@ -942,7 +1022,7 @@ int finish_create(dsf_engine *e, dsf_structure *s)
     if ((rc = upload(e, s->d_sym_t24, s->sym_t24.data(), s->sym_t24.size()))) return rc;
     if ((rc = upload_types(s))) return rc;
     refresh_dev(s);
-    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    DSF_CUDA(cudaStreamSynchronize(e->setup));
     return DSF_OK;
 }
 
@@ -1004,6 +1084,7 @@ int dsf_engine_create(int device, dsf_engine **out)
     e->device = device;
     cudaError_t ce = cudaSetDevice(device);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->setup, cudaStreamNonBlocking);
     if (ce != cudaSuccess) {
         delete e;
         return DSF_ERR_CUDA;
@@ -1022,11 +1103,13 @@ int dsf_engine_destroy(dsf_engine *e)
     if (e->live_structures > 0) return fail(e, DSF_ERR_STATE, "engine still owns structures; destroy them first");
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamDestroy(e->stream);
+    if (e->setup) cudaStreamDestroy(e->setup);
+    if (e->d_rotfit) cudaFree(e->d_rotfit);
     delete e;
     return DSF_OK;
 }
 
-const char *dsf_last_error(const dsf_engine *e) { return e ? e->err.c_str() : "null engine"; }
+const char *dsf_last_error(const dsf_engine *e) { return e ? tl_err.c_str() : "null engine"; }
 
 static int create_common(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms, int model,
                          dsf_structure **out, dsf_structure **sp)
@@ -1305,11 +1388,11 @@ int dsf_structure_create_tabulated_device(dsf_engine *e, const dsf_symmetry *sym
         d_order.release();
         return bail(fail(e, DSF_ERR_MEMORY, "table allocation failed"));
     }
-    table_gather_kernel<<<std::max(1, e->n_sm) * 8, 256, 0, e->stream>>>(
+    table_gather_kernel<<<std::max(1, e->n_sm) * 8, 256, 0, e->setup>>>(
         n_pad, n_hkl, s->n_sym, s->n_atoms, s->table_stride, s->table_split, s->table_shift, d_order.as<int>(),
         s->d_perm.as<int>(), table_device, table_fp64, s->d_table_f.as<float2>());
     ce = cudaGetLastError();
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->setup);
     d_order.release();
     if (ce != cudaSuccess) return bail(fail(e, DSF_ERR_CUDA, cudaGetErrorString(ce)));
     if ((rc = finish_create(e, s))) return bail(rc);
@@ -1324,6 +1407,7 @@ int dsf_structure_destroy(dsf_structure *s)
     if (!s) return DSF_ERR_ARGUMENT;
     cudaSetDevice(s->eng->device);
     cudaStreamSynchronize(s->eng->stream);
+    cudaStreamSynchronize(s->eng->setup);
     DevBuf *bufs[] = {&s->d_sym_rot, &s->d_sym_t24, &s->d_tile_begin, &s->d_tile_ntypes, &s->d_tile_types,
                       &s->d_atom_ltype, &s->d_atom_adpk, &s->d_active, &s->d_xq, &s->d_xlo, &s->d_xd, &s->d_adp_f,
                       &s->d_adp_d, &s->d_w_f, &s->d_w_d, &s->d_anom_f, &s->d_anom_d, &s->d_pg_f, &s->d_pg_d,
@@ -1331,7 +1415,8 @@ int dsf_structure_destroy(dsf_structure *s)
                       &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw, &s->d_dmat, &s->d_raw,
                       &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc, &s->d_out, &s->d_plm_lmax,
                       &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d, &s->d_trm_f, &s->d_trm_d, &s->d_err,
-                      &s->d_hperm, &s->d_cont, &s->d_tile_lmax};
+                      &s->d_hperm, &s->d_cont, &s->d_tile_lmax, &s->d_lcs, &s->d_type_plm, &s->d_type_lmax,
+                      &s->d_atom_type0};
     for (DevBuf *b : bufs) b->release();
     if (s->ev_begin) cudaEventDestroy(s->ev_begin);
     if (s->ev_end) cudaEventDestroy(s->ev_end);
@@ -1352,13 +1437,21 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
     // tables and per-reflection arrays padded with zero rows to whole sub-tiles (ht divides kMaxHT)
     const int n_pad = (n_hkl + kMaxHT - 1) / kMaxHT * kMaxHT;
     // line order: sorted by (h, k, l) so runs of l + 1 share a lattice line
-    s->hperm.resize(n_hkl);
-    std::iota(s->hperm.begin(), s->hperm.end(), 0);
-    std::stable_sort(s->hperm.begin(), s->hperm.end(), [&](int x, int y) {
-        for (int j = 0; j < 3; j++)
-            if (hkl[3 * x + j] != hkl[3 * y + j]) return hkl[3 * x + j] < hkl[3 * y + j];
-        return false;
-    });
+    // (keys pack h, k, l in 21 bits each, offset to non-negative; the index breaks ties, so the order is
+    // that of a stable sort)
+    for (int i = 0; i < 3 * n_hkl; i++)
+        if (hkl[i] <= -(1 << 20) || hkl[i] >= (1 << 20)) return fail(e, DSF_ERR_ARGUMENT, "Miller index out of range");
+    {
+        std::vector<std::pair<uint64_t, int>> key(n_hkl);
+        for (int i = 0; i < n_hkl; i++) {
+            const uint64_t h = (uint64_t)(hkl[3 * i] + (1 << 20)), k = (uint64_t)(hkl[3 * i + 1] + (1 << 20)),
+                           l = (uint64_t)(hkl[3 * i + 2] + (1 << 20));
+            key[i] = {(h << 42) | (k << 21) | l, i};
+        }
+        std::sort(key.begin(), key.end());
+        s->hperm.resize(n_hkl);
+        for (int i = 0; i < n_hkl; i++) s->hperm[i] = key[i].second;
+    }
     std::vector<int> cont(n_pad, 0);
     for (int i = 1; i < n_hkl; i++) {
         const int *p = hkl + 3 * s->hperm[i - 1], *q = hkl + 3 * s->hperm[i];
@@ -1366,6 +1459,17 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
     }
     std::vector<int4> h4(n_pad, make_int4(0, 0, 0, 0));
     std::vector<double> h2(n_pad, 0.0), mult(n_pad, 0.0), cinv(2 * (size_t)n_pad, 0.0);
+    // e^{2 pi i r / 24}, exact at quarter turns
+    double turn24[24][2];
+    for (int r = 0; r < 24; r++) {
+        turn24[r][0] = std::cos(2.0 * DSF_PI * r / 24.0);
+        turn24[r][1] = std::sin(2.0 * DSF_PI * r / 24.0);
+        if (r % 6 == 0) {
+            const int q = r / 6;
+            turn24[r][0] = q == 0 ? 1.0 : q == 2 ? -1.0 : 0.0;
+            turn24[r][1] = q == 1 ? 1.0 : q == 3 ? -1.0 : 0.0;
+        }
+    }
     for (int i = 0; i < n_hkl; i++) {
         const int *hp = hkl + 3 * s->hperm[i];
         const int h = hp[0], k = hp[1], l = hp[2];
@@ -1376,13 +1480,8 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
         mult[i] = centering_multiplier(s->centering, s->obverse, h, k, l);
         int r = (h * s->t_inv24[0] + k * s->t_inv24[1] + l * s->t_inv24[2]) % 24;
         if (r < 0) r += 24;
-        cinv[2 * i] = std::cos(2.0 * DSF_PI * r / 24.0);
-        cinv[2 * i + 1] = std::sin(2.0 * DSF_PI * r / 24.0);
-        if (r % 6 == 0) {  // exact values at quarter turns
-            const int q = r / 6;
-            cinv[2 * i] = q == 0 ? 1.0 : q == 2 ? -1.0 : 0.0;
-            cinv[2 * i + 1] = q == 1 ? 1.0 : q == 3 ? -1.0 : 0.0;
-        }
+        cinv[2 * i] = turn24[r][0];
+        cinv[2 * i + 1] = turn24[r][1];
     }
     int rc;
     if ((rc = upload(e, s->d_hperm, s->hperm.data(), s->hperm.size()))) return rc;
@@ -1399,22 +1498,19 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
     DSF_CUDA(s->d_gw_d.alloc(16 * (size_t)n_pad));
     DSF_CUDA(s->d_gw_f.alloc(8 * (size_t)n_pad));
     DSF_CUDA(s->d_facc.alloc(16 * (size_t)n_pad));
-    DSF_CUDA(cudaMemsetAsync(s->d_gw_d.p, 0, 16 * (size_t)n_pad, e->stream));
-    DSF_CUDA(cudaMemsetAsync(s->d_gw_f.p, 0, 8 * (size_t)n_pad, e->stream));
+    DSF_CUDA(cudaMemsetAsync(s->d_gw_d.p, 0, 16 * (size_t)n_pad, e->setup));
+    DSF_CUDA(cudaMemsetAsync(s->d_gw_f.p, 0, 8 * (size_t)n_pad, e->setup));
     DSF_CUDA(s->d_err.alloc(sizeof(int)));
-    DSF_CUDA(cudaMemsetAsync(s->d_err.p, 0, sizeof(int), e->stream));
+    DSF_CUDA(cudaMemsetAsync(s->d_err.p, 0, sizeof(int), e->setup));
     s->n_hkl = n_hkl;
     s->n_hkl_pad = n_pad;
     s->have_hkl = true;
     refresh_dev(s);
-    // resident per-(reflection, operation) table
-    DSF_CUDA(s->d_rs_f.alloc(rs_record_bytes(false) * (size_t)n_pad * s->n_sym));
-    DSF_CUDA(s->d_rs_d.alloc(rs_record_bytes(true) * (size_t)n_pad * s->n_sym));
-    DSF_CUDA(launch_rs_prep(s->dev, n_pad, s->d_rs_f.p, s->d_rs_d.p, e->stream));
-    s->tr_valid = s->trm_valid = false;
-    int rc2 = build_radial_tables(s, false);
+    // resident per-(reflection, operation) and radial tables: FP32 now, FP64 on the first FP64 call
+    for (int p = 0; p < 2; p++) s->rs_ok[p] = s->tr_ok[p] = s->trm_ok[p] = false;
+    int rc2 = ensure_tables(s, false, false);
     if (rc2) return rc2;
-    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    DSF_CUDA(cudaStreamSynchronize(e->setup));
     return DSF_OK;
 }
 
@@ -1476,10 +1572,10 @@ int dsf_structure_update_types(dsf_structure *s, const double *plm, const double
     int rc;
     if ((rc = upload_types(s))) return rc;
     if (plm && (rc = compute_global_plm(s))) return rc;
-    s->trm_valid = false;
-    if ((rc = build_radial_tables(s, false))) return rc;
+    for (int p = 0; p < 2; p++) s->tr_ok[p] = s->trm_ok[p] = false;
+    if ((rc = ensure_tables(s, false, false))) return rc;
     refresh_dev(s);
-    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    DSF_CUDA(cudaStreamSynchronize(e->setup));
     return DSF_OK;
 }
 
@@ -1493,7 +1589,7 @@ int dsf_structure_set_lcs(dsf_structure *s, const double *lcs)
     int rc = compute_global_plm(s);
     if (rc) return rc;
     refresh_dev(s);
-    DSF_CUDA(cudaStreamSynchronize(e->stream));
+    DSF_CUDA(cudaStreamSynchronize(e->setup));
     return DSF_OK;
 }
 
@@ -1507,7 +1603,8 @@ int64_t dsf_structure_device_bytes(const dsf_structure *s)
                             &s->d_hmult, &s->d_cinv, &s->d_table_f, &s->d_table_d, &s->d_perm, &s->d_multw,
                             &s->d_dmat, &s->d_raw, &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc,
                             &s->d_out, &s->d_plm_lmax, &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d,
-                            &s->d_trm_f, &s->d_trm_d, &s->d_err, &s->d_hperm, &s->d_cont, &s->d_tile_lmax};
+                            &s->d_trm_f, &s->d_trm_d, &s->d_err, &s->d_hperm, &s->d_cont, &s->d_tile_lmax,
+                            &s->d_lcs, &s->d_type_plm, &s->d_type_lmax, &s->d_atom_type0};
     int64_t b = 0;
     for (const DevBuf *p : bufs) b += (int64_t)p->bytes;
     return b;
@@ -1539,11 +1636,7 @@ static int call_check(dsf_structure *s, int precision, int flags, const double *
     if (!out || !out->f || !dtdf_device) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
     if (precision != DSF_FP64 && precision != DSF_FP32_BULK) return fail(e, DSF_ERR_ARGUMENT, "unknown precision");
     const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
-    if (mp && !s->trm_valid) {
-        int rc = build_radial_tables(s, true);
-        if (rc) return rc;
-    }
-    return DSF_OK;
+    return ensure_tables(s, precision == DSF_FP64, mp);
 }
 
 static int call_pre(dsf_structure *s, const double *dtdf_device, cudaStream_t st)
@@ -1723,10 +1816,61 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
     cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
     const bool fp64 = precision == DSF_FP64;
     int launches = 0, rc;
+    // adjoint weights and zeroed accumulators of all structures, kPrePostItems per launch
+    std::vector<PrePostItem> pp(n);
     for (int i = 0; i < n; i++) {
-        if ((rc = call_pre(structures[i], dtdf_device[i], st))) return rc;
-        launches++;
+        dsf_structure *s = structures[i];
+        PrePostItem &it = pp[i];
+        it.n_hkl = s->n_hkl;
+        it.n_atoms = s->n_atoms;
+        it.centro = s->centro_mode;
+        it.dtdf = reinterpret_cast<const double2 *>(dtdf_device[i]);
+        it.mult = s->d_hmult.as<double>();
+        it.cinv = s->d_cinv.as<double2>();
+        it.hperm = s->d_hperm.as<int>();
+        it.gw_d = s->d_gw_d.as<double2>();
+        it.gw_f = s->d_gw_f.as<float2>();
+        it.facc = s->d_facc.as<double2>();
+        it.gacc = s->d_gacc.as<double>();
+        it.f_out = out_device[i].f;
+        it.P.n_atoms = s->n_atoms;
+        it.P.xyz_conv = s->xyz_conv;
+        std::copy(s->Minv, s->Minv + 9, it.P.Minv);
+        std::copy(s->A6, s->A6 + 36, it.P.A6);
+        it.P.want_xyz = (flags & DSF_D_XYZ) != 0;
+        it.P.want_adp = (flags & DSF_D_ADP) != 0;
+        it.P.want_occ = (flags & DSF_D_OCC) != 0;
+        it.P.want_mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
+        it.want_grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
+        it.perm = s->d_perm.as<int>();
+        it.adpk = s->d_atom_adpk.as<int>();
+        it.plm_lmax = s->d_plm_lmax.as<int>();
+        it.w = s->d_w_d.as<double>();
+        it.mult_w = s->d_multw.as<double>();
+        it.dmat = s->d_dmat.as<double>();
+        it.out = out_device[i];
     }
+    static PrePostBatch PB;  // host staging of the launch parameters (copied at launch)
+    static std::mutex pp_mtx;
+    auto launch_prepost = [&](bool post) -> int {
+        std::lock_guard<std::mutex> lock(pp_mtx);
+        for (int b0 = 0; b0 < n; b0 += kPrePostItems) {
+            const int m = std::min(kPrePostItems, n - b0);
+            PB.n = m;
+            int longest = 1;
+            for (int k = 0; k < m; k++) {
+                PB.item[k] = pp[b0 + k];
+                longest = std::max(longest, std::max(pp[b0 + k].n_hkl, pp[b0 + k].n_atoms * (post ? 1 : kNch)));
+            }
+            const dim3 grid(std::min((longest + 255) / 256, 512), m);
+            if (post) batch_post_kernel<<<grid, 256, 0, st>>>(PB);
+            else batch_pre_kernel<<<grid, 256, 0, st>>>(PB);
+            DSF_CUDA(cudaGetLastError());
+            launches++;
+        }
+        return DSF_OK;
+    };
+    if ((rc = launch_prepost(false))) return rc;
     // group the batched items by kernel shape and sign table; the reflection
     // chunks are chosen per launch (below) so that each launch covers the SMs
     // about eight times
@@ -1832,8 +1976,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
             DSF_CUDA(launch_k3b_f32(A, g.model, g.aniso == 1));
             launches++;
         }
-    for (int i = 0; i < n; i++)
-        if ((rc = call_post(structures[i], flags, &out_device[i], st, launches))) return rc;
+    if ((rc = launch_prepost(true))) return rc;
     for (int i = 0; i < n; i++) structures[i]->last_launches = launches;
     return DSF_OK;
 }
@@ -1971,6 +2114,13 @@ static int calculate_host(dsf_structure *s, int precision, int flags, const doub
 int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int flags,
                         const double *const *dtdf, const int *const *include, const dsf_outputs *out)
 {
+    return dsf_calculate_batch_atoms(structures, n, precision, flags, nullptr, nullptr, nullptr, dtdf, include, out);
+}
+
+int dsf_calculate_batch_atoms(dsf_structure *const *structures, int n, int precision, int flags,
+                              const double *const *xyz, const double *const *adp, const double *const *occupancy,
+                              const double *const *dtdf, const int *const *include, const dsf_outputs *out)
+{
     if (!structures || n < 1 || !dtdf || !out || !structures[0]) return DSF_ERR_ARGUMENT;
     dsf_engine *e = structures[0]->eng;
     std::vector<HostCall> hc(n);
@@ -1979,8 +2129,9 @@ int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, 
     for (int i = 0; i < n; i++) {
         if (!structures[i] || structures[i]->eng != e)
             return fail(e, DSF_ERR_ARGUMENT, "batch structures must belong to one engine");
-        int rc = host_stage(structures[i], nullptr, nullptr, nullptr, dtdf[i], include ? include[i] : nullptr,
-                            &out[i], hc[i]);
+        int rc = host_stage(structures[i], xyz ? xyz[i] : nullptr, adp ? adp[i] : nullptr,
+                            occupancy ? occupancy[i] : nullptr, dtdf[i], include ? include[i] : nullptr, &out[i],
+                            hc[i]);
         if (rc) return rc;
         d[i] = hc[i].d;
         g[i] = structures[i]->d_dtdf.as<double>();

@@ -144,8 +144,8 @@ __global__ void tr_prep_kernel(DevStructure S, int n_hkl_pad, R *tr, R *trm, int
 cudaError_t launch_rs_prep(const DevStructure &S, int n_hkl_pad, void *rs_f, void *rs_d, cudaStream_t st)
 {
     const int n = n_hkl_pad * S.n_sym;
-    rs_prep_kernel<float><<<(n + 127) / 128, 128, 0, st>>>(S, n_hkl_pad, (RsRec<float> *)rs_f);
-    rs_prep_kernel<double><<<(n + 127) / 128, 128, 0, st>>>(S, n_hkl_pad, (RsRec<double> *)rs_d);
+    if (rs_f) rs_prep_kernel<float><<<(n + 127) / 128, 128, 0, st>>>(S, n_hkl_pad, (RsRec<float> *)rs_f);
+    if (rs_d) rs_prep_kernel<double><<<(n + 127) / 128, 128, 0, st>>>(S, n_hkl_pad, (RsRec<double> *)rs_d);
     return cudaGetLastError();
 }
 
@@ -153,11 +153,73 @@ cudaError_t launch_tr_prep(const DevStructure &S, int n_hkl_pad, void *tr_f, voi
                            bool mp, cudaStream_t st)
 {
     dim3 grid((n_hkl_pad + 127) / 128, S.n_types);
-    tr_prep_kernel<float><<<grid, 128, 0, st>>>(S, n_hkl_pad, mp ? nullptr : (float *)tr_f, (float *)trm_f, mp);
-    tr_prep_kernel<double><<<grid, 128, 0, st>>>(S, n_hkl_pad, mp ? nullptr : (double *)tr_d, (double *)trm_d, mp);
+    float *tf = mp ? nullptr : (float *)tr_f, *mf = mp ? (float *)trm_f : nullptr;
+    double *td = mp ? nullptr : (double *)tr_d, *md = mp ? (double *)trm_d : nullptr;
+    if (tf || mf) tr_prep_kernel<float><<<grid, 128, 0, st>>>(S, n_hkl_pad, tf, mf, mp);
+    if (td || md) tr_prep_kernel<double><<<grid, 128, 0, st>>>(S, n_hkl_pad, td, md, mp);
     return cudaGetLastError();
 }
 
 size_t rs_record_bytes(bool fp64) { return fp64 ? sizeof(RsRec<double>) : sizeof(RsRec<float>); }
+
+// Per atom (engine order): the rotation blocks D_l (l = 0..4) of the
+// density-normalised real harmonics between the atom's local frame and the
+// crystal frame, d(L^T u) = D d(u), fitted over K sample directions
+// (D_l^T = pinv_l B_l with B_l the harmonics of the rotated directions), and
+// the global-frame populations P_glob = D^T P up to the type's l_max
+// (calculateGlobalCoordinatesPlm, src/Scattering/HansenCoppens_SF_Engine3.cpp:594-654).
+// fit = [pinv_0 .. pinv_4] ([2l+1][K] each, at offset K l^2) then the K directions [K][3].
+__global__ void global_plm_kernel(int n, int K, const int *perm, const int *atom_type, const double *lcs,
+                                  const double *type_plm, const int *type_lmax, const double *fit, double *dmat,
+                                  double *pg_d, float *pg_f)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const int o = perm[a], t = atom_type[o];
+    const double *L = lcs + 9 * (size_t)o;
+    const double *u = fit + (size_t)K * 25;
+    double D[165];
+    for (int q = 0; q < 165; q++) D[q] = 0.0;
+    for (int k = 0; k < K; k++) {
+        double v[3], p[25];
+        for (int j = 0; j < 3; j++) v[j] = L[0 + j] * u[3 * k] + L[3 + j] * u[3 * k + 1] + L[6 + j] * u[3 * k + 2];
+        harmonic_polys<double>(v[0], v[1], v[2], p);
+        int off = 0;
+        for (int l = 0; l <= 4; l++) {
+            const int nl = 2 * l + 1;
+            const double *pinv = fit + (size_t)K * l * l;
+            for (int i = 0; i < nl; i++) {
+                const double b = p[l * l + i] * kDensityNorm[l * l + i];
+                for (int j = 0; j < nl; j++) D[off + i * nl + j] += pinv[j * K + k] * b;
+            }
+            off += nl * nl;
+        }
+    }
+    double *Dout = dmat + 165 * (size_t)a;
+    for (int q = 0; q < 165; q++) Dout[q] = D[q];
+    const int lmax = type_lmax[t];
+    const double *P = type_plm + 25 * (size_t)t;
+    int off = 0;
+    for (int l = 0; l <= 4; l++) {
+        const int nl = 2 * l + 1;
+        for (int j = 0; j < nl; j++) {
+            double v = 0.0;
+            if (l <= lmax)
+                for (int i = 0; i < nl; i++) v += D[off + i * nl + j] * P[l * l + i];
+            pg_d[25 * (size_t)a + l * l + j] = v;
+            pg_f[25 * (size_t)a + l * l + j] = (float)v;
+        }
+        off += nl * nl;
+    }
+}
+
+cudaError_t launch_global_plm(int n, int K, const int *perm, const int *atom_type, const double *lcs,
+                              const double *type_plm, const int *type_lmax, const double *fit, double *dmat,
+                              double *pg_d, float *pg_f, cudaStream_t st)
+{
+    global_plm_kernel<<<(n + 63) / 64, 64, 0, st>>>(n, K, perm, atom_type, lcs, type_plm, type_lmax, fit, dmat,
+                                                     pg_d, pg_f);
+    return cudaGetLastError();
+}
 
 }  // namespace dsf

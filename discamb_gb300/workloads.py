@@ -315,3 +315,55 @@ def config4_table(st, rng, n_ops=4):
     shape = (st.n_hkl, n_ops, st.n_atoms)
     noise = (rng.normal(size=shape) + 1j * rng.normal(size=shape)) * (0.05 / math.sqrt(2.0))
     return f0 * (1.0 + noise)
+
+
+# ---------------------------------------------------------------------------
+# config 3: a served stream of refinement requests
+# ---------------------------------------------------------------------------
+CONFIG3_GROUPS = ("P1", "P-1", "P21", "P21/c", "P212121", "C2/c")
+
+
+def config3_specs(n_structures=400, seed=3):
+    """(n_atoms, n_hkl, space group) per structure: atoms log-uniform in
+    [20, 20000], reflections log-uniform in [1000, 300000], the space group
+    uniform over P1, P-1, P2_1, P2_1/c, P2_1 2_1 2_1, C2/c."""
+    rng = np.random.default_rng(seed)
+    atoms = np.exp(rng.uniform(math.log(20), math.log(20000), n_structures)).astype(int)
+    hkl = np.exp(rng.uniform(math.log(1000), math.log(300000), n_structures)).astype(int)
+    groups = rng.integers(len(CONFIG3_GROUPS), size=n_structures)
+    return [(int(a), int(h), CONFIG3_GROUPS[g]) for a, h, g in zip(atoms, hkl, groups)]
+
+
+def config3_structure(n_atoms, n_hkl, sg_symbol, seed):
+    """One served structure, parameters as config0 (Hansen-Coppens multipoles
+    to l = 4, anisotropic non-H atoms) with min(n_atoms, 64) shared types; a
+    cell of about 18 A^3 per atom and the n_hkl lowest-resolution unique
+    reflections."""
+    rng = np.random.default_rng(seed)
+    sg = space_group(sg_symbol)
+    vol = 18.0 * n_atoms * sg.n_total
+    kind = {"P1": "triclinic", "P-1": "triclinic"}.get(sg_symbol,
+                                                       "orthorhombic" if sg_symbol == "P212121" else "monoclinic")
+    angles = {"triclinic": (rng.uniform(80, 100), rng.uniform(95, 110), rng.uniform(80, 100)),
+              "monoclinic": (90.0, rng.uniform(95, 110), 90.0), "orthorhombic": (90.0, 90.0, 90.0)}[kind]
+    ratios = rng.uniform(0.8, 1.25, 3)
+    unit = random_cell(rng, kind)  # consume the same draws as the small cases
+    del unit
+    cell0 = (1.0, 1.0, 1.0) + tuple(angles)
+    v1 = abs(np.linalg.det(frac_to_cart_matrix(cell0)))
+    edge = (vol / (np.prod(ratios) * v1)) ** (1 / 3)
+    cell = tuple(edge * ratios) + tuple(angles)
+    d = (4.0 * math.pi / 3.0 * vol / (max(2, sg.n_total) * n_hkl * 1.3)) ** (1 / 3)
+    while True:
+        hkl = unique_hkl(cell, sg, d_min=d)
+        if len(hkl) >= n_hkl:
+            break
+        d *= 0.9
+    b = frac_to_cart_matrix(cell)
+    binv = np.linalg.inv(b).T
+    s2 = np.sum((np.asarray(hkl, dtype=np.float64) @ binv.T) ** 2, axis=1)
+    hkl = np.asarray(hkl)[np.argsort(s2, kind="stable")[:n_hkl]]
+    elements = [("C", "N", "O", "H")[i] for i in rng.choice(4, n_atoms, p=[0.35, 0.1, 0.1, 0.45])]
+    elements[:3] = ["C", "N", "O"][:min(3, n_atoms)]
+    return build_structure(cell=cell, sg_symbol=sg_symbol, elements=elements, rng=rng,
+                           n_types=min(n_atoms, 64), hkl=hkl, aniso=True, name=f"config3-{seed}")

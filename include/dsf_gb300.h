@@ -202,6 +202,11 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
  * stream synchronisation for the whole batch */
 int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int derivative_flags,
                         const double *const *dtdf, const int *const *include, const dsf_outputs *out);
+/* the same with every structure's atomic parameters of this call (xyz[i] NULL: the resident ones), as
+ * dsf_calculate_atoms does for one structure: a serving loop's least-squares cycles in one submission */
+int dsf_calculate_batch_atoms(dsf_structure *const *structures, int n, int precision, int derivative_flags,
+                              const double *const *xyz, const double *const *adp, const double *const *occupancy,
+                              const double *const *dtdf, const int *const *include, const dsf_outputs *out);
 
 /* number of kernel launches issued by the last calculation (for accounting) */
 int dsf_last_launch_count(const dsf_structure *s);
