@@ -23,9 +23,16 @@
  *                               dTarget_dparam, dTarget_df, countAtomContribution, selector)
  *                               (HansenCoppensStructureFactorCalculator.cpp:380-508 and
  *                                AnyScattererStructureFactorCalculator.cpp:614-829), host buffers
+ *   dsf_calculate_atoms         the same call with the atoms' parameters of the call (one submission)
  *   dsf_calculate_device        the same with device-resident buffers on a caller stream
+ *   dsf_structure_create_tabulated_device
+ *                               the tabulated model from a device table (no host copy of the table)
+ *   dsf_calculate_batch, dsf_calculate_batch_atoms, dsf_calculate_batch_device
+ *                               many structures in one submission (the reference's callers run one
+ *                               calculator per structure in turn, HcAtomBankStructureFactorCalculator.cpp:482-520)
  *   dsf_last_error              on_error::throwException messages (include/discamb/BasicUtilities/on_error.h:24-36):
- *                               every function returns a status instead of throwing
+ *                               every function returns a status instead of throwing; the message is the
+ *                               calling thread's last one
  *
  * Conventions follow the reference: dT/dF = dT/dA + i dT/dB per reflection;
  * derivatives are returned in the crystal's xyz and ADP conventions;
