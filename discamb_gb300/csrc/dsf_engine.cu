@@ -196,7 +196,8 @@ struct dsf_structure {
     // which they differ by a sign-diagonal Cartesian map of the reciprocal
     // vector; sym_sign: that map's signs relative to the coset's first operation
     int coset_size = 0;
-    std::vector<int> sym_sign;  // [n_sym][3]
+    std::vector<int> sym_sign;   // [n_sym][3] Cartesian
+    std::vector<int> sym_fsign;  // [n_sym][3] fractional h' components
     // tabulated model: column of sorted atom a = a + (a >= table_split ? table_shift : 0), table_stride
     // columns per row (even), so every tile's columns start on a 16-byte boundary
     int table_stride = 0, table_split = 0, table_shift = 0;
@@ -487,6 +488,8 @@ __global__ void atom_convert_kernel(AtomParams P, const double *raw, const int *
 // harmonics of the operations of one coset are then signed copies of each
 // other (sf_grad_kernel3's class-sum form).  Leaves the order alone unless all
 // cosets have one size >= 2.
+bool fractional_signs(dsf_structure *s, int cs);
+
 void order_sign_cosets(dsf_structure *s)
 {
     const int n = s->n_sym;
@@ -547,6 +550,34 @@ void order_sign_cosets(dsf_structure *s)
     s->sym_t24.swap(t24);
     s->sym_sign = sign;
     s->coset_size = cs;
+    // the same cosets must be sign-diagonal on the fractional h' as well (standard settings are)
+    if (!fractional_signs(s, cs)) s->coset_size = 0;
+}
+
+// fractional signs of every operation relative to the first of its coset (cosets of
+// cs consecutive operations): R_s^T = D R_r^T with D = diag(+-1, +-1, +-1), i.e. column
+// i of R_s is +-column i of R_r; false if an operation is not of that form
+bool fractional_signs(dsf_structure *s, int cs)
+{
+    const int n = s->n_sym;
+    s->sym_fsign.assign(3 * (size_t)n, 1);
+    if (cs < 1) return false;
+    for (int op = 0; op < n; op++) {
+        const int *R = &s->sym_rot[9 * op], *Rr = &s->sym_rot[9 * (op - op % cs)];
+        for (int i = 0; i < 3; i++) {
+            int d = 0;
+            for (int j = 0; j < 3; j++) {
+                const int a = R[3 * j + i], b = Rr[3 * j + i];
+                if (a == 0 && b == 0) continue;
+                const int sg = (a == b) ? 1 : (a == -b ? -1 : 0);
+                if (sg == 0 || (d != 0 && d != sg)) return false;
+                d = sg;
+            }
+            if (d == 0) return false;
+            s->sym_fsign[3 * op + i] = d;
+        }
+    }
+    return true;
 }
 
 int sym_from_desc(dsf_engine *e, dsf_structure *s, const dsf_symmetry *sym)
@@ -567,7 +598,14 @@ int sym_from_desc(dsf_engine *e, dsf_structure *s, const dsf_symmetry *sym)
         if (v < 0) v += 24;
         s->sym_t24[i] = v;
     }
-    if (s->model == MODEL_HC) order_sign_cosets(s);
+    if (s->model == MODEL_HC) {
+        order_sign_cosets(s);
+    } else {
+        // generic engine: the operations keep the caller's order (the tabulated model's table follows it);
+        // one coset when every operation is a sign-diagonal image of the first
+        s->coset_size = (s->n_sym >= 2 && fractional_signs(s, s->n_sym)) ? s->n_sym : 0;
+        s->sym_sign.assign(3 * (size_t)s->n_sym, 1);
+    }
     s->centro_mode = 0;
     if (sym->centrosymmetric) {
         bool origin = true;
@@ -1667,18 +1705,23 @@ static void call_buffers(dsf_structure *s, bool fp64, CallBuffers &C, SfLaunch &
     L.error = s->d_err.as<int>();
     L.cont = s->d_cont.as<int>();
     L.tile_lmax = s->d_tile_lmax.as<int>();
-    // class-sum kernels: HC, operations in sign-diagonal cosets
+    // coset kernels: operations in sign-diagonal cosets (HC: harmonics and ADPs; other models: ADPs)
     L.coset = 0;
     std::memset(&G, 0, sizeof(G));
-    if (s->model == MODEL_HC && s->coset_size && coset_form_compiled(fp64, s->n_sym, s->coset_size)) {
+    if (s->coset_size && coset_form_compiled(fp64, s->model, s->n_sym, s->coset_size)) {
         L.coset = s->coset_size;
         for (int op = 0; op < s->n_sym; op++)
             for (int c = 0; c < 8; c++) {
-                int sg = 1;
+                int sg = 1, fs = 1;
                 for (int i = 0; i < 3; i++)
-                    if ((c >> i) & 1) sg *= s->sym_sign[3 * op + i];
+                    if ((c >> i) & 1) {
+                        sg *= s->sym_sign[3 * op + i];
+                        fs *= s->sym_fsign[3 * op + i];
+                    }
                 G.f[op][c] = (float)sg;
                 G.d[op][c] = (double)sg;
+                G.xf[op][c] = (float)fs;
+                G.xd[op][c] = (double)fs;
             }
     }
 }

@@ -8,8 +8,8 @@ cudaError_t launch_k3_f32_hc(const K3Args &A, bool mp, bool aniso)
 {
     if (mp) return launch_k3_f32_hc_mp(A, aniso);
     if (A.coset)
-        return aniso ? dispatch_coset<false, float, false, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
-                     : dispatch_coset<false, float, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);
+        return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
+                     : dispatch_coset<false, float, MODEL_HC, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);
     return aniso ? dispatch_k3<false, float, MODEL_HC, false, true, 2, 4, 8>(A)
                  : dispatch_k3<false, float, MODEL_HC, false, false, 2, 4, 8>(A);
 }

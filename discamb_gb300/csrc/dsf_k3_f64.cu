@@ -7,13 +7,13 @@ cudaError_t launch_k3_f64(const K3Args &A, int model, bool mp, bool aniso)
 {
     if (model == MODEL_HC) {
         if (mp && A.coset)
-            return aniso ? dispatch_coset<false, double, true, true, 4, 4, 8, 4>(A)
-                         : dispatch_coset<false, double, true, false, 4, 4, 8, 4>(A);
+            return aniso ? dispatch_coset<false, double, MODEL_HC, true, true, 4, 4, 8, 4>(A)
+                         : dispatch_coset<false, double, MODEL_HC, true, false, 4, 4, 8, 4>(A);
         if (mp) return aniso ? dispatch_k3<false, double, MODEL_HC, true, true, 4, 8>(A)
                              : dispatch_k3<false, double, MODEL_HC, true, false, 4, 8>(A);
         if (A.coset)
-            return aniso ? dispatch_coset<false, double, false, true, 4, 4, 8, 4>(A)
-                         : dispatch_coset<false, double, false, false, 4, 4, 8, 4>(A);
+            return aniso ? dispatch_coset<false, double, MODEL_HC, false, true, 4, 4, 8, 4>(A)
+                         : dispatch_coset<false, double, MODEL_HC, false, false, 4, 4, 8, 4>(A);
         return aniso ? dispatch_k3<false, double, MODEL_HC, false, true, 4, 8>(A)
                      : dispatch_k3<false, double, MODEL_HC, false, false, 4, 8>(A);
     }

@@ -54,25 +54,28 @@ cudaError_t dispatch_k3(const K3Args &A)
     return dispatch_k3<BATCH, R, MODEL, MP, ANISO, NS...>(A);
 }
 
-// HC, operations in sign-diagonal cosets: the class-sum kernels of the
-// compiled (operation count, coset size) pairs; the engine sets L.coset only
-// for those pairs (coset_form_compiled)
-template <bool BATCH, typename R, bool MP, bool ANISO>
+// operations in sign-diagonal cosets: the coset kernels of the compiled
+// (operation count, coset size) pairs; the engine sets L.coset only for those
+// pairs (coset_form_compiled)
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO>
 cudaError_t dispatch_coset(const K3Args &)
 {
     return cudaErrorInvalidValue;
 }
 
-template <bool BATCH, typename R, bool MP, bool ANISO, int N0, int CS0, int... NC>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, int N0, int CS0, int... NC>
 cudaError_t dispatch_coset(const K3Args &A)
 {
-    if (A.n_sym == N0 && A.coset == CS0) return launch_k3<BATCH, R, MODEL_HC, MP, ANISO, N0, CS0>(A);
-    return dispatch_coset<BATCH, R, MP, ANISO, NC...>(A);
+    if (A.n_sym == N0 && A.coset == CS0) return launch_k3<BATCH, R, MODEL, MP, ANISO, N0, CS0>(A);
+    return dispatch_coset<BATCH, R, MODEL, MP, ANISO, NC...>(A);
 }
 
-// (operation count, coset size) pairs with compiled class-sum kernels
-__host__ inline bool coset_form_compiled(bool fp64, int n_sym, int cs)
+// (operation count, coset size) pairs with compiled coset kernels.  HC: both
+// ADP kinds; IAM and tabulated: the anisotropic kernels, one coset of all
+// operations (their launches of isotropic tiles use the general form)
+__host__ inline bool coset_form_compiled(bool fp64, int model, int n_sym, int cs)
 {
+    if (model != MODEL_HC) return !fp64 && cs == n_sym && (n_sym == 2 || n_sym == 4 || n_sym == 8);
     if (fp64) return (n_sym == 4 && cs == 4) || (n_sym == 8 && cs == 4);
     return (n_sym == 2 && cs == 2) || (n_sym == 4 && (cs == 4 || cs == 2)) || (n_sym == 8 && (cs == 8 || cs == 4));
 }

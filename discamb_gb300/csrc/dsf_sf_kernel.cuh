@@ -178,6 +178,10 @@ struct SfLaunch {
 struct SignTable {
     float f[8][8];
     double d[8][8];
+    // the same classes for the fractional components of h' (the ADP quadratic
+    // form and the position adjoint work in fractional coordinates)
+    float xf[8][8];
+    double xd[8][8];
 };
 
 // structures of one batched launch (sf_grad_batch3): kernel-parameter space
@@ -293,9 +297,14 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     // parity class from the harmonics of the coset's first operation, and each
     // operation combines the eight class sums with its signs -- the same sums
     // as the per-operation form
-    constexpr bool DIAG = CS > 0;
-    static_assert(!DIAG || (MODEL == MODEL_HC && NSC > 0 && NSC <= 8 && NSC % CS == 0),
-                  "coset form: HC, compiled count <= 8");
+    // The ADP side of the coset form (all models, ANISO): within a coset h' of
+    // operation s is a sign-diagonal image of the first operation's h', so the
+    // quadratic form is q_s = q_diag + signed cross terms, and the position and
+    // ADP adjoints need six signed sums of u per coset instead of h' and m6 per
+    // operation (ADIAG).
+    constexpr bool DIAG = CS > 0 && MODEL == MODEL_HC;
+    constexpr bool ADIAG = CS > 0 && ANISO;
+    static_assert(CS == 0 || (NSC > 0 && NSC <= 8 && NSC % CS == 0), "coset form: compiled count <= 8");
     using R2 = typename Vec2<R>::T;
     constexpr bool F32 = sizeof(R) == 4;
     constexpr int NT = n_channels<R, MP>();
@@ -498,6 +507,34 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     for (int q = 0; q < (ANISO ? 6 : 1); q++) { Are[q] = R(0); Aim[q] = R(0); }
                     R Ere = 0, Eim = 0, Kre = 0, Kim = 0;
                     const RsRec<R> *recs = sRs + (size_t)hl * nS;
+                    // ADIAG: the coset's first h', its m6, the split quadratic form, and the signed
+                    // sums of u: x y z (classes 1 2 4) and xy xz yz (classes 3 5 6), and plain U
+                    R hr[3] = {0, 0, 0}, m6r[ADIAG ? 6 : 1], qd = 0, qc[3] = {0, 0, 0};
+                    R Sre[ADIAG ? 6 : 1], Sim[ADIAG ? 6 : 1], Ucre = 0, Ucim = 0;
+#pragma unroll
+                    for (int q = 0; q < (ADIAG ? 6 : 1); q++) { m6r[q] = R(0); Sre[q] = R(0); Sim[q] = R(0); }
+                    auto adp_coset_begin = [&](const RsRec<R> &rec) {
+                        if constexpr (ADIAG) {
+                            hr[0] = rec.hf[0]; hr[1] = rec.hf[1]; hr[2] = rec.hf[2];
+                            m6r[0] = hr[0] * hr[0]; m6r[1] = hr[1] * hr[1]; m6r[2] = hr[2] * hr[2];
+                            m6r[3] = R(2) * hr[0] * hr[1]; m6r[4] = R(2) * hr[0] * hr[2]; m6r[5] = R(2) * hr[1] * hr[2];
+                            qd = adp[0] * m6r[0] + adp[1] * m6r[1] + adp[2] * m6r[2];
+                            qc[0] = adp[3] * m6r[3]; qc[1] = adp[4] * m6r[4]; qc[2] = adp[5] * m6r[5];
+#pragma unroll
+                            for (int q = 0; q < 6; q++) { Sre[q] = R(0); Sim[q] = R(0); }
+                            Ucre = R(0); Ucim = R(0);
+                        }
+                    };
+                    auto adp_coset_end = [&]() {
+                        if constexpr (ADIAG) {
+#pragma unroll
+                            for (int c = 0; c < 3; c++) { Xre[c] += hr[c] * Sre[c]; Xim[c] += hr[c] * Sim[c]; }
+#pragma unroll
+                            for (int q = 0; q < 3; q++) { Are[q] -= m6r[q] * Ucre; Aim[q] -= m6r[q] * Ucim; }
+#pragma unroll
+                            for (int q = 3; q < 6; q++) { Are[q] -= m6r[q] * Sre[q]; Aim[q] -= m6r[q] * Sim[q]; }
+                        }
+                    };
                     // coset form: radial-weighted class sums, even l (real part) and odd l (imaginary part)
                     R Ec[4] = {0, 0, 0, 0}, Oc[4] = {0, 0, 0, 0};  // classes 0 3 6 5 | 2 4 1 7
                     // with the multipole adjoint: unweighted slot sums (l, class) and the
@@ -566,7 +603,14 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         }
                         R zre = cs, zim = sn;  // e^{i theta} T_s
                         R m6[ANISO ? 6 : 1];
-                        if constexpr (ANISO) {
+                        const auto xs = [&](int c) -> R {
+                            if constexpr (F32) return G.xf[s][c]; else return G.xd[s][c];
+                        };
+                        if constexpr (ADIAG) {
+                            const R q = qd + xs(3) * qc[0] + xs(5) * qc[1] + xs(6) * qc[2];
+                            const R T = texp<R>(-q);
+                            zre *= T; zim *= T;
+                        } else if constexpr (ANISO) {
                             m6[0] = h0f * h0f; m6[1] = h1f * h1f; m6[2] = h2f * h2f;
                             m6[3] = R(2) * h0f * h1f; m6[4] = R(2) * h0f * h2f; m6[5] = R(2) * h1f * h2f;
                             const R q = adp[0] * m6[0] + adp[1] * m6[1] + adp[2] * m6[2] + adp[3] * m6[3] +
@@ -641,12 +685,23 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         const R ure = fre * zre - fim * zim;
                         const R uim = fre * zim + fim * zre;
                         Ure += ure; Uim += uim;
-                        Xre[0] += h0f * ure; Xim[0] += h0f * uim;
-                        Xre[1] += h1f * ure; Xim[1] += h1f * uim;
-                        Xre[2] += h2f * ure; Xim[2] += h2f * uim;
-                        if constexpr (ANISO) {
+                        if constexpr (ADIAG) {
+                            Ucre += ure; Ucim += uim;
+                            // signed sums: x y z -> slots 0 1 2 (classes 1 2 4), xy xz yz -> 3 4 5 (3 5 6)
+                            Sre[0] += xs(1) * ure; Sim[0] += xs(1) * uim;
+                            Sre[1] += xs(2) * ure; Sim[1] += xs(2) * uim;
+                            Sre[2] += xs(4) * ure; Sim[2] += xs(4) * uim;
+                            Sre[3] += xs(3) * ure; Sim[3] += xs(3) * uim;
+                            Sre[4] += xs(5) * ure; Sim[4] += xs(5) * uim;
+                            Sre[5] += xs(6) * ure; Sim[5] += xs(6) * uim;
+                        } else {
+                            Xre[0] += h0f * ure; Xim[0] += h0f * uim;
+                            Xre[1] += h1f * ure; Xim[1] += h1f * uim;
+                            Xre[2] += h2f * ure; Xim[2] += h2f * uim;
+                            if constexpr (ANISO) {
 #pragma unroll
-                            for (int q = 0; q < 6; q++) { Are[q] -= m6[q] * ure; Aim[q] -= m6[q] * uim; }
+                                for (int q = 0; q < 6; q++) { Are[q] -= m6[q] * ure; Aim[q] -= m6[q] * uim; }
+                            }
                         }
                         if constexpr (MP) {
                             const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
@@ -682,16 +737,23 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     if constexpr (NSC > 0) {
 #pragma unroll
                         for (int s = 0; s < NSC; s++) {
-                            if constexpr (DIAG) {
+                            if constexpr (CS > 0) {
                                 if (s % CS == 0) {
-                                    if (s > 0) flush_slots(recs[s - CS].y);
+                                    if (s > 0) {
+                                        flush_slots(recs[s - CS].y);
+                                        adp_coset_end();
+                                    }
                                     class_sums(recs[s].y);
                                     slot_sums(recs[s].y);
+                                    adp_coset_begin(recs[s]);
                                 }
                             }
                             term(s);
                         }
-                        if constexpr (DIAG) flush_slots(recs[NSC - CS].y);
+                        if constexpr (CS > 0) {
+                            flush_slots(recs[NSC - CS].y);
+                            adp_coset_end();
+                        }
                     } else {
 #pragma unroll 1
                         for (int s = 0; s < nS; s++) term(s);
