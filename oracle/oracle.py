@@ -87,6 +87,8 @@ def lib():
         _lib = C.CDLL(LIB_PATH)
         _lib.sfo_compute.argtypes = [_P(_Problem), _P(_Result), C.c_int]
         _lib.sfo_compute.restype = C.c_int
+        _lib.sfo_compute_lines.argtypes = [_P(_Problem), _P(C.c_int), _P(C.c_double), _P(_Result), C.c_int]
+        _lib.sfo_compute_lines.restype = C.c_int
         _lib.sfo_g.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double]
         _lib.sfo_g.restype = C.c_double
         _lib.sfo_dlm.argtypes = [_P(C.c_double), _P(C.c_double)]
@@ -155,7 +157,7 @@ def hc_model_arrays(st):
 
 
 def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), multipoles=False,
-            iam=None, table=None, hkl_subset=None):
+            iam=None, table=None, hkl_subset=None, loop="direct"):
     """F and dT/dparam for a Structure at the API level (crystal conventions).
 
     model: 'hc' (HansenCoppens engine: symmetry subset, inversion and
@@ -164,6 +166,9 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     complex array [hkl][op][atom] over all operations.
     Returns dict with f (complex), d_xyz, d_adp, d_occ and, with multipoles,
     d_pval, d_plm, d_kappa, d_kappa_p.
+    loop: 'direct' (every term evaluated directly) or, for the HC model,
+    'lines' (the reference engine's line-ordered loop with recurrences: the
+    benchmark's CPU baseline).
     """
     from discamb_gb300.crystal import (centering_multipliers, convert_adp, convert_adp_gradient,
                                        convert_xyz_gradient)
@@ -256,7 +261,13 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     res = _Result()
     for k, v in out.items():
         setattr(res, k, _ptr(v, C.c_double))
-    rc = lib().sfo_compute(C.byref(pr), C.byref(res), int(n_threads))
+    if loop == "lines" and model == "hc":
+        hk = np.ascontiguousarray(np.asarray(hkl, dtype=np.int32).reshape(-1))
+        b3 = np.ascontiguousarray(bm[:, 2], dtype=np.float64)
+        rc = lib().sfo_compute_lines(C.byref(pr), hk.ctypes.data_as(_P(C.c_int)), b3.ctypes.data_as(_P(C.c_double)),
+                                     C.byref(res), int(n_threads))
+    else:
+        rc = lib().sfo_compute(C.byref(pr), C.byref(res), int(n_threads))
     if rc != 0:
         raise RuntimeError("oracle failed")
     f = (out["f"][0::2] + 1j * out["f"][1::2]) * mult

@@ -404,3 +404,414 @@ int sfo_compute(const sfo_problem *p, sfo_result *r, int n_threads)
     free(type_wfn);
     return 0;
 }
+
+/* ========================================================================
+ * Line-ordered evaluation of the HC model: the reference engine's own loop
+ * structure (HansenCoppens_SF_Engine3::calculateSF_Serial*, src/Scattering/
+ * HansenCoppens_SF_Engine3.cpp:1030-1509, 1511-1992, 2649-2894):
+ *   - reflections grouped in lattice lines (h, k, l), (h, k, l+1), ...
+ *     (scattering_utilities::splitHklLines, src/Scattering/scattering_utilities.cpp:463-517);
+ *   - per line: h' = h R and h.t per (reflection, operation), the harmonics of
+ *     h' in the crystal frame, the radial terms per (reflection, type);
+ *   - per (atom, operation): the phase factor and the anisotropic temperature
+ *     factor by recurrences along the line (calculate_line_phase_factors,
+ *     calculate_line_temperature_factors, scattering_utilities.cpp:575-756),
+ *     re-anchored every 32 reflections;
+ *   - P_lm rotated once per atom to the crystal frame
+ *     (calculateGlobalCoordinatesPlm, HansenCoppens_SF_Engine3.cpp:594-654),
+ *     here by a least-squares fit of the rotated harmonics over 40 directions.
+ * The CPU baseline of the benchmark; the same sums as sfo_compute.
+ * ======================================================================== */
+#define FIT_K 40
+static double fit_u[FIT_K][3];
+static double fit_pinv[5][9 * FIT_K];
+static int fit_ready = 0;
+
+static void fit_init(void)
+{
+    if (fit_ready) return;
+    const double ga = PI * (3.0 - sqrt(5.0));
+    for (int k = 0; k < FIT_K; k++) {
+        const double z = 1.0 - (2.0 * k + 1.0) / FIT_K, rr = sqrt(1.0 - z * z);
+        fit_u[k][0] = rr * cos(ga * k);
+        fit_u[k][1] = rr * sin(ga * k);
+        fit_u[k][2] = z;
+    }
+    for (int l = 0; l <= 4; l++) {
+        const int n = 2 * l + 1;
+        double A[FIT_K * 9], M[9 * 18];
+        for (int k = 0; k < FIT_K; k++) {
+            double v[25];
+            sfo_dlm(fit_u[k], v);
+            for (int m = 0; m < n; m++) A[k * n + m] = v[l * l + m];
+        }
+        /* [A^T A | I] -> [I | (A^T A)^-1] by Gauss-Jordan */
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < 2 * n; j++) {
+                double s = 0.0;
+                if (j < n)
+                    for (int k = 0; k < FIT_K; k++) s += A[k * n + i] * A[k * n + j];
+                else
+                    s = (j - n == i) ? 1.0 : 0.0;
+                M[i * 2 * n + j] = s;
+            }
+        for (int c = 0; c < n; c++) {
+            int piv = c;
+            for (int i = c + 1; i < n; i++)
+                if (fabs(M[i * 2 * n + c]) > fabs(M[piv * 2 * n + c])) piv = i;
+            for (int j = 0; j < 2 * n; j++) {
+                double t = M[c * 2 * n + j];
+                M[c * 2 * n + j] = M[piv * 2 * n + j];
+                M[piv * 2 * n + j] = t;
+            }
+            const double d = M[c * 2 * n + c];
+            for (int j = 0; j < 2 * n; j++) M[c * 2 * n + j] /= d;
+            for (int i = 0; i < n; i++)
+                if (i != c) {
+                    const double f = M[i * 2 * n + c];
+                    for (int j = 0; j < 2 * n; j++) M[i * 2 * n + j] -= f * M[c * 2 * n + j];
+                }
+        }
+        /* pinv = (A^T A)^-1 A^T : [n][K] */
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < FIT_K; k++) {
+                double s = 0.0;
+                for (int j = 0; j < n; j++) s += M[i * 2 * n + n + j] * A[k * n + j];
+                fit_pinv[l][i * FIT_K + k] = s;
+            }
+    }
+    fit_ready = 1;
+}
+
+/* D_l blocks (165 values, [i][j] per l) with d(L^T u) = D d(u) (L: columns = local axes) */
+static void rotation_blocks_cpu(const double *L, double *D)
+{
+    double B[FIT_K][25];
+    for (int k = 0; k < FIT_K; k++) {
+        double v[3];
+        for (int j = 0; j < 3; j++) v[j] = L[0 + j] * fit_u[k][0] + L[3 + j] * fit_u[k][1] + L[6 + j] * fit_u[k][2];
+        sfo_dlm(v, B[k]);
+    }
+    int off = 0;
+    for (int l = 0; l <= 4; l++) {
+        const int n = 2 * l + 1;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++) {
+                double s = 0.0;
+                for (int k = 0; k < FIT_K; k++) s += fit_pinv[l][j * FIT_K + k] * B[k][l * l + i];
+                D[off + i * n + j] = s;
+            }
+        off += n * n;
+    }
+}
+
+typedef struct { int h, k, l, idx; } hkl_key;
+static int hkl_cmp(const void *a, const void *b)
+{
+    const hkl_key *x = (const hkl_key *)a, *y = (const hkl_key *)b;
+    if (x->h != y->h) return x->h < y->h ? -1 : 1;
+    if (x->k != y->k) return x->k < y->k ? -1 : 1;
+    if (x->l != y->l) return x->l < y->l ? -1 : 1;
+    return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+
+int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sfo_result *r, int n_threads)
+{
+    if (p->model != SFO_MODEL_HC) return 2;
+    g_init();
+    fit_init();
+    const int nA = p->n_atoms, nH = p->n_hkl, nS = p->n_sym, nT = p->n_types > 0 ? p->n_types : 1;
+    const int nW = p->n_wfn > 0 ? p->n_wfn : 1;
+    if (n_threads < 1) n_threads = 1;
+#ifndef _OPENMP
+    n_threads = 1;
+#endif
+    /* lines */
+    hkl_key *key = (hkl_key *)malloc(sizeof(hkl_key) * (nH > 0 ? nH : 1));
+    for (int i = 0; i < nH; i++) {
+        key[i].h = hkl[3 * i]; key[i].k = hkl[3 * i + 1]; key[i].l = hkl[3 * i + 2]; key[i].idx = i;
+    }
+    qsort(key, nH, sizeof(hkl_key), hkl_cmp);
+    int *line_start = (int *)malloc(sizeof(int) * (nH + 1));
+    int n_lines = 0, max_len = 1;
+    for (int i = 0; i < nH; i++) {
+        const int cont = i > 0 && key[i].h == key[i - 1].h && key[i].k == key[i - 1].k && key[i].l == key[i - 1].l + 1;
+        if (!cont) line_start[n_lines++] = i;
+    }
+    line_start[n_lines] = nH;
+    for (int q = 0; q < n_lines; q++)
+        if (line_start[q + 1] - line_start[q] > max_len) max_len = line_start[q + 1] - line_start[q];
+    /* per atom: crystal-frame P_lm and rotation blocks */
+    int *type_wfn = (int *)malloc(sizeof(int) * nT);
+    for (int t = 0; t < nT; t++) type_wfn[t] = 0;
+    for (int a = 0; a < nA; a++) type_wfn[p->atom_type[a]] = p->atom_wfn[a];
+    double *pg = (double *)calloc((size_t)nA * 25, sizeof(double));
+    double *Dm = (double *)calloc((size_t)nA * 165, sizeof(double));
+    int *lmu = (int *)malloc(sizeof(int) * nA), *lmp = (int *)malloc(sizeof(int) * nA);
+    for (int a = 0; a < nA; a++) {
+        const int t = p->atom_type[a], w = p->atom_wfn[a];
+        lmu[a] = type_lmax_used(p, t, w);
+        lmp[a] = type_lmax_params(p, t, w);
+        rotation_blocks_cpu(p->lcs + 9 * a, Dm + 165 * (size_t)a);
+        int off = 0;
+        for (int l = 0; l <= 4; l++) {
+            const int n = 2 * l + 1;
+            if (l <= lmu[a])
+                for (int j = 0; j < n; j++) {
+                    double v = 0.0;
+                    for (int i = 0; i < n; i++) v += Dm[165 * (size_t)a + off + i * n + j] * p->type_plm[25 * t + l * l + i];
+                    pg[25 * (size_t)a + l * l + j] = v;
+                }
+            off += n * n;
+        }
+    }
+    double *acc = (double *)calloc((size_t)n_threads * nA * NCH, sizeof(double));
+    const int at_origin = p->inv_trans[0] == 0.0 && p->inv_trans[1] == 0.0 && p->inv_trans[2] == 0.0;
+
+#pragma omp parallel num_threads(n_threads)
+    {
+#ifdef _OPENMP
+        const int tid = omp_get_thread_num();
+#else
+        const int tid = 0;
+#endif
+        double *A = acc + (size_t)tid * nA * NCH;
+        const size_t L = (size_t)max_len;
+        double *hr = (double *)malloc(sizeof(double) * L * nS * 3);
+        double *tf = (double *)malloc(sizeof(double) * L * nS);
+        double *dd = (double *)malloc(sizeof(double) * L * nS * 25);
+        double *h2v = (double *)malloc(sizeof(double) * L);
+        double *fcore = (double *)malloc(sizeof(double) * L * nW);
+        double *fval = (double *)malloc(sizeof(double) * L * nT), *dfval = (double *)malloc(sizeof(double) * L * nT);
+        double *gl = (double *)malloc(sizeof(double) * L * nT * 5), *dgl = (double *)malloc(sizeof(double) * L * nT * 5);
+        cplx *gev = (cplx *)malloc(sizeof(cplx) * L), *Fl = (cplx *)malloc(sizeof(cplx) * L);
+        cplx *cinvv = (cplx *)malloc(sizeof(cplx) * L);
+        cplx *e = (cplx *)malloc(sizeof(cplx) * nS), *st = (cplx *)malloc(sizeof(cplx) * nS);
+        double *Tn = (double *)malloc(sizeof(double) * nS), *Tr = (double *)malloc(sizeof(double) * nS);
+        double *Trho = (double *)malloc(sizeof(double) * nS);
+        int *is000 = (int *)malloc(sizeof(int) * L);
+
+#pragma omp for schedule(dynamic, 4)
+        for (int q = 0; q < n_lines; q++) {
+            const int i0 = line_start[q], len = line_start[q + 1] - i0;
+            for (int j = 0; j < len; j++) {
+                const double *h = p->h + 3 * key[i0 + j].idx;
+                const double h2 = h[0] * h[0] + h[1] * h[1] + h[2] * h[2], hl = sqrt(h2);
+                h2v[j] = h2;
+                is000[j] = hl < 1e-10;
+                for (int s = 0; s < nS; s++) {
+                    const double *R = p->rot + 9 * s, *t = p->trans + 3 * s;
+                    double *x = hr + ((size_t)j * nS + s) * 3;
+                    for (int c = 0; c < 3; c++) x[c] = h[0] * R[c] + h[1] * R[3 + c] + h[2] * R[6 + c];
+                    tf[(size_t)j * nS + s] = h[0] * t[0] + h[1] * t[1] + h[2] * t[2];
+                    double *d = dd + ((size_t)j * nS + s) * 25;
+                    if (!is000[j]) {
+                        const double u[3] = {x[0] / hl, x[1] / hl, x[2] / hl};
+                        sfo_dlm(u, d);
+                    } else {
+                        for (int c = 0; c < 25; c++) d[c] = 0.0;
+                    }
+                }
+                for (int w = 0; w < p->n_wfn; w++) {
+                    double s = 0.0;
+                    for (int k = p->core_off[w]; k < p->core_off[w + 1]; k++)
+                        s += p->core_coeff[k] * sfo_g(0, p->core_pow[k] + 2, hl, p->core_exp[k]);
+                    fcore[(size_t)j * nW + w] = 4.0 * PI * s;
+                }
+                for (int ty = 0; ty < p->n_types; ty++) {
+                    const int w = type_wfn[ty];
+                    const double kap = p->type_kappa[ty], kp = p->type_kappa_p[ty];
+                    double s = 0.0, ds = 0.0;
+                    for (int k = p->val_off[w]; k < p->val_off[w + 1]; k++) {
+                        s += p->val_coeff[k] * sfo_g(0, p->val_pow[k] + 2, hl / kap, p->val_exp[k]);
+                        if (p->d_mp) ds += p->val_coeff[k] * g_dh(0, p->val_pow[k] + 2, hl / kap, p->val_exp[k]);
+                    }
+                    fval[(size_t)j * nT + ty] = 4.0 * PI * s;
+                    dfval[(size_t)j * nT + ty] = 4.0 * PI * ds * (-hl / (kap * kap));
+                    const double zeta = p->def_exp[w];
+                    for (int l = 0; l < 5; l++) {
+                        double gv = 0.0, dg = 0.0;
+                        if (l < p->def_npow[w]) {
+                            const int nl = p->def_pow[w * 5 + l];
+                            double norm = pow(zeta, nl + 3);
+                            for (int c = 2; c <= nl + 2; c++) norm /= c;
+                            gv = norm * sfo_g(l, nl + 2, hl / kp, zeta);
+                            if (p->d_mp) dg = norm * g_dh(l, nl + 2, hl / kp, zeta) * (-hl / (kp * kp));
+                        }
+                        gl[((size_t)j * nT + ty) * 5 + l] = gv;
+                        dgl[((size_t)j * nT + ty) * 5 + l] = dg;
+                    }
+                }
+                const cplx g = {p->dtdf[2 * key[i0 + j].idx], p->dtdf[2 * key[i0 + j].idx + 1]};
+                const double ph_inv = 2.0 * PI * (h[0] * p->inv_trans[0] + h[1] * p->inv_trans[1] + h[2] * p->inv_trans[2]);
+                cinvv[j].re = cos(ph_inv);
+                cinvv[j].im = sin(ph_inv);
+                cplx ge = g;
+                if (p->centro) {
+                    if (at_origin) { ge.re = 2.0 * g.re; ge.im = 0.0; }
+                    else ge = cadd(g, cconj(cmul(g, cinvv[j])));
+                }
+                gev[j] = ge;
+                Fl[j].re = Fl[j].im = 0.0;
+            }
+            const double *h0 = p->h + 3 * key[i0].idx;
+            for (int a = 0; a < nA; a++) {
+                if (!p->include[a]) continue;
+                const int w = p->atom_wfn[a], ty = p->atom_type[a], nadp = p->n_adp[a];
+                const double wgt = p->occ[a] * p->mult_w[a];
+                const double *adp = p->adp + 6 * a, *pos = p->pos + 3 * a, *P = pg + 25 * (size_t)a;
+                const double U[9] = {adp[0], adp[3], adp[4], adp[3], adp[1], adp[5], adp[4], adp[5], adp[2]};
+                cplx anom;
+                if (p->atom_anom) { anom.re = p->atom_anom[2 * a]; anom.im = p->atom_anom[2 * a + 1]; }
+                else { anom.re = p->wfn_anom[2 * w]; anom.im = p->wfn_anom[2 * w + 1]; }
+                double *Aa = A + (size_t)a * NCH;
+                for (int j = 0; j < len; j++) {
+                    cplx Us = {0, 0}, Ex = {0, 0}, Kp = {0, 0};
+                    cplx X[3] = {{0, 0}, {0, 0}, {0, 0}}, Ad[6] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}, {0, 0}};
+                    cplx Pd[25];
+                    if (p->d_mp)
+                        for (int c = 0; c < 25; c++) Pd[c].re = Pd[c].im = 0.0;
+                    const double fsph = fcore[(size_t)j * nW + w] + fval[(size_t)j * nT + ty] * p->type_pval[ty];
+                    for (int s = 0; s < nS; s++) {
+                        const double *hs = hr + ((size_t)j * nS + s) * 3;
+                        /* phase and temperature factor: exact at the line start and every 32 reflections,
+                         * otherwise one step of the recurrences */
+                        if (j % 32 == 0) {
+                            const double th = 2.0 * PI * (hs[0] * pos[0] + hs[1] * pos[1] + hs[2] * pos[2] + tf[(size_t)j * nS + s]);
+                            e[s].re = cos(th); e[s].im = sin(th);
+                            if (j == 0) {
+                                const double *R = p->rot + 9 * s, *t = p->trans + 3 * s;
+                                double d3[3];
+                                for (int c = 0; c < 3; c++) d3[c] = b3[0] * R[c] + b3[1] * R[3 + c] + b3[2] * R[6 + c];
+                                const double ps = 2.0 * PI * (d3[0] * pos[0] + d3[1] * pos[1] + d3[2] * pos[2] +
+                                                              b3[0] * t[0] + b3[1] * t[1] + b3[2] * t[2]);
+                                st[s].re = cos(ps); st[s].im = sin(ps);
+                                if (nadp == 6) {
+                                    double Ud[3];
+                                    for (int c = 0; c < 3; c++) Ud[c] = U[3 * c] * d3[0] + U[3 * c + 1] * d3[1] + U[3 * c + 2] * d3[2];
+                                    Trho[s] = exp(-2.0 * (d3[0] * Ud[0] + d3[1] * Ud[1] + d3[2] * Ud[2]));
+                                }
+                            }
+                            if (nadp == 6) {
+                                const double *R = p->rot + 9 * s;
+                                double d3[3], Uh[3], Ud[3];
+                                for (int c = 0; c < 3; c++) d3[c] = b3[0] * R[c] + b3[1] * R[3 + c] + b3[2] * R[6 + c];
+                                for (int c = 0; c < 3; c++) {
+                                    Uh[c] = U[3 * c] * hs[0] + U[3 * c + 1] * hs[1] + U[3 * c + 2] * hs[2];
+                                    Ud[c] = U[3 * c] * d3[0] + U[3 * c + 1] * d3[1] + U[3 * c + 2] * d3[2];
+                                }
+                                Tn[s] = exp(-(hs[0] * Uh[0] + hs[1] * Uh[1] + hs[2] * Uh[2]));
+                                Tr[s] = exp(-(2.0 * (hs[0] * Ud[0] + hs[1] * Ud[1] + hs[2] * Ud[2]) +
+                                              (d3[0] * Ud[0] + d3[1] * Ud[1] + d3[2] * Ud[2])));
+                            }
+                        }
+                        const cplx es = e[s];
+                        const double T = nadp == 6 ? Tn[s] : 1.0;
+                        /* advance to the next reflection of the line */
+                        e[s] = cmul(e[s], st[s]);
+                        if (nadp == 6) { Tn[s] *= Tr[s]; Tr[s] *= Trho[s]; }
+                        cplx f = {fsph + anom.re, anom.im};
+                        const double *d = dd + ((size_t)j * nS + s) * 25;
+                        double ang[5] = {0, 0, 0, 0, 0};
+                        if (!is000[j] && lmp[a] >= 0) {
+                            cplx fd = {0, 0};
+                            for (int l = 0; l <= lmu[a]; l++) {
+                                double sum = 0.0;
+                                for (int m = 0; m < 2 * l + 1; m++) sum += P[l * l + m] * d[l * l + m];
+                                ang[l] = sum;
+                                fd = cadd(fd, cscale(IPOW[l], 4.0 * PI * gl[((size_t)j * nT + ty) * 5 + l] * sum));
+                            }
+                            f = cadd(f, fd);
+                        }
+                        const cplx eT = cscale(es, T);
+                        const cplx u = cmul(f, eT);
+                        Us = cadd(Us, u);
+                        if (nadp == 6) {
+                            const double m6[6] = {hs[0] * hs[0], hs[1] * hs[1], hs[2] * hs[2], 2.0 * hs[0] * hs[1],
+                                                  2.0 * hs[0] * hs[2], 2.0 * hs[1] * hs[2]};
+                            for (int c = 0; c < 6; c++) Ad[c] = cadd(Ad[c], cscale(u, -m6[c]));
+                        }
+                        for (int c = 0; c < 3; c++) X[c] = cadd(X[c], cscale(u, hs[c]));
+                        if (p->d_mp) {
+                            Ex = cadd(Ex, eT);
+                            if (!is000[j] && lmp[a] >= 0) {
+                                for (int l = 0; l <= lmp[a]; l++)
+                                    for (int m = 0; m < 2 * l + 1; m++)
+                                        Pd[l * l + m] = cadd(Pd[l * l + m],
+                                            cmul(IPOW[l], cscale(eT, 4.0 * PI * gl[((size_t)j * nT + ty) * 5 + l] * d[l * l + m])));
+                                cplx kd = {0, 0};
+                                for (int l = 0; l <= lmu[a]; l++)
+                                    kd = cadd(kd, cscale(IPOW[l], 4.0 * PI * dgl[((size_t)j * nT + ty) * 5 + l] * ang[l]));
+                                Kp = cadd(Kp, cmul(kd, eT));
+                            }
+                        }
+                    }
+                    if (nadp == 1) {
+                        const double Ti = exp(-h2v[j] * adp[0]);
+                        Us = cscale(Us, Ti);
+                        for (int c = 0; c < 3; c++) X[c] = cscale(X[c], Ti);
+                        Ex = cscale(Ex, Ti);
+                        if (p->d_mp)
+                            for (int c = 0; c < 25; c++) Pd[c] = cscale(Pd[c], Ti);
+                        Kp = cscale(Kp, Ti);
+                    }
+                    Fl[j] = cadd(Fl[j], cscale(Us, wgt));
+                    const cplx ge = gev[j];
+                    if (p->d_occ) Aa[CH_OCC] += cmul(ge, Us).re * p->mult_w[a];
+                    if (p->d_adp) {
+                        if (nadp == 1) Aa[CH_ADP] += -h2v[j] * cmul(ge, Us).re * 2.0 * PI * PI * wgt;
+                        else if (nadp == 6)
+                            for (int c = 0; c < 6; c++) Aa[CH_ADP + c] += cmul(ge, Ad[c]).re * 2.0 * PI * PI * wgt;
+                    }
+                    if (p->d_xyz)
+                        for (int c = 0; c < 3; c++) Aa[CH_XYZ + c] += -cmul(ge, X[c]).im * 2.0 * PI * wgt;
+                    if (p->d_mp) {
+                        Aa[CH_PV] += cmul(ge, cscale(Ex, fval[(size_t)j * nT + ty])).re * wgt;
+                        Aa[CH_K] += cmul(ge, cscale(Ex, p->type_pval[ty] * dfval[(size_t)j * nT + ty])).re * wgt;
+                        for (int c = 0; c < 25; c++) Aa[CH_PLM + c] += cmul(ge, Pd[c]).re * wgt;  /* crystal frame */
+                        Aa[CH_KP] += cmul(ge, Kp).re * wgt;
+                    }
+                }
+            }
+            for (int j = 0; j < len; j++) {
+                cplx F = Fl[j];
+                if (p->centro) {
+                    if (at_origin) { F.re = 2.0 * F.re; F.im = 0.0; }
+                    else F = cadd(F, cmul(cinvv[j], cconj(F)));
+                }
+                r->f[2 * key[i0 + j].idx] = F.re;
+                r->f[2 * key[i0 + j].idx + 1] = F.im;
+            }
+            (void)h0;
+        }
+        free(hr); free(tf); free(dd); free(h2v); free(fcore); free(fval); free(dfval); free(gl); free(dgl);
+        free(gev); free(Fl); free(cinvv); free(e); free(st); free(Tn); free(Tr); free(Trho); free(is000);
+    }
+    for (int a = 0; a < nA; a++) {
+        double s[NCH];
+        for (int c = 0; c < NCH; c++) s[c] = 0.0;
+        for (int t = 0; t < n_threads; t++)
+            for (int c = 0; c < NCH; c++) s[c] += acc[((size_t)t * nA + a) * NCH + c];
+        if (r->d_xyz) for (int j = 0; j < 3; j++) r->d_xyz[3 * a + j] = s[CH_XYZ + j];
+        if (r->d_adp) for (int j = 0; j < 6; j++) r->d_adp[6 * a + j] = s[CH_ADP + j];
+        if (r->d_occ) r->d_occ[a] = s[CH_OCC];
+        if (r->d_pval) r->d_pval[a] = s[CH_PV];
+        if (r->d_kappa) r->d_kappa[a] = s[CH_K];
+        if (r->d_kappa_p) r->d_kappa_p[a] = s[CH_KP];
+        if (r->d_plm) {  /* back to the local frame: dT/dP_local = D dT/dP_glob, zero above the parameters' l */
+            const double *D = Dm + 165 * (size_t)a;
+            int off = 0;
+            for (int l = 0; l <= 4; l++) {
+                const int n = 2 * l + 1;
+                for (int i = 0; i < n; i++) {
+                    double v = 0.0;
+                    for (int j = 0; j < n; j++) v += D[off + i * n + j] * s[CH_PLM + l * l + j];
+                    r->d_plm[25 * a + l * l + i] = l <= lmp[a] ? v : 0.0;
+                }
+                off += n * n;
+            }
+        }
+    }
+    free(acc); free(pg); free(Dm); free(lmu); free(lmp); free(type_wfn); free(key); free(line_start);
+    return 0;
+}

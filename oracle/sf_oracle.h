@@ -91,6 +91,12 @@ typedef struct {
 /* Structure factors and target-function derivatives; returns 0 on success. */
 int sfo_compute(const sfo_problem *p, sfo_result *r, int n_threads);
 
+/* The same for the HC model in the reference engine's line-ordered loop
+ * (recurrences along (h, k, l) lines, harmonics per (reflection, operation),
+ * P_lm rotated once per atom): the benchmark's CPU baseline.  hkl: the
+ * integer indices of p->h; b3: the Cartesian third reciprocal axis. */
+int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sfo_result *r, int n_threads);
+
 /* int_0^inf r^n exp(-z r) j_l(2 pi h r) dr, 0<=l<=5, l+1<=n<=12 */
 double sfo_g(int l, int n, double h, double z);
 

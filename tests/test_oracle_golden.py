@@ -66,3 +66,22 @@ def test_oracle_is_deterministic_across_thread_counts():
     b = O.compute(st, n_threads=3)
     assert rel_f(a["f"], b["f"]) < 1e-15
     assert rel_norm(a["d_xyz"], b["d_xyz"]) < 1e-13
+
+
+@pytest.mark.parametrize("name", HC)
+def test_line_ordered_loop_matches_the_golden_fixtures(name):
+    # the benchmark's CPU baseline (the reference engine's line-ordered loop with recurrences)
+    st, d = load_fixture(name)
+    o = O.compute(st, multipoles=False, loop="lines")
+    assert rel_f(o["f"], d["ref_f"]) < 1e-12
+    assert rel_norm(o["d_xyz"], d["ref_d_xyz"]) < 1e-11
+    assert rel_norm(o["d_adp"], ref_adp_list(st, d)) < 1e-11
+    assert rel_norm(o["d_occ"], d["ref_d_occ"]) < 1e-11
+
+
+def test_line_ordered_loop_multipole_derivatives():
+    st, d = load_fixture("hc_multipole_fd")
+    a = O.compute(st, multipoles=True)
+    b = O.compute(st, multipoles=True, loop="lines")
+    for k in ("d_pval", "d_plm", "d_kappa", "d_kappa_p"):
+        assert rel_norm(b[k], a[k]) < 1e-11, k
