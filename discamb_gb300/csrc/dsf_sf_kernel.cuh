@@ -458,12 +458,15 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     for (int h0 = h_begin; h0 < h_end; h0 += ht, k++) {
         const int buf = k & 1;
         if (tid == 0 && h0 + ht < h_end) issue(buf ^ 1, h0 + ht);
-        const bool ok = mbar_wait(&bar[buf], parity[buf]);
+        const uint32_t phase = parity[buf];
+        const bool ok = mbar_wait(&bar[buf], phase);
         parity[buf] ^= 1u;
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
                 atomicOr(L.error, 1);
-                mbar_wait(&bar[buf ^ 1], parity[buf ^ 1]);  // bounded: let copies in flight land
+                // bounded: let this sub-tile's copies and the next one's (if issued) land first
+                mbar_wait(&bar[buf], phase);
+                if (h0 + ht < h_end) mbar_wait(&bar[buf ^ 1], parity[buf ^ 1]);
             }
             return;
         }
