@@ -115,6 +115,7 @@ def library():
         L.dsf_calculate_batch_atoms.argtypes = [_P(C.c_void_p), C.c_int, C.c_int, C.c_int, _P(C.c_void_p),
                                                 _P(C.c_void_p), _P(C.c_void_p), _P(C.c_void_p), _P(C.c_void_p),
                                                 _P(_Out)]
+        L.dsf_reduce_to_types.argtypes = [C.c_void_p, _P(_Out), _P(_Out), C.c_void_p]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
@@ -445,6 +446,17 @@ class HcCalculator(_Calculator):
         if upload_atoms:  # else the first call brings the atoms (calculate(..., atoms=...))
             self.update_atoms(st.xyz, st.adp, st.occupancy)
 
+    def reduce_to_types(self, per_atom, per_type, stream=0):
+        """TAAM types: sum the multipole derivatives of the atoms of each type
+        on the device (dsf_reduce_to_types); per_atom / per_type: dicts of
+        device pointers (d_pval, d_plm, d_kappa, d_kappa_prime)."""
+        a, t = _Out(), _Out()
+        for o, d in ((a, per_atom), (t, per_type)):
+            for k, v in d.items():
+                setattr(o, k, v)
+        self.engine.check(self.lib.dsf_reduce_to_types(self.h, C.byref(a), C.byref(t), C.c_void_p(stream)),
+                          "reduce_to_types")
+
     def update_types(self, plm=None, pval=None, kappa=None, kappa_prime=None):
         ps = [None if v is None else _d(np.asarray(v).reshape(-1)) for v in (plm, pval, kappa, kappa_prime)]
         args = [None if p is None else p[1] for p in ps]
@@ -516,3 +528,57 @@ def all_ops_mod_centering(sg):
         for c in cv:
             seen.add((r.tobytes(), tuple((np.array(t) + np.array(c)) % 12)))
     return np.array([r for r, _ in chosen]), np.array([t for _, t in chosen], dtype=np.float64) / 12.0
+
+
+class CombinedCalculator:
+    """Atoms split over several calculators, F summed and every atom's
+    derivatives taken from its own calculator, as
+    CombinedStructureFactorCalculator (include/discamb/Scattering/
+    CombinedStructureFactorCalculator.h:14-60; TAAM: multipolar atoms on the
+    HC model, the rest IAM, src/Scattering/HcAtomBankStructureFactorCalculator.cpp:482-499).
+    Each part is a calculator over its own atoms (no masked-out work); the
+    parts run in one batched submission."""
+
+    def __init__(self, engine, st, parts):
+        """parts: [(make, atom_indices)], make(substructure) -> calculator."""
+        self.engine = engine
+        self.st = st
+        self.parts = []
+        seen = np.zeros(st.n_atoms, dtype=int)
+        for make, idx in parts:
+            idx = np.asarray(idx, dtype=np.int64)
+            seen[idx] += 1
+            sub = st.subset(idx)
+            self.parts.append((make(sub), idx))
+        if not np.all(seen == 1):
+            raise DsfError("every atom must belong to exactly one part")
+
+    def calculate(self, dtdf, precision=DSF_FP64, derivatives=("xyz", "adp", "occ"), atoms=None):
+        calcs = [c for c, _ in self.parts]
+        at = None
+        if atoms is not None:
+            xyz, adp, occ = atoms
+            xyz = np.asarray(xyz).reshape(-1, 3)
+            adp6 = adp if isinstance(adp, np.ndarray) and adp.shape == (self.st.n_atoms, 6) else None
+            if adp6 is None:
+                adp6 = np.zeros((self.st.n_atoms, 6))
+                for i, a in enumerate(adp):
+                    adp6[i, :len(a)] = a
+            occ = np.asarray(occ)
+            at = [(xyz[idx], adp6[idx], occ[idx]) for _, idx in self.parts]
+        res = self.engine.calculate_batch(calcs, [dtdf] * len(calcs), precision=precision, derivatives=derivatives,
+                                          atoms=at)
+        n = self.st.n_atoms
+        f = np.zeros(len(self.st.hkl), dtype=np.complex128)
+        d_xyz, d_adp, d_occ = np.zeros((n, 3)), np.zeros((n, 6)), np.zeros(n)
+        for (c, idx), r in zip(self.parts, res):
+            f += r["f"]
+            d_xyz[idx] = r["d_xyz"]
+            d_adp[idx] = r["d_adp"]
+            d_occ[idx] = r["d_occ"]
+        nadp = self.st.n_adp()
+        return dict(f=f, d_xyz=d_xyz, d_adp=[d_adp[i, :nadp[i]] for i in range(n)], d_occ=d_occ)
+
+    def close(self):
+        for c, _ in self.parts:
+            c.close()

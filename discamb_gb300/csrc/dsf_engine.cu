@@ -371,6 +371,28 @@ __global__ void grad_epilogue_kernel(GradParams P, const double *g_acc, const in
                           d_kappa, d_kappa_p);
 }
 
+// multipole-parameter derivatives summed over the atoms of each type (atoms of
+// one type share P_val, P_lm in their local frames, kappa, kappa'); inputs and
+// outputs in the caller's (original) atom order
+__global__ void type_reduce_kernel(int n_atoms, int n_types, const int *atom_type, const double *pv, const double *plm,
+                                   const double *ka, const double *kp, double *tpv, double *tplm, double *tka,
+                                   double *tkp)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_atoms * 28) return;
+    const int a = i / 28, q = i - a * 28, t = atom_type[a];
+    if (t < 0 || t >= n_types) return;
+    if (q < 25) {
+        if (plm && tplm) atomicAdd(&tplm[25 * (size_t)t + q], plm[25 * (size_t)a + q]);
+    } else if (q == 25) {
+        if (pv && tpv) atomicAdd(&tpv[t], pv[a]);
+    } else if (q == 26) {
+        if (ka && tka) atomicAdd(&tka[t], ka[a]);
+    } else {
+        if (kp && tkp) atomicAdd(&tkp[t], kp[a]);
+    }
+}
+
 // the per-structure work of a batched submission before and after the SF
 // kernels, for up to kPrePostItems structures per launch (kernel-parameter
 // space): block row blockIdx.y is one structure, grid-stride over its
@@ -2152,6 +2174,27 @@ static int calculate_host(dsf_structure *s, int precision, int flags, const doub
     if ((rc = host_readback(s, flags, hc))) return rc;
     DSF_CUDA(cudaStreamSynchronize(e->stream));
     return host_finish(s, flags, hc, out);
+}
+
+int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf_outputs *per_type, void *stream)
+{
+    if (!s || !per_atom || !per_type) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (s->model != MODEL_HC) return fail(e, DSF_ERR_STATE, "multipole parameters exist only for HC structures");
+    cudaSetDevice(e->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    const int nT = s->n_types, n = s->n_atoms;
+    if (per_type->d_pval) DSF_CUDA(cudaMemsetAsync(per_type->d_pval, 0, sizeof(double) * nT, st));
+    if (per_type->d_plm) DSF_CUDA(cudaMemsetAsync(per_type->d_plm, 0, sizeof(double) * 25 * (size_t)nT, st));
+    if (per_type->d_kappa) DSF_CUDA(cudaMemsetAsync(per_type->d_kappa, 0, sizeof(double) * nT, st));
+    if (per_type->d_kappa_prime) DSF_CUDA(cudaMemsetAsync(per_type->d_kappa_prime, 0, sizeof(double) * nT, st));
+    type_reduce_kernel<<<(n * 28 + 255) / 256, 256, 0, st>>>(n, nT, s->d_atom_type0.as<int>(), per_atom->d_pval,
+                                                            per_atom->d_plm, per_atom->d_kappa,
+                                                            per_atom->d_kappa_prime, per_type->d_pval,
+                                                            per_type->d_plm, per_type->d_kappa,
+                                                            per_type->d_kappa_prime);
+    DSF_CUDA(cudaGetLastError());
+    return DSF_OK;
 }
 
 int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int flags,

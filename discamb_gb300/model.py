@@ -18,7 +18,7 @@ These mirror the reference's inputs to ``HansenCoppensStructureFactorCalculator`
 """
 from __future__ import annotations
 
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 import math
 
 import numpy as np
@@ -126,6 +126,24 @@ class Structure:
         if self.include is None:
             return np.ones(self.n_atoms, dtype=bool)
         return np.asarray(self.include, dtype=bool)
+
+    def subset(self, idx):
+        """The structure of the atoms idx (same cell, symmetry, reflections and
+        dT/dF), with its wavefunctions and types renumbered to the ones used."""
+        idx = np.asarray(idx, dtype=np.int64)
+        used_t = sorted(set(int(t) for t in self.atom_type[idx]))
+        used_w = sorted(set(int(w) for w in self.atom_wfn[idx]))
+        tmap = {t: i for i, t in enumerate(used_t)}
+        wmap = {w: i for i, w in enumerate(used_w)}
+        return replace(self, xyz=np.asarray(self.xyz)[idx].copy(), adp=[list(self.adp[i]) for i in idx],
+                       occupancy=np.asarray(self.occupancy)[idx].copy(),
+                       multiplicity=np.asarray(self.multiplicity)[idx].copy(),
+                       atom_wfn=np.array([wmap[int(w)] for w in self.atom_wfn[idx]], dtype=np.int32),
+                       atom_type=np.array([tmap[int(t)] for t in self.atom_type[idx]], dtype=np.int32),
+                       lcs=np.asarray(self.lcs)[idx].copy(), wfns=[self.wfns[w] for w in used_w],
+                       types=[self.types[t] for t in used_t],
+                       anomalous=None if self.anomalous is None else np.asarray(self.anomalous)[idx].copy(),
+                       include=None if self.include is None else np.asarray(self.include)[idx].copy())
 
     def frac_to_cart(self):
         return frac_to_cart_matrix(self.cell)

@@ -30,6 +30,7 @@
  *   dsf_calculate_batch, dsf_calculate_batch_atoms, dsf_calculate_batch_device
  *                               many structures in one submission (the reference's callers run one
  *                               calculator per structure in turn, HcAtomBankStructureFactorCalculator.cpp:482-520)
+ *   dsf_reduce_to_types         per-type multipole derivatives for TAAM callers (no reference counterpart)
  *   dsf_last_error              on_error::throwException messages (include/discamb/BasicUtilities/on_error.h:24-36):
  *                               every function returns a status instead of throwing; the message is the
  *                               calling thread's last one
@@ -205,6 +206,11 @@ int dsf_calculate_device(dsf_structure *s, int precision, int derivative_flags, 
  * calculator per structure, SfCalculator.h:45-67, called in turn by its callers). */
 int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int precision, int derivative_flags,
                                const double *const *dtdf_device, const dsf_outputs *out_device, void *stream);
+/* TAAM-style types: the multipole-parameter derivatives of dsf_calculate_device (per_atom: device buffers in the
+ * caller's atom order) summed over the atoms of each type into per_type (device buffers [n_types], [n_types][25];
+ * NULL members are skipped); asynchronous on `stream`.  The reference computes no multipole derivatives; its TAAM
+ * callers refine per-type parameters (HcAtomBankStructureFactorCalculator.cpp:482-520). */
+int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf_outputs *per_type, void *stream);
 /* the same with host buffers (dtdf[i] [n_hkl_i][2], include[i] NULL = all atoms, outputs on the host); one
  * stream synchronisation for the whole batch */
 int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int derivative_flags,

@@ -184,3 +184,61 @@ def test_tabulated_batch_device_path(engine):
         assert rel_norm(o["d_xyz"].cpu().numpy(), ref["d_xyz"]) < 1e-5
     for c in calcs:
         c.close()
+
+
+def test_combined_hc_and_iam_atoms(engine):
+    # TAAM-style split: multipolar atoms on the HC model, the others IAM
+    st = W.small_case("P21/c", n_atoms=9, stol_max=0.5, seed=470)
+    hc_idx, iam_idx = [0, 1, 2, 4, 7], [3, 5, 6, 8]
+    sub_iam = st.subset(iam_idx)
+    ntype = int(sub_iam.atom_type.max()) + 1
+    rng = np.random.default_rng(8)
+    iam = dict(ngauss=np.full(ntype, 4, np.int32), a=rng.uniform(0.5, 3, (ntype, 5)),
+               b=rng.uniform(0.5, 30, (ntype, 5)), c=rng.uniform(0, 0.5, ntype))
+    comb = api.CombinedCalculator(engine, st, [(lambda s: api.HcCalculator(engine, s), hc_idx),
+                                               (lambda s: api.IamCalculator(engine, s, iam), iam_idx)])
+    xyz = st.xyz + 0.002
+    for prec, tf, tg in ((FP64, 1e-10, 1e-10), (FP32, 1e-6, 1e-5)):
+        r = comb.calculate(st.dtdf, precision=prec, atoms=(xyz, st.adp, st.occupancy))
+        s1, s2 = st.subset(hc_idx), st.subset(iam_idx)
+        s1.xyz, s2.xyz = xyz[hc_idx], xyz[iam_idx]
+        o1, o2 = O.compute(s1), O.compute(s2, model="iam", iam=iam)
+        assert rel_f(r["f"], o1["f"] + o2["f"]) < tf
+        ref_xyz = np.zeros((st.n_atoms, 3))
+        ref_xyz[hc_idx], ref_xyz[iam_idx] = o1["d_xyz"], o2["d_xyz"]
+        assert rel_norm(r["d_xyz"], ref_xyz) < tg
+        ref_adp = [None] * st.n_atoms
+        for k, i in enumerate(hc_idx):
+            ref_adp[i] = o1["d_adp"][k]
+        for k, i in enumerate(iam_idx):
+            ref_adp[i] = o2["d_adp"][k]
+        assert rel_norm(r["d_adp"], ref_adp) < tg
+    comb.close()
+
+
+def test_multipole_derivatives_reduced_to_types(engine):
+    torch = pytest.importorskip("torch")
+    st = W.build_structure(cell=(11.0, 12.0, 13.0, 90.0, 101.0, 90.0), sg_symbol="P21/c",
+                           elements=["C", "C", "N", "O", "C", "N", "O", "C", "H", "H"],
+                           rng=np.random.default_rng(480), n_types=5, stol_max=0.5)
+    calc = api.HcCalculator(engine, st)
+    dev = torch.device("cuda", 0)
+    n, nt = st.n_atoms, len(st.types)
+    g = torch.tensor(np.stack([st.dtdf.real, st.dtdf.imag], 1), dtype=torch.float64, device=dev)
+    f = torch.zeros(st.n_hkl, 2, dtype=torch.float64, device=dev)
+    pa = {k: torch.zeros(n, w, dtype=torch.float64, device=dev)
+          for k, w in (("d_pval", 1), ("d_plm", 25), ("d_kappa", 1), ("d_kappa_prime", 1))}
+    pt = {k: torch.zeros(nt, w, dtype=torch.float64, device=dev)
+          for k, w in (("d_pval", 1), ("d_plm", 25), ("d_kappa", 1), ("d_kappa_prime", 1))}
+    torch.cuda.synchronize()
+    calc.calculate_device(g.data_ptr(), {"f": f.data_ptr(), **{k: v.data_ptr() for k, v in pa.items()}},
+                          precision=FP64, derivatives=(), multipoles=True)
+    calc.reduce_to_types({k: v.data_ptr() for k, v in pa.items()}, {k: v.data_ptr() for k, v in pt.items()})
+    torch.cuda.synchronize()
+    o = O.compute(st, multipoles=True)
+    for k, ko in (("d_pval", "d_pval"), ("d_plm", "d_plm"), ("d_kappa", "d_kappa"), ("d_kappa_prime", "d_kappa_p")):
+        ref = np.zeros((nt,) + np.asarray(o[ko]).shape[1:])
+        np.add.at(ref, st.atom_type, np.asarray(o[ko]))
+        got = pt[k].cpu().numpy().reshape(ref.shape)
+        assert rel_norm(got, ref) < 1e-10, k
+    calc.close()
