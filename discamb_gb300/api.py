@@ -116,6 +116,7 @@ def library():
                                                 _P(C.c_void_p), _P(C.c_void_p), _P(C.c_void_p), _P(C.c_void_p),
                                                 _P(_Out)]
         L.dsf_reduce_to_types.argtypes = [C.c_void_p, _P(_Out), _P(_Out), C.c_void_p]
+        L.dsf_structure_set_electron.argtypes = [C.c_void_p, C.c_int, _P(C.c_int), _P(C.c_double)]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
@@ -445,6 +446,16 @@ class HcCalculator(_Calculator):
         self.set_hkl(st.hkl)
         if upload_atoms:  # else the first call brings the atoms (calculate(..., atoms=...))
             self.update_atoms(st.xyz, st.adp, st.occupancy)
+
+    def set_electron(self, on=True, f000=None):
+        """Electron scattering (Mott-Bethe) for every form factor; f000[w]:
+        the electron scattering factor at s = 0 of wavefunction w's element."""
+        if on:
+            z, pz = _i(np.array([w.atomic_number for w in self.st.wfns], dtype=np.int32))
+            f0, pf = _d(np.asarray(f000, dtype=np.float64))
+        else:
+            pz = pf = None
+        self.engine.check(self.lib.dsf_structure_set_electron(self.h, int(bool(on)), pz, pf), "set_electron")
 
     def reduce_to_types(self, per_atom, per_type, stream=0):
         """TAAM types: sum the multipole derivatives of the atoms of each type

@@ -39,10 +39,12 @@ struct TypeRadialT {
     int core_begin, core_end, val_begin, val_end;  // into the density-term arrays
     int iam_n;
     R iam_a[5], iam_b[5], iam_c;
+    R e_z, e_f000;      // electron scattering: atomic number, f_e at h = 0
 };
 
 struct DevStructure {
     int model;
+    int electron;                // HC form factors converted to electron scattering (Mott-Bethe)
     int n_atoms, n_hkl, n_sym, n_tiles, n_types;
     double B[9];                 // h_cart = B h_frac (row-major)
     float Bf[9];

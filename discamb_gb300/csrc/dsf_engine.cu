@@ -57,6 +57,7 @@ struct TypeHost {
     int core_begin = 0, core_end = 0, val_begin = 0, val_end = 0;
     int iam_n = 0;
     double iam_a[5] = {0, 0, 0, 0, 0}, iam_b[5] = {0, 0, 0, 0, 0}, iam_c = 0;
+    double e_z = 0, e_f000 = 0;  // electron scattering: atomic number and f_e(0) of the type's wavefunction
 };
 }  // namespace
 
@@ -195,6 +196,7 @@ struct dsf_structure {
     // HC: operations ordered in cosets of coset_size (0: no such order) within
     // which they differ by a sign-diagonal Cartesian map of the reciprocal
     // vector; sym_sign: that map's signs relative to the coset's first operation
+    int electron = 0;            // HC: Mott-Bethe electron scattering
     int coset_size = 0;
     std::vector<int> sym_sign;   // [n_sym][3] Cartesian
     std::vector<int> sym_fsign;  // [n_sym][3] fractional h' components
@@ -955,6 +957,8 @@ TypeRadialT<R> type_constants(const TypeHost &h)
             t.def_pre[l] = R(sgn * 4.0 * DSF_PI * h.norm[l] * g_prefactor(l, m));
         }
     }
+    t.e_z = R(h.e_z);
+    t.e_f000 = R(h.e_f000);
     t.core_begin = h.core_begin;
     t.core_end = h.core_end;
     t.val_begin = h.val_begin;
@@ -987,6 +991,7 @@ void refresh_dev(dsf_structure *s)
 {
     DevStructure &d = s->dev;
     d.model = s->model;
+    d.electron = s->electron;
     d.n_atoms = s->n_atoms;
     d.n_hkl = s->n_hkl;
     d.n_sym = s->n_sym;
@@ -1636,6 +1641,27 @@ int dsf_structure_update_types(dsf_structure *s, const double *plm, const double
     if ((rc = ensure_tables(s, false, false))) return rc;
     refresh_dev(s);
     DSF_CUDA(cudaStreamSynchronize(e->setup));
+    return DSF_OK;
+}
+
+int dsf_structure_set_electron(dsf_structure *s, int on, const int *wfn_z, const double *wfn_f000)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (s->model != MODEL_HC) return fail(e, DSF_ERR_STATE, "electron conversion applies to HC structures");
+    if (on && (!wfn_z || !wfn_f000)) return fail(e, DSF_ERR_ARGUMENT, "atomic numbers and f_e(0) are required");
+    cudaSetDevice(e->device);
+    for (int t = 0; t < s->n_types; t++) {
+        const int w = s->type_wfn[t];
+        s->trad[t].e_z = on ? (double)wfn_z[w] : 0.0;
+        s->trad[t].e_f000 = on ? wfn_f000[w] : 0.0;
+    }
+    s->electron = on ? 1 : 0;
+    int rc;
+    if ((rc = upload_types(s))) return rc;
+    refresh_dev(s);
+    for (int p = 0; p < 2; p++) s->tr_ok[p] = s->trm_ok[p] = false;
+    if ((rc = ensure_tables(s, false, false))) return rc;
     return DSF_OK;
 }
 

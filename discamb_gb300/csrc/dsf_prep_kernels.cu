@@ -121,6 +121,29 @@ __device__ void radial_terms2(const DevStructure &S, const TypeRadialT<R> &t, R 
     }
 }
 
+// Mott-Bethe conversion of the X-ray form factor of an HC type to electron
+// scattering, as the reference engine does per term (HansenCoppens_SF_Engine3.cpp:1387-1397):
+// f_e = C (Z - f_x) / s^2 with s^2 = |h|^2 / 4 and C = 0.023934 (the anomalous
+// term stays additive), f_e(000) = the element's electron f at s = 0.  Linear in
+// f_x, so the deformation radial terms and the multipole-adjoint terms scale by
+// -C / s^2 (zero at 000).  Evaluated in FP64 for both table precisions: Z - f_x
+// cancels at low angle.
+__device__ void electron_terms(const DevStructure &S, int t, double h2, double *base, double *mpv, bool mp)
+{
+    const TypeRadialT<double> &ty = S.types_d[t];
+    radial_terms2<double>(S, ty, h2, base, mpv, mp);
+    if (h2 > 0.0) {
+        const double s2 = 0.25 * h2, c = 0.023934;
+        base[0] = c * (ty.e_z - base[0]) / s2;
+        for (int q = 1; q < 8; q++) base[q] *= -c / s2;
+        for (int q = 0; q < 8; q++) mpv[q] *= -c / s2;
+    } else {
+        base[0] = ty.e_f000;
+        for (int q = 1; q < 8; q++) base[q] = 0.0;
+        for (int q = 0; q < 8; q++) mpv[q] = 0.0;
+    }
+}
+
 template <typename R>
 __global__ void tr_prep_kernel(DevStructure S, int n_hkl_pad, R *tr, R *trm, int mp)
 {
@@ -128,7 +151,14 @@ __global__ void tr_prep_kernel(DevStructure S, int n_hkl_pad, R *tr, R *trm, int
     const int t = blockIdx.y;
     if (h >= n_hkl_pad) return;
     R base[8], mpv[8];
-    if (h < S.n_hkl) {
+    if (h < S.n_hkl && S.electron && S.model == MODEL_HC) {
+        double bd[8], md[8];
+        electron_terms(S, t, S.h2[h], bd, md, mp != 0);
+        for (int q = 0; q < 8; q++) {
+            base[q] = R(bd[q]);
+            mpv[q] = R(md[q]);
+        }
+    } else if (h < S.n_hkl) {
         const R h2 = R(S.h2[h]);
         radial_terms2<R>(S, SelP<R>::types(S)[t], h2, base, mpv, mp != 0);
     } else {

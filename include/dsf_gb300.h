@@ -30,6 +30,7 @@
  *   dsf_calculate_batch, dsf_calculate_batch_atoms, dsf_calculate_batch_device
  *                               many structures in one submission (the reference's callers run one
  *                               calculator per structure in turn, HcAtomBankStructureFactorCalculator.cpp:482-520)
+ *   dsf_structure_set_electron  HansenCoppensStructureFactorCalculator::setElectronScattering
  *   dsf_reduce_to_types         per-type multipole derivatives for TAAM callers (no reference counterpart)
  *   dsf_last_error              on_error::throwException messages (include/discamb/BasicUtilities/on_error.h:24-36):
  *                               every function returns a status instead of throwing; the message is the
@@ -206,6 +207,11 @@ int dsf_calculate_device(dsf_structure *s, int precision, int derivative_flags, 
  * calculator per structure, SfCalculator.h:45-67, called in turn by its callers). */
 int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int precision, int derivative_flags,
                                const double *const *dtdf_device, const dsf_outputs *out_device, void *stream);
+/* electron scattering for an HC structure (the reference's setElectronScattering,
+ * HansenCoppensStructureFactorCalculator.cpp:510-514): every form factor converted by Mott-Bethe,
+ * f_e = 0.023934 (Z - f_x) / s^2 + f'' terms, f_e(000) = wfn_f000 (the element's electron scattering factor at s = 0,
+ * which the reference takes from its "electron-IT" table); wfn_z, wfn_f000: [n_wfn]; on = 0 switches back to X-rays */
+int dsf_structure_set_electron(dsf_structure *s, int on, const int *wfn_z, const double *wfn_f000);
 /* TAAM-style types: the multipole-parameter derivatives of dsf_calculate_device (per_atom: device buffers in the
  * caller's atom order) summed over the atoms of each type into per_type (device buffers [n_types], [n_types][25];
  * NULL members are skipped); asynchronous on `stream`.  The reference computes no multipole derivatives; its TAAM

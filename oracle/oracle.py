@@ -58,6 +58,7 @@ class _Problem(C.Structure):
         ("centro", C.c_int), ("inv_trans", C.c_double * 3),
         ("n_hkl", C.c_int), ("h", _P(C.c_double)), ("dtdf", _P(C.c_double)),
         ("d_xyz", C.c_int), ("d_adp", C.c_int), ("d_occ", C.c_int), ("d_mp", C.c_int),
+        ("electron", C.c_int), ("wfn_z", _P(C.c_int)), ("wfn_f000", _P(C.c_double)),
     ]
 
 
@@ -157,7 +158,7 @@ def hc_model_arrays(st):
 
 
 def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), multipoles=False,
-            iam=None, table=None, hkl_subset=None, loop="direct"):
+            iam=None, table=None, hkl_subset=None, loop="direct", electron_f000=None):
     """F and dT/dparam for a Structure at the API level (crystal conventions).
 
     model: 'hc' (HansenCoppens engine: symmetry subset, inversion and
@@ -169,6 +170,8 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     loop: 'direct' (every term evaluated directly) or, for the HC model,
     'lines' (the reference engine's line-ordered loop with recurrences: the
     benchmark's CPU baseline).
+    electron_f000: per wavefunction, the electron scattering factor at s = 0;
+    given, the HC form factors are converted to electron scattering.
     """
     from discamb_gb300.crystal import (centering_multipliers, convert_adp, convert_adp_gradient,
                                        convert_xyz_gradient)
@@ -256,6 +259,10 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     pr.d_adp = int("adp" in derivatives)
     pr.d_occ = int("occ" in derivatives)
     pr.d_mp = int(bool(multipoles))
+    if electron_f000 is not None and model == "hc":
+        pr.electron = 1
+        pr.wfn_z = keep.i(np.array([w.atomic_number for w in st.wfns], dtype=np.int32))
+        pr.wfn_f000 = keep.d(np.asarray(electron_f000, dtype=np.float64))
     out = dict(f=np.zeros(2 * len(hkl)), d_xyz=np.zeros(3 * n), d_adp=np.zeros(6 * n), d_occ=np.zeros(n),
                d_pval=np.zeros(n), d_plm=np.zeros(25 * n), d_kappa=np.zeros(n), d_kappa_p=np.zeros(n))
     res = _Result()

@@ -13,6 +13,7 @@
 //     (the AnyIamCalculator path, src/Scattering/AnyIamCalculator.cpp:49-154);
 //   * AnyScattererStructureFactorCalculator + ConstFormFactorCalculationsManager
 //     (the tabulated path behind TscFileBasedSfCalculator).
+#include "discamb/BasicChemistry/periodic_table.h"
 #include "discamb/CrystalStructure/Crystal.h"
 #include "discamb/CrystalStructure/SpaceGroup.h"
 #include "discamb/CrystalStructure/SpaceGroupOperation.h"
@@ -99,6 +100,14 @@ extern "C" {
 
 const char *ref_last_error(void) { return g_last_error.c_str(); }
 
+// electron scattering (Mott-Bethe conversion inside the engine) for the following ref_hc_sf calls
+static bool g_electron = false;
+int ref_set_electron(int on)
+{
+    g_electron = on != 0;
+    return 0;
+}
+
 // Hansen-Coppens path through HansenCoppensStructureFactorCalculator ("CPU").
 // Wavefunctions as Slater orbitals: per wfn [orb_off[w], orb_off[w+1]) orbitals,
 // per orbital [sto_off[o], sto_off[o+1]) Slater functions.
@@ -115,7 +124,11 @@ int ref_hc_sf(const double *cell, const char *ops, int n_atoms, const double *xy
               int n_threads, double *f_out, double *d_xyz, double *d_adp, double *d_occ, double *ms)
 {
     try {
-        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, nullptr};
+        // atom type labels = element symbols of the atoms' wavefunctions (the engine takes the atomic numbers
+        // for electron scattering from them, crystal_structure_utilities::atomicNumbers)
+        std::string types;
+        for (int a = 0; a < n_atoms; a++) types += periodic_table::symbol(wfn_z[atom_wfn[a]]) + ";";
+        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, types.c_str()};
         Crystal crystal = make_crystal(in);
         HC_ModelParameters p;
         p.wfn_parameters.resize(n_wfn);
@@ -159,6 +172,7 @@ int ref_hc_sf(const double *cell, const char *ops, int n_atoms, const double *xy
         HansenCoppensStructureFactorCalculator calc(crystal, p);
         calc.setCalculationMode("CPU");
         calc.setN_Threads(n_threads);
+        calc.setElectronScattering(g_electron);
         if (atom_anom) {
             vector<complex<double> > an(n_atoms);
             for (int a = 0; a < n_atoms; a++) an[a] = complex<double>(atom_anom[2 * a], atom_anom[2 * a + 1]);

@@ -262,6 +262,8 @@ int sfo_compute(const sfo_problem *p, sfo_result *r, int n_threads)
                 if (at_origin) { ge.re = 2.0 * g.re; ge.im = 0.0; }
                 else ge = cadd(g, cconj(cmul(g, cinv)));
             }
+            /* electron scattering: f_e = C (Z - f_x) / s^2 + anomalous, linear in f_x with slope -C/s^2 */
+            const double esc = (p->electron && p->model == SFO_MODEL_HC) ? (h000 ? 0.0 : -0.023934 / (0.25 * h2)) : 1.0;
             cplx Ftot = {0, 0};
             for (int a = 0; a < nA; a++) {
                 if (!p->include[a]) continue;
@@ -325,6 +327,13 @@ int sfo_compute(const sfo_problem *p, sfo_result *r, int n_threads)
                         }
                         f = cadd(f, fd);
                     }
+                    if (p->electron && p->model == SFO_MODEL_HC) {
+                        if (h000) { f.re = p->wfn_f000[w] + anom.re; f.im = anom.im; }
+                        else {
+                            f.re = esc * (f.re - anom.re) - esc * p->wfn_z[w] + anom.re;
+                            f.im = esc * (f.im - anom.im) + anom.im;
+                        }
+                    }
                     cplx eT = cscale(e, T);
                     cplx u_s = cmul(f, eT);
                     U = cadd(U, u_s);
@@ -371,10 +380,10 @@ int sfo_compute(const sfo_problem *p, sfo_result *r, int n_threads)
                     for (int j = 0; j < 3; j++)
                         Aa[CH_XYZ + j] += -cmul(ge, X[j]).im * 2.0 * PI * wgt;
                 if (p->d_mp && p->model == SFO_MODEL_HC) {
-                    Aa[CH_PV] += cmul(ge, cscale(Ex, fval[ty])).re * wgt;
-                    Aa[CH_K] += cmul(ge, cscale(Ex, p->type_pval[ty] * dfval[ty])).re * wgt;
-                    for (int q = 0; q < 25; q++) Aa[CH_PLM + q] += cmul(ge, Pd[q]).re * wgt;
-                    Aa[CH_KP] += cmul(ge, Kp).re * wgt;
+                    Aa[CH_PV] += cmul(ge, cscale(Ex, esc * fval[ty])).re * wgt;
+                    Aa[CH_K] += cmul(ge, cscale(Ex, esc * p->type_pval[ty] * dfval[ty])).re * wgt;
+                    for (int q = 0; q < 25; q++) Aa[CH_PLM + q] += esc * cmul(ge, Pd[q]).re * wgt;
+                    Aa[CH_KP] += esc * cmul(ge, Kp).re * wgt;
                 }
             }
             if (p->centro) {
@@ -672,6 +681,7 @@ int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sf
                     if (p->d_mp)
                         for (int c = 0; c < 25; c++) Pd[c].re = Pd[c].im = 0.0;
                     const double fsph = fcore[(size_t)j * nW + w] + fval[(size_t)j * nT + ty] * p->type_pval[ty];
+                    const double esc = p->electron ? (is000[j] ? 0.0 : -0.023934 / (0.25 * h2v[j])) : 1.0;
                     for (int s = 0; s < nS; s++) {
                         const double *hs = hr + ((size_t)j * nS + s) * 3;
                         /* phase and temperature factor: exact at the line start and every 32 reflections,
@@ -723,6 +733,13 @@ int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sf
                             }
                             f = cadd(f, fd);
                         }
+                        if (p->electron) {
+                            if (is000[j]) { f.re = p->wfn_f000[w] + anom.re; f.im = anom.im; }
+                            else {
+                                f.re = esc * (f.re - anom.re) - esc * p->wfn_z[w] + anom.re;
+                                f.im = esc * (f.im - anom.im) + anom.im;
+                            }
+                        }
                         const cplx eT = cscale(es, T);
                         const cplx u = cmul(f, eT);
                         Us = cadd(Us, u);
@@ -766,10 +783,10 @@ int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sf
                     if (p->d_xyz)
                         for (int c = 0; c < 3; c++) Aa[CH_XYZ + c] += -cmul(ge, X[c]).im * 2.0 * PI * wgt;
                     if (p->d_mp) {
-                        Aa[CH_PV] += cmul(ge, cscale(Ex, fval[(size_t)j * nT + ty])).re * wgt;
-                        Aa[CH_K] += cmul(ge, cscale(Ex, p->type_pval[ty] * dfval[(size_t)j * nT + ty])).re * wgt;
-                        for (int c = 0; c < 25; c++) Aa[CH_PLM + c] += cmul(ge, Pd[c]).re * wgt;  /* crystal frame */
-                        Aa[CH_KP] += cmul(ge, Kp).re * wgt;
+                        Aa[CH_PV] += cmul(ge, cscale(Ex, esc * fval[(size_t)j * nT + ty])).re * wgt;
+                        Aa[CH_K] += cmul(ge, cscale(Ex, esc * p->type_pval[ty] * dfval[(size_t)j * nT + ty])).re * wgt;
+                        for (int c = 0; c < 25; c++) Aa[CH_PLM + c] += esc * cmul(ge, Pd[c]).re * wgt;  /* crystal frame */
+                        Aa[CH_KP] += esc * cmul(ge, Kp).re * wgt;
                     }
                 }
             }

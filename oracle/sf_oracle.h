@@ -75,6 +75,11 @@ typedef struct {
     const double *dtdf;         /* [n_hkl*2] conj(dT/dF) * centering */
     /* derivative switches */
     int d_xyz, d_adp, d_occ, d_mp;
+    /* electron scattering (HC, Mott-Bethe, HansenCoppens_SF_Engine3.cpp:1387-1397):
+     * per wavefunction atomic number and f_e at s = 0 */
+    int electron;
+    const int *wfn_z;
+    const double *wfn_f000;
 } sfo_problem;
 
 typedef struct {

@@ -118,6 +118,24 @@ def main():
     out.update(ref_d_pval=d_pval, ref_d_plm=d_plm, ref_d_kappa=d_k, ref_d_kappa_p=d_kp)
     np.savez_compressed(os.path.join(HERE, "hc_multipole_fd.npz"), **out)
     print("wrote hc_multipole_fd")
+    # electron scattering (Mott-Bethe inside the engine), F(000) included; f_e(0) per wavefunction from the
+    # reference's "electron-IT" table
+    for name, sg, seed in (("el_hc_p21c", "P21/c", 501), ("el_hc_p212121", "P212121", 502)):
+        st = W.small_case(sg, n_atoms=6, stol_max=0.55, seed=seed, anomalous_per_atom=(seed == 502))
+        st.hkl = np.concatenate([np.zeros((1, 3), dtype=np.int32), st.hkl])
+        st.dtdf = np.concatenate([[0.4 + 0.2j], st.dtdf])
+        f000 = []
+        for w in st.wfns:
+            a, b, c = R.iam_coefficients(w.label, "electron-IT")
+            f000.append(float(np.sum(a) + c))
+        R.lib().ref_set_electron(1)
+        try:
+            out = run_hc(name, st)
+        finally:
+            R.lib().ref_set_electron(0)
+        out.update(electron_f000=np.array(f000))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("wrote", name, st.n_atoms, st.n_hkl)
     # IAM with the reference's IT92 Gaussian table
     st = W.small_case("C2/c", n_atoms=6, stol_max=0.6, seed=401)
     labels = [w.label for w in st.wfns]

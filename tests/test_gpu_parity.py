@@ -266,3 +266,24 @@ def test_reflection_order_is_free(engine, prec):
             t[i, s] = lut[tuple(int(v) for v in h @ r_)]
     r2 = api.TabulatedCalculator(engine, st2, t).calculate(st2.dtdf, precision=prec)
     check(r2, d2["ref_f"][perm2], d2["ref_d_xyz"], ref_adp_list(st2, d2), d2["ref_d_occ"], prec)
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+@pytest.mark.parametrize("name", fixture_names("el_"))
+def test_electron_scattering_matches_reference(engine, name, prec):
+    st, d = load_fixture(name)
+    calc = api.HcCalculator(engine, st)
+    calc.set_electron(True, d["electron_f000"])
+    r = calc.calculate(st.dtdf, precision=prec)
+    check(r, d["ref_f"], d["ref_d_xyz"], ref_adp_list(st, d), d["ref_d_occ"], prec)
+    # multipole-parameter derivatives against the oracle's (checked by finite differences on the CPU)
+    r = calc.calculate(st.dtdf, precision=prec, multipoles=True)
+    o = O.compute(st, electron_f000=d["electron_f000"], multipoles=True)
+    tol = TOL[prec][1]
+    for k in ("d_pval", "d_plm", "d_kappa", "d_kappa_p"):
+        assert rel_norm(r[k], o[k]) < tol, k
+    # and back to X-rays
+    calc.set_electron(False)
+    x = calc.calculate(st.dtdf, precision=FP64)
+    assert rel_f(x["f"], O.compute(st)["f"]) < 1e-10
+    calc.close()

@@ -85,3 +85,43 @@ def test_line_ordered_loop_multipole_derivatives():
     b = O.compute(st, multipoles=True, loop="lines")
     for k in ("d_pval", "d_plm", "d_kappa", "d_kappa_p"):
         assert rel_norm(b[k], a[k]) < 1e-11, k
+
+
+EL = fixture_names("el_")
+
+
+@pytest.mark.parametrize("loop", ["direct", "lines"])
+@pytest.mark.parametrize("name", EL)
+def test_electron_scattering_matches_reference(name, loop):
+    st, d = load_fixture(name)
+    r = O.compute(st, electron_f000=d["electron_f000"], loop=loop)
+    assert rel_f(r["f"], d["ref_f"]) < 1e-12
+    assert rel_norm(r["d_xyz"], d["ref_d_xyz"]) < 1e-11
+    assert rel_norm(r["d_adp"], ref_adp_list(st, d)) < 1e-11
+    assert rel_norm(r["d_occ"], d["ref_d_occ"]) < 1e-11
+
+
+def test_electron_multipole_derivatives_by_finite_differences():
+    # F is linear in P_val and P_lm: one central difference of the oracle's own F
+    st, d = load_fixture("el_hc_p21c")
+    f000 = d["electron_f000"]
+    r = O.compute(st, electron_f000=f000, multipoles=True)
+
+    def target(s):
+        return float(np.sum((np.conj(s.dtdf) * O.compute(s, electron_f000=f000)["f"]).real))
+
+    import copy
+    for a in (0, 3):
+        t = st.atom_type[a]
+        for q, h in ((None, 1e-2), (6, 1e-2)):
+            s1, s2 = copy.deepcopy(st), copy.deepcopy(st)
+            if q is None:
+                s1.types[t].p_val += h
+                s2.types[t].p_val -= h
+                ana = r["d_pval"][a]
+            else:
+                s1.types[t].plm[q] += h
+                s2.types[t].plm[q] -= h
+                ana = r["d_plm"][a][q]
+            fd = (target(s1) - target(s2)) / (2 * h)
+            assert abs(fd - ana) <= 1e-8 * max(1.0, abs(ana)), (a, q, fd, ana)
