@@ -117,6 +117,9 @@ def library():
                                                 _P(_Out)]
         L.dsf_reduce_to_types.argtypes = [C.c_void_p, _P(_Out), _P(_Out), C.c_void_p]
         L.dsf_structure_set_electron.argtypes = [C.c_void_p, C.c_int, _P(C.c_int), _P(C.c_double)]
+        L.dsf_structure_create_tsc.argtypes = [C.c_void_p, _P(_Sym), _P(_Atoms), C.c_int, _P(C.c_int), C.c_char_p,
+                                               _P(C.c_void_p)]
+        L.dsf_tsc_load.argtypes = [C.c_char_p, _P(C.c_int), _P(C.c_int), _P(C.c_int), _P(C.c_double), C.c_int]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
@@ -504,15 +507,20 @@ class TabulatedCalculator(_Calculator):
     """Tabulated complex form factors per (reflection, operation, atom) over
     all operations modulo centering."""
 
-    def __init__(self, engine, st, table=None, fp32_table=False, table_device=None, table_device_fp64=False):
+    def __init__(self, engine, st, table=None, fp32_table=False, table_device=None, table_device_fp64=False,
+                 tsc_path=None):
         """table: host complex [n_hkl][n_ops][n_atoms]; or table_device: a
         device pointer to the same layout (complex64, or complex128 with
-        table_device_fp64), gathered on the device (FP32 table)."""
+        table_device_fp64), gathered on the device (FP32 table); or
+        tsc_path: a .tsc file whose columns are the structure's atoms."""
         super().__init__(engine, st)
         sym, k1 = symmetry_desc(st, "all")
         atoms, k3 = _atoms_desc(st, lcs=False)
         x, p = _i(np.asarray(st.hkl).reshape(-1))
-        if table_device is not None:
+        if tsc_path is not None:
+            engine.check(self.lib.dsf_structure_create_tsc(engine.h, C.byref(sym), C.byref(atoms), len(st.hkl), p,
+                                                           os.fsencode(tsc_path), C.byref(self.h)), "create_tsc")
+        elif table_device is not None:
             engine.check(self.lib.dsf_structure_create_tabulated_device(
                 engine.h, C.byref(sym), C.byref(atoms), len(st.hkl), p, C.c_void_p(int(table_device)),
                 int(table_device_fp64), C.byref(self.h)), "create_tabulated_device")
@@ -593,3 +601,28 @@ class CombinedCalculator:
     def close(self):
         for c, _ in self.parts:
             c.close()
+
+
+def tsc_load(path):
+    """The rows of a .tsc file: (hkl [n][3] int, form factors [n][n_atoms] complex)."""
+    L = library()
+    na, nr = C.c_int(0), C.c_int(0)
+    rc = L.dsf_tsc_load(os.fsencode(path), C.byref(na), C.byref(nr), None, None, 0)
+    if rc != 0:
+        raise DsfError(f"dsf_tsc_load failed with status {rc}")
+    hkl = np.zeros((nr.value, 3), dtype=np.int32)
+    val = np.zeros((nr.value, na.value, 2))
+    rc = L.dsf_tsc_load(os.fsencode(path), C.byref(na), C.byref(nr), hkl.ctypes.data_as(_P(C.c_int)),
+                        val.ctypes.data_as(_P(C.c_double)), nr.value)
+    if rc != 0:
+        raise DsfError(f"dsf_tsc_load failed with status {rc}")
+    return hkl, val[..., 0] + 1j * val[..., 1]
+
+
+def write_tsc(path, labels, hkl, ff, title="form factors"):
+    """Writes a .tsc file (header, then "h k l re,im ..." per row; full precision)."""
+    with open(path, "w") as fh:
+        fh.write(f"TITLE: {title}\nAD: FALSE\nSYMM: expanded\nSCATTERERS: {' '.join(labels)}\nDATA:\n")
+        for h, row in zip(np.asarray(hkl), np.asarray(ff)):
+            fh.write(f"{int(h[0])} {int(h[1])} {int(h[2])} " +
+                     " ".join(f"{float(v.real)!r},{float(v.imag)!r}" for v in row) + "\n")

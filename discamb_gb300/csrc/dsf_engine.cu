@@ -34,6 +34,8 @@ cudaError_t launch_rs_prep(const DevStructure &S, int n_hkl_pad, void *rs_f, voi
 cudaError_t launch_tr_prep(const DevStructure &S, int n_hkl_pad, void *tr_f, void *tr_d, void *trm_f, void *trm_d,
                            bool mp, cudaStream_t st);
 size_t rs_record_bytes(bool fp64);
+int tsc_expand(const char *path, int n_atoms, int n_hkl, const int *hkl, int ns, const int *rot,
+               std::vector<float> &tab, std::string &err);
 cudaError_t launch_global_plm(int n, int K, const int *perm, const int *atom_type, const double *lcs,
                               const double *type_plm, const int *type_lmax, const double *fit, double *dmat,
                               double *pg_d, float *pg_f, cudaStream_t st);
@@ -1465,6 +1467,28 @@ int dsf_structure_create_tabulated_device(dsf_engine *e, const dsf_symmetry *sym
     if ((rc = dsf_structure_set_hkl(s, n_hkl, hkl))) { s->eng->live_structures--; return bail(rc); }
     *out = s;
     return DSF_OK;
+}
+
+int dsf_structure_create_tsc(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms, int n_hkl,
+                             const int *hkl, const char *path, dsf_structure **out)
+{
+    if (!e || !sym || !atoms || !hkl || !path || !out || n_hkl < 1 || sym->n_symops < 1)
+        return fail(e, DSF_ERR_ARGUMENT, "tsc structure needs symmetry, atoms, reflections and a file");
+    std::vector<float> tab;
+    std::string err;
+    int rc = tsc_expand(path, atoms->n_atoms, n_hkl, hkl, sym->n_symops, sym->symop_rotation, tab, err);
+    if (rc) return fail(e, rc, err);
+    cudaSetDevice(e->device);
+    DevBuf d;
+    DSF_CUDA(d.alloc(sizeof(float) * tab.size()));
+    cudaError_t ce = cudaMemcpy(d.p, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        d.release();
+        return fail(e, DSF_ERR_CUDA, cudaGetErrorString(ce));
+    }
+    rc = dsf_structure_create_tabulated_device(e, sym, atoms, n_hkl, hkl, d.p, 0, out);
+    d.release();
+    return rc;
 }
 
 int dsf_structure_destroy(dsf_structure *s)

@@ -30,6 +30,8 @@
  *   dsf_calculate_batch, dsf_calculate_batch_atoms, dsf_calculate_batch_device
  *                               many structures in one submission (the reference's callers run one
  *                               calculator per structure in turn, HcAtomBankStructureFactorCalculator.cpp:482-520)
+ *   dsf_structure_create_tsc, dsf_tsc_load
+ *                               TscFileBasedSfCalculator / tsc_io::read_tsc (the .tsc reader)
  *   dsf_structure_set_electron  HansenCoppensStructureFactorCalculator::setElectronScattering
  *   dsf_reduce_to_types         per-type multipole derivatives for TAAM callers (no reference counterpart)
  *   dsf_last_error              on_error::throwException messages (include/discamb/BasicUtilities/on_error.h:24-36):
@@ -178,6 +180,14 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
 int dsf_structure_create_tabulated_device(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms,
                                           int n_hkl, const int *hkl, const void *table_device, int table_fp64,
                                           dsf_structure **out);
+/* the tabulated model from a .tsc file (TscFileBasedSfCalculator, src/Scattering/TscFileBasedSfCalculator.cpp:17-123;
+ * format of tsc_io::read_tsc, src/IO/tsc_io.cpp:60-125): the file's columns are the structure's atoms in order; its
+ * rows must cover h' = h R for every reflection and operation of sym (a missing h' is an error, as in the reference) */
+int dsf_structure_create_tsc(dsf_engine *e, const dsf_symmetry *sym, const dsf_atoms *atoms, int n_hkl,
+                             const int *hkl, const char *path, dsf_structure **out);
+/* the raw contents of a .tsc file (no device needed): first call with hkl = values = NULL for the sizes, then with
+ * hkl [n_rows][3] and values [n_rows][n_atoms][2] of capacity_rows rows */
+int dsf_tsc_load(const char *path, int *n_atoms, int *n_rows, int *hkl, double *values, int capacity_rows);
 int dsf_structure_destroy(dsf_structure *s);
 
 int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl);

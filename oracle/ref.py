@@ -180,3 +180,22 @@ def table(st, keys, values):
     if rc != 0:
         raise RuntimeError("reference tabulated path raised an exception: " + _err())
     return _pack(out, st, ms.value)
+
+
+def tsc(st, path):
+    """The tabulated path reading a .tsc file with the reference's own reader
+    (tsc_io::read_tsc), columns = the structure's atoms in order."""
+    labels = ";".join(st.wfns[w].label for w in st.atom_wfn).encode()
+    cell, ops, adp = _common(st)
+    n = st.n_atoms
+    out = _outputs(st.n_hkl, n)
+    xyz = np.ascontiguousarray(st.xyz.reshape(-1)); adpf = np.ascontiguousarray(adp.reshape(-1))
+    nadp = st.n_adp(); mult = np.asarray(st.multiplicity, dtype=np.int32); occ = np.ascontiguousarray(st.occupancy)
+    hkl = np.ascontiguousarray(st.hkl.reshape(-1), dtype=np.int32)
+    g = np.ascontiguousarray(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1))
+    rc = lib().ref_tsc_sf(C.c_char_p(os.fsencode(path)), D_out(cell), C.c_char_p(ops), C.c_char_p(labels), C.c_int(n),
+                          D_out(xyz), D_out(nadp), D_out(adpf), D_out(occ), D_out(mult), C.c_int(st.n_hkl), D_out(hkl),
+                          D_out(g), D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]))
+    if rc != 0:
+        raise RuntimeError("reference tsc path raised an exception: " + _err())
+    return _pack(out, st, 0.0)

@@ -19,6 +19,7 @@
 #include "discamb/CrystalStructure/SpaceGroupOperation.h"
 #include "discamb/CrystalStructure/UnitCell.h"
 #include "discamb/HC_Model/HC_ModelParameters.h"
+#include "discamb/IO/tsc_io.h"
 #include "discamb/Scattering/AnyScattererStructureFactorCalculator.h"
 #include "discamb/Scattering/ConstFormFactorCalculationsManager.h"
 #include "discamb/Scattering/HansenCoppensStructureFactorCalculator.h"
@@ -295,6 +296,42 @@ int ref_table_sf(const double *cell, const char *ops, const char *labels, int n_
         if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         write_out(f, d, f_out, d_xyz, d_adp, d_occ);
         return 0;
+    } catch (const std::exception &ex) {
+        g_last_error = ex.what();
+        return 1;
+    } catch (...) {
+        g_last_error = "unknown exception";
+        return 1;
+    }
+}
+
+// The tabulated path from a .tsc file read by the reference's own reader
+// (tsc_io::read_tsc, src/IO/tsc_io.cpp:60-125), then as ref_table_sf
+// (TscFileBasedSfCalculator, src/Scattering/TscFileBasedSfCalculator.cpp:17-123).
+int ref_tsc_sf(const char *path, const double *cell, const char *ops, const char *labels, int n_atoms,
+               const double *xyz, const int *n_adp, const double *adp, const double *occ, const int *mult, int n_hkl,
+               const int *hkl, const double *dtdf, double *f_out, double *d_xyz, double *d_adp, double *d_occ)
+{
+    try {
+        vector<string> names;
+        vector<Vector3i> keys;
+        vector<vector<complex<double> > > ff;
+        tsc_io::read_tsc(path, names, keys, ff);
+        if ((int)names.size() != n_atoms) {
+            g_last_error = "tsc file lists a different number of scatterers";
+            return 1;
+        }
+        vector<int> k(3 * keys.size());
+        vector<double> v(2 * keys.size() * (size_t)n_atoms);
+        for (size_t i = 0; i < keys.size(); i++) {
+            for (int j = 0; j < 3; j++) k[3 * i + j] = keys[i][j];
+            for (int a = 0; a < n_atoms; a++) {
+                v[2 * (i * n_atoms + a)] = ff[i][a].real();
+                v[2 * (i * n_atoms + a) + 1] = ff[i][a].imag();
+            }
+        }
+        return ref_table_sf(cell, ops, labels, n_atoms, xyz, n_adp, adp, occ, mult, (int)keys.size(), k.data(),
+                            v.data(), n_hkl, hkl, dtdf, f_out, d_xyz, d_adp, d_occ, nullptr);
     } catch (const std::exception &ex) {
         g_last_error = ex.what();
         return 1;

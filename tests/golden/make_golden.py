@@ -136,6 +136,28 @@ def main():
         out.update(electron_f000=np.array(f000))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print("wrote", name, st.n_atoms, st.n_hkl)
+    # a .tsc file read by the reference's own reader (tsc_io::read_tsc), expanded h' set of all operations
+    import tempfile
+    from discamb_gb300 import api as A
+    st = W.small_case("P21/c", n_atoms=5, stol_max=0.5, seed=601)
+    rot, _ = A.all_ops_mod_centering(st.sg)
+    keys = sorted({tuple(int(v) for v in h @ r_) for h in st.hkl for r_ in rot})
+    rng = np.random.default_rng(602)
+    vals = rng.normal(size=(len(keys), st.n_atoms)) + 1j * rng.normal(size=(len(keys), st.n_atoms))
+    labels = [f"{st.wfns[w].label}{i + 1}" for i, w in enumerate(st.atom_wfn)]
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "form_factors.tsc")
+        A.write_tsc(path, labels, np.array(keys), vals)
+        r = R.tsc(st, path)
+    out = structure_to_arrays(st)
+    nadp = st.n_adp()
+    d_adp = np.zeros((st.n_atoms, 6))
+    for i, v in enumerate(r["d_adp"]):
+        d_adp[i, :nadp[i]] = v
+    out.update(tsc_keys=np.array(keys, dtype=np.int32), tsc_values=vals, tsc_labels=np.array(labels),
+               ref_f=r["f"], ref_d_xyz=r["d_xyz"], ref_d_adp=d_adp, ref_d_occ=r["d_occ"])
+    np.savez_compressed(os.path.join(HERE, "tsc_p21c.npz"), **out)
+    print("wrote tsc_p21c", st.n_atoms, st.n_hkl, len(keys))
     # IAM with the reference's IT92 Gaussian table
     st = W.small_case("C2/c", n_atoms=6, stol_max=0.6, seed=401)
     labels = [w.label for w in st.wfns]
