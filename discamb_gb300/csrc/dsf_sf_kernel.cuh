@@ -455,6 +455,12 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     if (tid == 0) issue(0, h_begin);
     uint32_t parity[2] = {0u, 0u};
     int k = 0;
+    // per-thread partial derivative sums, folded into the compensated totals
+    // every `fold` sub-tiles (about 16 reflections)
+    R part[NT];
+#pragma unroll
+    for (int q = 0; q < NT; q++) part[q] = R(0);
+    const int fold = ht >= 16 ? 1 : 16 / ht;
     for (int h0 = h_begin; h0 < h_end; h0 += ht, k++) {
         const int buf = k & 1;
         if (tid == 0 && h0 + ht < h_end) issue(buf ^ 1, h0 + ht);
@@ -477,10 +483,6 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
         const R2 *sG = reinterpret_cast<const R2 *>(st + SL.gw);
         const R *sH2 = reinterpret_cast<const R *>(st + SL.h2);
         const int *sCont = reinterpret_cast<const int *>(st + SL.cont);
-
-        R part[NT];
-#pragma unroll
-        for (int q = 0; q < NT; q++) part[q] = R(0);
 
         // reflections in groups of four: the partial F of a group is reduced across
         // the warp by one butterfly reduce-scatter of its eight values
@@ -812,15 +814,18 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                 dst[idx & 1] = v1;
             }
         }
-        // fold the sub-tile sums into the Kahan totals (each thread its own column)
+        // fold the partial sums into the Kahan totals (each thread its own column)
+        if ((k + 1) % fold == 0 || h0 + ht >= h_end) {
 #pragma unroll
-        for (int q = 0; q < NT; q++) {
-            R sum = sTot[q * kTileAtoms + tid], comp = sCmp[q * kTileAtoms + tid];
-            const R yv = part[q] - comp;
-            const R tv = sum + yv;
-            comp = (tv - sum) - yv;
-            sTot[q * kTileAtoms + tid] = tv;
-            sCmp[q * kTileAtoms + tid] = comp;
+            for (int q = 0; q < NT; q++) {
+                R sum = sTot[q * kTileAtoms + tid], comp = sCmp[q * kTileAtoms + tid];
+                const R yv = part[q] - comp;
+                const R tv = sum + yv;
+                comp = (tv - sum) - yv;
+                sTot[q * kTileAtoms + tid] = tv;
+                sCmp[q * kTileAtoms + tid] = comp;
+                part[q] = R(0);
+            }
         }
         __syncthreads();
         for (int i = tid; i < ht; i += blockDim.x) {
