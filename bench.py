@@ -547,7 +547,10 @@ def run_gpu(args):
     from discamb_gb300 import api, build, workloads as W
     build.build()
     wl = WORKLOADS[args.workload]
-    st = getattr(W, args.workload)(seed=wl["seed"] + rank)
+    kw = {}
+    if args.workload == "config2" and args.c2_atoms:  # a cut of config 2 (e.g. for a profile capture)
+        kw = dict(n_atoms=args.c2_atoms, d_min=args.c2_dmin)
+    st = getattr(W, args.workload)(seed=wl["seed"] + rank, **kw)
     mpd = wl["multipoles"]
     eng = api.Engine(device)
     calc = api.HcCalculator(eng, st)
@@ -691,6 +694,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config1", choices=sorted(WORKLOADS))
     ap.add_argument("--c4-crystals", type=int, default=256)
+    ap.add_argument("--c2-atoms", type=int, default=0, help="config2 cut: atoms (0 = the full 50,000)")
+    ap.add_argument("--c2-dmin", type=float, default=1.2)
     ap.add_argument("--c3-structures", type=int, default=400)
     ap.add_argument("--c3-rate", type=float, default=200.0)
     ap.add_argument("--c3-hbm-gb", type=float, default=160.0)

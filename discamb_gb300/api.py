@@ -337,6 +337,28 @@ class _Calculator:
         (x1, p1), (x2, p2), (x3, p3) = self._atom_arrays(xyz, adp, occupancy)
         self.engine.check(self.lib.dsf_structure_update_atoms(self.h, p1, p2, p3), "update_atoms")
 
+    def calculate_at_hkl(self, hkl, include=None, atoms=None, precision=DSF_FP64):
+        """F(h) and the derivatives of F itself at one reflection (complex per
+        atom), as calculateStructureFactorsAndDerivatives(hkl, F,
+        SfDerivativesAtHkl, mask) (include/discamb/Scattering/SfCalculator.h:82-86):
+        two calls on the one reflection with dT/dF = 1 and i give Re and Im of
+        dF/dp.  The resident reflection set is restored afterwards."""
+        saved = getattr(self, "_hkl_cache", None)
+        if saved is None:
+            saved = np.asarray(self.st.hkl, dtype=np.int32)
+        self.set_hkl(np.asarray(hkl, dtype=np.int32).reshape(1, 3))
+        try:
+            a = self.calculate(np.array([1.0 + 0j]), precision=precision, include=include, atoms=atoms,
+                               adp_layout="padded")
+            b = self.calculate(np.array([1j]), precision=precision, include=include, adp_layout="padded")
+        finally:
+            self.set_hkl(saved)
+            self._hkl_cache = saved
+        nadp = self._n_adp
+        d_adp = a["d_adp"] + 1j * b["d_adp"]
+        return dict(f=a["f"][0], d_xyz=a["d_xyz"] + 1j * b["d_xyz"],
+                    d_adp=[d_adp[i, :nadp[i]] for i in range(self.n_atoms)], d_occ=a["d_occ"] + 1j * b["d_occ"])
+
     def _out_arrays(self, multipoles):
         n, m = self.n_atoms, self.n_hkl
         r = dict(f=np.zeros(2 * m), d_xyz=np.zeros(3 * n), d_adp=np.zeros(6 * n), d_occ=np.zeros(n))

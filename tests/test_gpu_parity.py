@@ -287,3 +287,27 @@ def test_electron_scattering_matches_reference(engine, name, prec):
     x = calc.calculate(st.dtdf, precision=FP64)
     assert rel_f(x["f"], O.compute(st)["f"]) < 1e-10
     calc.close()
+
+
+def test_single_reflection_derivatives(engine):
+    # dF/dp at one reflection against central differences of F (the per-h API of the reference)
+    st = W.small_case("P21/c", n_atoms=4, stol_max=0.5, seed=620)
+    calc = api.HcCalculator(engine, st)
+    h = st.hkl[7]
+    r = calc.calculate_at_hkl(h)
+    full = calc.calculate(st.dtdf, precision=FP64)
+    assert abs(r["f"] - full["f"][7]) < 1e-12 * abs(full["f"][7]) + 1e-12
+    eps = 1e-6
+    for a in (0, 2):
+        for c in range(3):
+            xp, xm = st.xyz.copy(), st.xyz.copy()
+            xp[a, c] += eps
+            xm[a, c] -= eps
+            fp = calc.calculate_at_hkl(h, atoms=(xp, st.adp, st.occupancy))["f"]
+            fm = calc.calculate_at_hkl(h, atoms=(xm, st.adp, st.occupancy))["f"]
+            fd = (fp - fm) / (2 * eps)
+            assert abs(fd - r["d_xyz"][a, c]) < 1e-6 * max(1.0, abs(fd)), (a, c, fd, r["d_xyz"][a, c])
+    # the resident reflection set is back
+    again = calc.calculate(st.dtdf, precision=FP64, atoms=(st.xyz, st.adp, st.occupancy))
+    assert rel_f(again["f"], full["f"]) < 1e-13
+    calc.close()
