@@ -463,6 +463,7 @@ class HcCalculator(_Calculator):
 
     def __init__(self, engine, st, representation="engine", upload_atoms=True):
         super().__init__(engine, st)
+        self.def_val_symm = False
         sym, k1 = symmetry_desc(st, representation)
         model, k2 = _hc_desc(st)
         atoms, k3 = _atoms_desc(st)
@@ -481,6 +482,17 @@ class HcCalculator(_Calculator):
         else:
             pz = pf = None
         self.engine.check(self.lib.dsf_structure_set_electron(self.h, int(bool(on)), pz, pf), "set_electron")
+
+    def set_def_val_symm(self, on=True):
+        """The reference's point-group-symmetrised deformation valence
+        (HansenCoppensStructureFactorCalculator::set_def_val_symm, which
+        selects HansenCoppens_SF_EngineSymm: the same F and derivatives as
+        Engine3, the harmonics of a point group's operations evaluated once
+        per parity class).  The kernels here always take that split where the
+        operations have sign-diagonal cosets (the coset form), so the switch
+        changes nothing in the result or in the work; it is kept so callers
+        that set it run unchanged."""
+        self.def_val_symm = bool(on)
 
     def reduce_to_types(self, per_atom, per_type, stream=0):
         """TAAM types: sum the multipole derivatives of the atoms of each type

@@ -109,6 +109,15 @@ int ref_set_electron(int on)
     return 0;
 }
 
+// point-group-symmetrised deformation valence (HansenCoppens_SF_EngineSymm instead of Engine3, selected by
+// set_def_val_symm, HansenCoppensStructureFactorCalculator.cpp:447-468) for the following ref_hc_sf calls
+static bool g_def_val_symm = false;
+int ref_set_def_val_symm(int on)
+{
+    g_def_val_symm = on != 0;
+    return 0;
+}
+
 // Hansen-Coppens path through HansenCoppensStructureFactorCalculator ("CPU").
 // Wavefunctions as Slater orbitals: per wfn [orb_off[w], orb_off[w+1]) orbitals,
 // per orbital [sto_off[o], sto_off[o+1]) Slater functions.
@@ -174,6 +183,7 @@ int ref_hc_sf(const double *cell, const char *ops, int n_atoms, const double *xy
         calc.setCalculationMode("CPU");
         calc.setN_Threads(n_threads);
         calc.setElectronScattering(g_electron);
+        calc.set_def_val_symm(g_def_val_symm);
         if (atom_anom) {
             vector<complex<double> > an(n_atoms);
             for (int a = 0; a < n_atoms; a++) an[a] = complex<double>(atom_anom[2 * a], atom_anom[2 * a + 1]);

@@ -2,7 +2,7 @@
 library's own CPU code (oracle/_ref/libref_driver.so, built from the
 reference sources by oracle/Makefile.ref) on seeded synthetic structures.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [hc|def_val_symm|rest ...]   (default: all)
 
 Each fixture (.npz) holds every input of the case (structure_to_arrays) and
 the reference outputs: F, d_xyz, d_adp, d_occ in the crystal's conventions.
@@ -106,11 +106,36 @@ def multipole_fd(st):
     return d_pval, d_plm, d_kappa, d_kappa_p
 
 
-def main():
-    os.makedirs(HERE, exist_ok=True)
+def write_hc():
     for name, st in hc_cases():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **run_hc(name, st))
         print("wrote", name, st.n_atoms, st.n_hkl)
+
+
+def write_def_val_symm():
+    """The reference's point-group-symmetrised deformation valence engine
+    (HansenCoppens_SF_EngineSymm, selected by set_def_val_symm): the same
+    structure factors as Engine3, computed per point group (a closed form for
+    222, a z-axis shortcut for dipole/quadrupole-only atoms)."""
+    for i, sg in enumerate(["P212121", "P21/c", "P43212", "Pbca"]):
+        st = W.small_case(sg, n_atoms=5, stol_max=0.55, seed=700 + i, improper_lcs=True)
+        if sg == "P212121":  # one dipole/quadrupole-along-z type (the engine's pz/dz branch)
+            t = st.types[st.atom_type[0]]
+            t.plm[:] = 0.0
+            t.plm[2] = 0.05
+            t.plm[6] = -0.04
+            t.n_l = 3
+        name = "dvs_hc_" + sg.replace("/", "_").lower()
+        R.lib().ref_set_def_val_symm(1)
+        try:
+            out = run_hc(name, st)
+        finally:
+            R.lib().ref_set_def_val_symm(0)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("wrote", name, st.n_atoms, st.n_hkl)
+
+
+def write_rest():
     # multipole-parameter derivatives
     st = W.small_case("P21/c", n_atoms=3, stol_max=0.45, seed=301)
     out = run_hc("hc_multipole_fd", st)
@@ -198,5 +223,14 @@ def main():
     print("wrote table_p21c")
 
 
+GROUPS = {"hc": write_hc, "def_val_symm": write_def_val_symm, "rest": write_rest}
+
+
+def main(groups):
+    os.makedirs(HERE, exist_ok=True)
+    for g in groups or list(GROUPS):
+        GROUPS[g]()
+
+
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

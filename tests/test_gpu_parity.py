@@ -41,6 +41,18 @@ def test_hc_matches_reference(engine, name, prec):
 
 
 @pytest.mark.parametrize("prec", [FP64, FP32])
+@pytest.mark.parametrize("name", fixture_names("dvs_"))
+def test_def_val_symmetrised_engine_matches_reference(engine, name, prec):
+    # fixtures from the reference's HansenCoppens_SF_EngineSymm (set_def_val_symm(true)): point groups 222
+    # (its closed form, one dipole/quadrupole-only type), 2/m, 422, mmm
+    st, d = load_fixture(name)
+    calc = api.HcCalculator(engine, st)
+    calc.set_def_val_symm(True)
+    r = calc.calculate(st.dtdf, precision=prec)
+    check(r, d["ref_f"], d["ref_d_xyz"], ref_adp_list(st, d), d["ref_d_occ"], prec)
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
 def test_hc_all_operations_representation(engine, prec):
     # the generic engine's representation (all operations modulo centering, no
     # inversion shortcut) gives the same F for a structure without anomalous

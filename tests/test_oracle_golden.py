@@ -6,7 +6,8 @@ import pytest
 from conftest import fixture_names, load_fixture, rel_f, rel_norm, ref_adp_list
 from oracle import oracle as O
 
-HC = [n for n in fixture_names("hc_")]
+# hc_*: Engine3; dvs_*: the def-val-symmetrised EngineSymm (same results by construction)
+HC = fixture_names("hc_") + fixture_names("dvs_")
 
 
 @pytest.mark.parametrize("name", HC)
