@@ -207,19 +207,14 @@ __host__ __device__ constexpr int harmonic_class(int q)
     return cls[q];
 }
 
-// the 16 (l, parity class) slots of the multipole adjoint's class sums: the
-// slot of harmonic q, and the parity class and l of slot k
+// the 16 (l, parity class) slots of the multipole adjoint's class sums, the
+// slot of harmonic q; (l, class) of slots 0-15: (0,0) (1,2) (1,4) (1,1) (2,3)
+// (2,6) (2,0) (2,5) (3,2) (3,7) (3,4) (3,1) (4,3) (4,6) (4,0) (4,5)
 __host__ __device__ constexpr int harmonic_slot(int q)
 {
     constexpr int sl[25] = {0, 1, 2, 3, 4, 5, 6, 7, 6, 8, 9, 8, 10, 11, 10, 11, 12, 13, 12, 13, 14, 15, 14, 15, 14};
     return sl[q];
 }
-__host__ __device__ constexpr int slot_class(int k)
-{
-    constexpr int c[16] = {0, 2, 4, 1, 3, 6, 0, 5, 2, 7, 4, 1, 3, 6, 0, 5};
-    return c[k];
-}
-__host__ __device__ constexpr int slot_l(int k) { return k == 0 ? 0 : (k < 4 ? 1 : k / 4 + 1); }
 
 template <typename R>
 struct StageLayout {
@@ -542,30 +537,61 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     };
                     // coset form: radial-weighted class sums, even l (real part) and odd l (imaginary part)
                     R Ec[4] = {0, 0, 0, 0}, Oc[4] = {0, 0, 0, 0};  // classes 0 3 6 5 | 2 4 1 7
-                    // with the multipole adjoint: unweighted slot sums (l, class) and the
-                    // operations' signed adjoint weights per slot, folded into the P_lm
-                    // channels once per coset
-                    R Acl[DIAG && MP ? 16 : 1], QC[DIAG && MP ? 16 : 1];
+                    // with the multipole adjoint: the same class sums weighted by the kappa'
+                    // derivatives of the radial terms (De, Do), and the operations' signed
+                    // adjoint weights per class (We: Re(g z) of the even classes, Wo: Im(g z) of
+                    // the odd ones), folded into the P_lm channels once per coset: the weight of
+                    // harmonic (l, c) is r_l We[c] (even l) or -r_l Wo[c] (odd l)
+                    R De[DIAG && MP ? 4 : 1], Do[DIAG && MP ? 4 : 1], We[DIAG && MP ? 4 : 1], Wo[DIAG && MP ? 4 : 1];
 #pragma unroll
-                    for (int k = 0; k < (DIAG && MP ? 16 : 1); k++) { Acl[k] = R(0); QC[k] = R(0); }
-                    auto slot_sums = [&](const R *y) {
+                    for (int k = 0; k < (DIAG && MP ? 4 : 1); k++) { De[k] = Do[k] = We[k] = Wo[k] = R(0); }
+                    auto mp_coset_begin = [&](const R *y, const R *dr) {
                         if constexpr (DIAG && MP) {
+                            // unweighted slot sums (l, class) of the coset's first operation
+                            R Acl[16];
 #pragma unroll
                             for (int k = 0; k < 16; k++) Acl[k] = R(0);
 #pragma unroll
                             for (int q = 0; q < 9; q++) Acl[harmonic_slot(q)] += pg[q] * y[q];
+                            Ec[0] = fsre + r0 * Acl[0] + r2 * Acl[6];
+                            Ec[1] = r2 * Acl[4];
+                            Ec[2] = r2 * Acl[5];
+                            Ec[3] = r2 * Acl[7];
+                            Oc[0] = r1 * Acl[1];
+                            Oc[1] = r1 * Acl[2];
+                            Oc[2] = r1 * Acl[3];
+                            Oc[3] = R(0);
+                            De[0] = dr[2] * Acl[0] + dr[4] * Acl[6];
+                            De[1] = dr[4] * Acl[4];
+                            De[2] = dr[4] * Acl[5];
+                            De[3] = dr[4] * Acl[7];
+                            Do[0] = dr[3] * Acl[1];
+                            Do[1] = dr[3] * Acl[2];
+                            Do[2] = dr[3] * Acl[3];
+                            Do[3] = R(0);
                             if (high_l) {
 #pragma unroll
                                 for (int q = 9; q < 25; q++) Acl[harmonic_slot(q)] += pg[q] * y[q];
+                                Ec[0] += r4 * Acl[14]; Ec[1] += r4 * Acl[12]; Ec[2] += r4 * Acl[13]; Ec[3] += r4 * Acl[15];
+                                Oc[0] += r3 * Acl[8]; Oc[1] += r3 * Acl[10]; Oc[2] += r3 * Acl[11]; Oc[3] = r3 * Acl[9];
+                                De[0] += dr[6] * Acl[14]; De[1] += dr[6] * Acl[12]; De[2] += dr[6] * Acl[13];
+                                De[3] += dr[6] * Acl[15];
+                                Do[0] += dr[5] * Acl[8]; Do[1] += dr[5] * Acl[10]; Do[2] += dr[5] * Acl[11];
+                                Do[3] = dr[5] * Acl[9];
                             }
+#pragma unroll
+                            for (int k = 0; k < 4; k++) { We[k] = R(0); Wo[k] = R(0); }
                         }
                     };
                     auto flush_slots = [&](const R *y) {
                         if constexpr (DIAG && MP) {
+                            // slot weights in harmonic_slot order
+                            const R QC[16] = {r0 * We[0], -r1 * Wo[0], -r1 * Wo[1], -r1 * Wo[2],
+                                              r2 * We[1], r2 * We[2], r2 * We[0], r2 * We[3],
+                                              -r3 * Wo[0], -r3 * Wo[3], -r3 * Wo[1], -r3 * Wo[2],
+                                              r4 * We[1], r4 * We[2], r4 * We[0], r4 * We[3]};
 #pragma unroll
                             for (int q = 0; q < 25; q++) part[CH_PLM + q] += QC[harmonic_slot(q)] * y[q];
-#pragma unroll
-                            for (int k = 0; k < 16; k++) QC[k] = R(0);
                         }
                     };
                     auto class_sums = [&](const R *y) {
@@ -646,19 +672,6 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                                 }
                                 fre = tv.x + anre; fim = tv.y + anim;
                             }
-                        } else if constexpr (DIAG && MP) {
-                            const auto sg = [&](int c) -> R {
-                                if constexpr (F32) return G.f[s][c]; else return G.d[s][c];
-                            };
-                            A0 = Acl[0];
-                            A1 = sg(2) * Acl[1] + sg(4) * Acl[2] + sg(1) * Acl[3];
-                            A2 = Acl[6] + sg(3) * Acl[4] + sg(6) * Acl[5] + sg(5) * Acl[7];
-                            if (high_l) {
-                                A3 = sg(2) * Acl[8] + sg(7) * Acl[9] + sg(4) * Acl[10] + sg(1) * Acl[11];
-                                A4 = Acl[14] + sg(3) * Acl[12] + sg(6) * Acl[13] + sg(5) * Acl[15];
-                            }
-                            fre = fsre + r0 * A0 + r2 * A2 + r4 * A4;
-                            fim = fsim + r1 * A1 + r3 * A3;
                         } else if constexpr (DIAG) {
                             // fsph rides in the class-0 sums (sign +1 for every operation)
                             if constexpr (F32) {
@@ -713,16 +726,17 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             Ere += zre; Eim += zim;
                             // q_l = Re(g i^l rr_l z): even l rs_l Re(gz), odd l -rs_l Im(gz)
                             const R wre = gre * zre - gim * zim, wim = gre * zim + gim * zre;
-                            const R q0 = r0 * wre, q1 = -r1 * wim, q2 = r2 * wre, q3 = -r3 * wim, q4 = r4 * wre;
+                            R dre, dim;
                             if constexpr (DIAG) {
-                                const R ql[5] = {q0, q1, q2, q3, q4};
-                                QC[0] += q0;
-#pragma unroll
-                                for (int k = 1; k < 16; k++) {
-                                    if constexpr (F32) QC[k] += G.f[s][slot_class(k)] * ql[slot_l(k)];
-                                    else QC[k] += G.d[s][slot_class(k)] * ql[slot_l(k)];
-                                }
+                                const auto sg = [&](int c) -> R {
+                                    if constexpr (F32) return G.f[s][c]; else return G.d[s][c];
+                                };
+                                We[0] += wre; We[1] += sg(3) * wre; We[2] += sg(6) * wre; We[3] += sg(5) * wre;
+                                Wo[0] += sg(2) * wim; Wo[1] += sg(4) * wim; Wo[2] += sg(1) * wim; Wo[3] += sg(7) * wim;
+                                dre = De[0] + sg(3) * De[1] + sg(6) * De[2] + sg(5) * De[3];
+                                dim = sg(2) * Do[0] + sg(4) * Do[1] + sg(1) * Do[2] + sg(7) * Do[3];
                             } else {
+                                const R q0 = r0 * wre, q1 = -r1 * wim, q2 = r2 * wre, q3 = -r3 * wim, q4 = r4 * wre;
                                 part[CH_PLM] += q0 * y[0];
 #pragma unroll
                                 for (int q = 1; q < 4; q++) part[CH_PLM + q] += q1 * y[q];
@@ -732,9 +746,9 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                                 for (int q = 9; q < 16; q++) part[CH_PLM + q] += q3 * y[q];
 #pragma unroll
                                 for (int q = 16; q < 25; q++) part[CH_PLM + q] += q4 * y[q];
+                                dre = dr[2] * A0 + dr[4] * A2 + dr[6] * A4;
+                                dim = dr[3] * A1 + dr[5] * A3;
                             }
-                            const R dre = dr[2] * A0 + dr[4] * A2 + dr[6] * A4;
-                            const R dim = dr[3] * A1 + dr[5] * A3;
                             Kre += dre * zre - dim * zim;
                             Kim += dre * zim + dim * zre;
                         }
@@ -749,7 +763,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                                         adp_coset_end();
                                     }
                                     class_sums(recs[s].y);
-                                    slot_sums(recs[s].y);
+                                    mp_coset_begin(recs[s].y, sTrm + (size_t)(lt * ht + hl) * 8);
                                     adp_coset_begin(recs[s]);
                                 }
                             }

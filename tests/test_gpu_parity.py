@@ -146,10 +146,15 @@ def test_sign_coset_forms_match_oracle(engine, sg, rep, prec):
         if rep == "all":  # no inversion shortcut: equal F only without anomalous dispersion
             for w in st.wfns:
                 w.anomalous = 0j
-        o = O.compute(st)
+        o = O.compute(st, multipoles=True)
         calc = api.HcCalculator(engine, st, representation=rep)
         r = calc.calculate(st.dtdf, precision=prec)
         check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
+        # the multipole-adjoint kernels of the same shape
+        r = calc.calculate(st.dtdf, precision=prec, multipoles=True)
+        check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
+        for k in ("d_pval", "d_plm", "d_kappa", "d_kappa_p"):
+            assert rel_norm(r[k], o[k]) < TOL[prec][1], (k, rel_norm(r[k], o[k]))
         calc.close()
 
 
