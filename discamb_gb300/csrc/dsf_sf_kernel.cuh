@@ -583,8 +583,15 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             for (int k = 0; k < 4; k++) { We[k] = R(0); Wo[k] = R(0); }
                         }
                     };
-                    auto flush_slots = [&](const R *y) {
+                    auto flush_slots = [&](const R *y, const R *dr) {
                         if constexpr (DIAG && MP) {
+                            // P_val and kappa: Re(g sum_s z_s T) dr_0,1 = We[0] dr_0,1; kappa':
+                            // sum_s Re(g z_s T (dre_s + i dim_s)) with dre_s = sum_c sign_c(s) De[c]
+                            // (dim_s likewise) = sum_c De[c] We[c] - Do[c] Wo[c]
+                            part[CH_PV] += dr[0] * We[0];
+                            part[CH_KAPPA] += dr[1] * We[0];
+                            part[CH_KAPPA_P] += De[0] * We[0] + De[1] * We[1] + De[2] * We[2] + De[3] * We[3] -
+                                                (Do[0] * Wo[0] + Do[1] * Wo[1] + Do[2] * Wo[2] + Do[3] * Wo[3]);
                             // slot weights in harmonic_slot order
                             const R QC[16] = {r0 * We[0], -r1 * Wo[0], -r1 * Wo[1], -r1 * Wo[2],
                                               r2 * We[1], r2 * We[2], r2 * We[0], r2 * We[3],
@@ -722,20 +729,19 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             }
                         }
                         if constexpr (MP) {
-                            const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
-                            Ere += zre; Eim += zim;
                             // q_l = Re(g i^l rr_l z): even l rs_l Re(gz), odd l -rs_l Im(gz)
                             const R wre = gre * zre - gim * zim, wim = gre * zim + gim * zre;
-                            R dre, dim;
                             if constexpr (DIAG) {
+                                // everything else of the multipole adjoint follows from these sums
+                                // once per coset (flush_slots)
                                 const auto sg = [&](int c) -> R {
                                     if constexpr (F32) return G.f[s][c]; else return G.d[s][c];
                                 };
                                 We[0] += wre; We[1] += sg(3) * wre; We[2] += sg(6) * wre; We[3] += sg(5) * wre;
                                 Wo[0] += sg(2) * wim; Wo[1] += sg(4) * wim; Wo[2] += sg(1) * wim; Wo[3] += sg(7) * wim;
-                                dre = De[0] + sg(3) * De[1] + sg(6) * De[2] + sg(5) * De[3];
-                                dim = sg(2) * Do[0] + sg(4) * Do[1] + sg(1) * Do[2] + sg(7) * Do[3];
                             } else {
+                                const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
+                                Ere += zre; Eim += zim;
                                 const R q0 = r0 * wre, q1 = -r1 * wim, q2 = r2 * wre, q3 = -r3 * wim, q4 = r4 * wre;
                                 part[CH_PLM] += q0 * y[0];
 #pragma unroll
@@ -746,11 +752,11 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                                 for (int q = 9; q < 16; q++) part[CH_PLM + q] += q3 * y[q];
 #pragma unroll
                                 for (int q = 16; q < 25; q++) part[CH_PLM + q] += q4 * y[q];
-                                dre = dr[2] * A0 + dr[4] * A2 + dr[6] * A4;
-                                dim = dr[3] * A1 + dr[5] * A3;
+                                const R dre = dr[2] * A0 + dr[4] * A2 + dr[6] * A4;
+                                const R dim = dr[3] * A1 + dr[5] * A3;
+                                Kre += dre * zre - dim * zim;
+                                Kim += dre * zim + dim * zre;
                             }
-                            Kre += dre * zre - dim * zim;
-                            Kim += dre * zim + dim * zre;
                         }
                     };
                     if constexpr (NSC > 0) {
@@ -759,7 +765,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             if constexpr (CS > 0) {
                                 if (s % CS == 0) {
                                     if (s > 0) {
-                                        flush_slots(recs[s - CS].y);
+                                        flush_slots(recs[s - CS].y, sTrm + (size_t)(lt * ht + hl) * 8);
                                         adp_coset_end();
                                     }
                                     class_sums(recs[s].y);
@@ -770,7 +776,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             term(s);
                         }
                         if constexpr (CS > 0) {
-                            flush_slots(recs[NSC - CS].y);
+                            flush_slots(recs[NSC - CS].y, sTrm + (size_t)(lt * ht + hl) * 8);
                             adp_coset_end();
                         }
                     } else {
@@ -781,7 +787,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         Ure *= Tiso; Uim *= Tiso;
 #pragma unroll
                         for (int q = 0; q < 3; q++) { Xre[q] *= Tiso; Xim[q] *= Tiso; }
-                        if constexpr (MP) { Ere *= Tiso; Eim *= Tiso; Kre *= Tiso; Kim *= Tiso; }
+                        if constexpr (MP && !DIAG) { Ere *= Tiso; Eim *= Tiso; Kre *= Tiso; Kim *= Tiso; }
                     }
                     Fv[2 * j] = w * Ure;
                     Fv[2 * j + 1] = w * Uim;
@@ -795,7 +801,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     }
 #pragma unroll
                     for (int q = 0; q < 3; q++) part[CH_XYZ + q] -= g.x * Xim[q] + g.y * Xre[q];  // -Im(g X)
-                    if constexpr (MP) {
+                    if constexpr (MP && !DIAG) {
                         const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
                         const R gE = g.x * Ere - g.y * Eim;
                         part[CH_PV] += dr[0] * gE;
