@@ -17,7 +17,8 @@ cudaError_t launch_k3_f32_hc(const K3Args &A, bool mp, bool aniso)
 size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types, bool table)
 {
     if (fp64) return mp ? sf_smem_bytes<double, true>(ht, n_sym, max_types) : sf_smem_bytes<double, false>(ht, n_sym, max_types);
-    return mp ? sf_smem_bytes<float, true>(ht, n_sym, max_types) : sf_smem_bytes<float, false>(ht, n_sym, max_types, table);
+    return mp ? sf_smem_bytes<float, true>(ht, n_sym, max_types)
+              : sf_smem_bytes<float, false>(ht, n_sym, max_types, table && !table_count_compiled(n_sym));
 }
 
 cudaError_t launch_sf3(const K3Args &A, int model, bool fp64, bool mp, bool aniso)

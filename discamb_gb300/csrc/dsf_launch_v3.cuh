@@ -80,6 +80,11 @@ __host__ inline bool coset_form_compiled(bool fp64, int model, int n_sym, int cs
     return (n_sym == 2 && cs == 2) || (n_sym == 4 && (cs == 4 || cs == 2)) || (n_sym == 8 && (cs == 8 || cs == 4));
 }
 
+// operation counts with compiled FP32 tabulated kernels: those read the form
+// factors straight into registers; the runtime-count kernel stages them in
+// shared memory (the dispatch lists of dsf_k3_f32_other.cu and dsf_k3b_f32.cu)
+__host__ inline bool table_count_compiled(int n_sym) { return n_sym == 2 || n_sym == 4 || n_sym == 8; }
+
 // per-translation-unit entries (model, multipole adjoint and ADP kind resolved at run time)
 cudaError_t launch_k3_f32_hc(const K3Args &A, bool mp, bool aniso);
 cudaError_t launch_k3_f32_hc_mp(const K3Args &A, bool aniso);

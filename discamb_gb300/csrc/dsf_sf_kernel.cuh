@@ -322,8 +322,13 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 
     // shared memory carve-up
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_raw);  // [2]
-    const StageLayout<R> SL(ht, nS, L.max_types, MP, TABLE);
-    constexpr bool TAB_SMEM = TABLE && F32;  // form factors staged by bulk copies
+    // FP32 tabulated form factors: with a compiled operation count each thread
+    // loads its own column of the next group of four reflections into registers
+    // while the current group runs (coalesced streaming loads, no shared memory,
+    // so the sub-tiles stay long); otherwise they are staged by bulk copies
+    constexpr bool TAB_REG = TABLE && F32 && NSC > 0;
+    constexpr bool TAB_SMEM = TABLE && F32 && NSC == 0;
+    const StageLayout<R> SL(ht, nS, L.max_types, MP, TAB_SMEM);
     unsigned char *stage0 = smem_raw + 64;
     R2 *sF = reinterpret_cast<R2 *>(stage0 + 2 * SL.bytes);           // [kWarps][ht]
     R *sTot = reinterpret_cast<R *>(sF + kWarps * ht);                 // [NT][kTileAtoms]
@@ -447,6 +452,27 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
         }
     }
 
+    // TAB_REG: form factors of the current and the next group of four reflections
+    float2 tab_cur[TAB_REG ? 4 * NR : 1], tab_next[TAB_REG ? 4 * NR : 1];
+    const float2 *tab_col = nullptr;
+    if constexpr (TAB_REG) {
+        // a tile's columns are contiguous (tiles do not straddle table_split)
+        tab_col = S.table_f + (a + (a >= S.table_split ? S.table_shift : 0));
+#pragma unroll
+        for (int q = 0; q < 4 * NR; q++) tab_cur[q] = tab_next[q] = make_float2(0.f, 0.f);
+    }
+    // rows hg .. hg + 3 (below n_hkl_pad for every group that starts before h_end)
+    auto tab_load = [&](int hg) {
+        if constexpr (TAB_REG) {
+            if (have && hg < h_end) {
+#pragma unroll
+                for (int q = 0; q < 4 * NR; q++)
+                    tab_next[q] = __ldcs(tab_col + ((size_t)hg * NR + q) * S.table_stride);
+            }
+        }
+    };
+    tab_load(h_begin);
+
     if (tid == 0) issue(0, h_begin);
     uint32_t parity[2] = {0u, 0u};
     int k = 0;
@@ -482,6 +508,11 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
         // reflections in groups of four: the partial F of a group is reduced across
         // the warp by one butterfly reduce-scatter of its eight values
         for (int g0 = 0; g0 < ht; g0 += 4) {
+            if constexpr (TAB_REG) {
+#pragma unroll
+                for (int q = 0; q < 4 * NR; q++) tab_cur[q] = tab_next[q];
+                tab_load(h0 + g0 + 4);
+            }
             R Fv[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) Fv[q] = R(0);
@@ -662,7 +693,10 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         if constexpr (TABLE) {
                             // the table holds n_hkl_pad rows (zero past the last reflection), columns in
                             // the engine's atom order (consecutive lanes read consecutive values)
-                            if constexpr (F32) {
+                            if constexpr (TAB_REG) {
+                                const float2 tv = tab_cur[j * NR + s];
+                                fre = tv.x + anre; fim = tv.y + anim;
+                            } else if constexpr (F32) {
                                 const float2 tv = reinterpret_cast<const float2 *>(st + SL.tab)[
                                     (size_t)(hl * nS + s) * kTileAtoms + tid];
                                 fre = tv.x + anre; fim = tv.y + anim;
@@ -882,9 +916,15 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     }
 }
 
+// at least four blocks per SM for the tabulated model with up to four
+// operations (HBM-streaming: occupancy over registers; eight operations'
+// prefetched form factors do not fit that budget)
+template <int MODEL, int NSC>
+constexpr int min_blocks() { return MODEL == MODEL_TABLE && NSC <= 4 ? 4 : 1; }
+
 // one structure: block (tile, reflection chunk)
 template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
-__global__ void __launch_bounds__(kTileAtoms)
+__global__ void __launch_bounds__(kTileAtoms, min_blocks<MODEL, NSC>())
 sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 {
     sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(S, C, L, G, blockIdx.x, blockIdx.y);
@@ -893,7 +933,7 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 // many structures of one kernel shape (and one sign table) in one launch: the
 // block's item is the last with block_begin <= blockIdx.x
 template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
-__global__ void __launch_bounds__(kTileAtoms)
+__global__ void __launch_bounds__(kTileAtoms, min_blocks<MODEL, NSC>())
 sf_grad_batch3(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
 {
     const int b = blockIdx.x;
