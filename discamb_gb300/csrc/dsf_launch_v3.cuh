@@ -23,21 +23,28 @@ struct K3Args {
     cudaStream_t st = nullptr;
 };
 
+template <typename K, typename... Args>
+cudaError_t launch_with(K k, dim3 grid, size_t smem, cudaStream_t st, const Args &...args)
+{
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k<<<grid, kTileAtoms, smem, st>>>(args...);
+    return cudaGetLastError();
+}
+
 template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
 cudaError_t launch_k3(const K3Args &A)
 {
-    if constexpr (BATCH) {
-        auto k = sf_grad_batch3<R, MODEL, MP, ANISO, NSC, CS>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A.smem);
-        if (e != cudaSuccess) return e;
-        k<<<A.blocks, kTileAtoms, A.smem, A.st>>>(*A.B, *A.G);
-    } else {
-        auto k = sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)A.smem);
-        if (e != cudaSuccess) return e;
-        k<<<dim3(A.n_tiles, A.n_chunks), kTileAtoms, A.smem, A.st>>>(*A.S, *A.C, *A.L, *A.G);
-    }
-    return cudaGetLastError();
+    constexpr bool OCC4 = occ4_kernel<MODEL, NSC>();
+    const dim3 grid = BATCH ? dim3(A.blocks) : dim3(A.n_tiles, A.n_chunks);
+    if constexpr (BATCH && OCC4)
+        return launch_with(sf_grad_batch3_occ4<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.B, *A.G);
+    else if constexpr (BATCH)
+        return launch_with(sf_grad_batch3<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.B, *A.G);
+    else if constexpr (OCC4)
+        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.S, *A.C, *A.L, *A.G);
+    else
+        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.S, *A.C, *A.L, *A.G);
 }
 
 // compiled operation counts first, runtime count last

@@ -916,25 +916,29 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     }
 }
 
-// at least four blocks per SM for the tabulated model with up to four
-// operations (HBM-streaming: occupancy over registers; eight operations'
-// prefetched form factors do not fit that budget)
-template <int MODEL, int NSC>
-constexpr int min_blocks() { return MODEL == MODEL_TABLE && NSC <= 4 ? 4 : 1; }
-
 // one structure: block (tile, reflection chunk)
 template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
-__global__ void __launch_bounds__(kTileAtoms, min_blocks<MODEL, NSC>())
+__global__ void __launch_bounds__(kTileAtoms)
 sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
+{
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(S, C, L, G, blockIdx.x, blockIdx.y);
+}
+
+// the same with at least four blocks per SM: the tabulated model with up to
+// four compiled operations (HBM streaming: occupancy over registers).  The
+// other kernels keep the compiler's own register choice, which an explicit
+// minimum of one block would change.
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+__global__ void __launch_bounds__(kTileAtoms, 4)
+sf_grad_kernel3_occ4(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 {
     sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(S, C, L, G, blockIdx.x, blockIdx.y);
 }
 
 // many structures of one kernel shape (and one sign table) in one launch: the
 // block's item is the last with block_begin <= blockIdx.x
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
-__global__ void __launch_bounds__(kTileAtoms, min_blocks<MODEL, NSC>())
-sf_grad_batch3(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS>
+__device__ __forceinline__ void sf_grad_batch_body(const SfBatch &B, const SignTable &G)
 {
     const int b = blockIdx.x;
     int lo = 0, hi = B.n - 1;
@@ -947,5 +951,23 @@ sf_grad_batch3(const __grid_constant__ SfBatch B, const __grid_constant__ SignTa
     const int lb = b - B.block_begin[lo];
     sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(it.S, it.C, it.L, G, lb % it.n_tiles, lb / it.n_tiles);
 }
+
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+__global__ void __launch_bounds__(kTileAtoms)
+sf_grad_batch3(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
+{
+    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS>(B, G);
+}
+
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+__global__ void __launch_bounds__(kTileAtoms, 4)
+sf_grad_batch3_occ4(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
+{
+    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS>(B, G);
+}
+
+// kernels that take the four-block minimum
+template <int MODEL, int NSC>
+constexpr bool occ4_kernel() { return MODEL == MODEL_TABLE && NSC > 0 && NSC <= 4; }
 
 }  // namespace dsf
