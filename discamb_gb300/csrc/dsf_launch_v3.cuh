@@ -35,7 +35,7 @@ cudaError_t launch_with(K k, dim3 grid, size_t smem, cudaStream_t st, const Args
 template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
 cudaError_t launch_k3(const K3Args &A)
 {
-    constexpr bool OCC4 = occ4_kernel<MODEL, NSC>();
+    constexpr bool OCC4 = occ4_kernel<R, MODEL, NSC>();
     const dim3 grid = BATCH ? dim3(A.blocks) : dim3(A.n_tiles, A.n_chunks);
     if constexpr (BATCH && OCC4)
         return launch_with(sf_grad_batch3_occ4<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.B, *A.G);

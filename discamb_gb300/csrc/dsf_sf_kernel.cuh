@@ -327,6 +327,11 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     // while the current group runs (coalesced streaming loads, no shared memory,
     // so the sub-tiles stay long); otherwise they are staged by bulk copies
     constexpr bool TAB_REG = TABLE && F32 && NSC > 0;
+    // the four reflections of a group as a loop (one copy of the reflection
+    // body: kernels with eight unrolled operations or the multipole adjoint
+    // otherwise outgrow the instruction cache) or unrolled (small bodies, and
+    // the register-held form factors, which need a compile-time index)
+    constexpr bool ROLL_J = !TAB_REG && (NSC > 4 || MP);
     constexpr bool TAB_SMEM = TABLE && F32 && NSC == 0;
     const StageLayout<R> SL(ht, nS, L.max_types, MP, TAB_SMEM);
     unsigned char *stage0 = smem_raw + 64;
@@ -516,8 +521,8 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             R Fv[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) Fv[q] = R(0);
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
+            // reflection j of the group; its partial F goes to Fv[2j], Fv[2j + 1]
+            auto reflection = [&](const int j) {
                 const int hl = g0 + j;
                 const bool anchor = !REC || sCont[hl] == 0 || hl == 0 || (F32 && (hl % kAnchorF32) == 0);
                 if (active) {
@@ -823,8 +828,15 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         for (int q = 0; q < 3; q++) { Xre[q] *= Tiso; Xim[q] *= Tiso; }
                         if constexpr (MP && !DIAG) { Ere *= Tiso; Eim *= Tiso; Kre *= Tiso; Kim *= Tiso; }
                     }
-                    Fv[2 * j] = w * Ure;
-                    Fv[2 * j + 1] = w * Uim;
+                    if constexpr (ROLL_J) {
+                        const R fv0 = w * Ure, fv1 = w * Uim;
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (q == j) { Fv[2 * q] = fv0; Fv[2 * q + 1] = fv1; }
+                    } else {
+                        Fv[2 * j] = w * Ure;
+                        Fv[2 * j + 1] = w * Uim;
+                    }
                     const R gU = g.x * Ure - g.y * Uim;  // Re(g U)
                     part[CH_OCC] += gU;
                     if constexpr (ANISO) {
@@ -843,6 +855,13 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         part[CH_KAPPA_P] += g.x * Kre - g.y * Kim;
                     }
                 }
+            };
+            if constexpr (ROLL_J) {
+#pragma unroll 1
+                for (int j = 0; j < 4; j++) reflection(j);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; j++) reflection(j);
             }
             // butterfly reduce-scatter of the group's 8 values over the warp:
             // value index 4*bit4 + 2*bit3 + bit2 of the lane ends summed in lanes with bits 1,0 = 0
@@ -966,8 +985,8 @@ sf_grad_batch3_occ4(const __grid_constant__ SfBatch B, const __grid_constant__ S
     sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS>(B, G);
 }
 
-// kernels that take the four-block minimum
-template <int MODEL, int NSC>
-constexpr bool occ4_kernel() { return MODEL == MODEL_TABLE && NSC > 0 && NSC <= 4; }
+// kernels that take the four-block minimum: FP32 tabulated, form factors in registers
+template <typename R, int MODEL, int NSC>
+constexpr bool occ4_kernel() { return sizeof(R) == 4 && MODEL == MODEL_TABLE && NSC > 0 && NSC <= 4; }
 
 }  // namespace dsf
