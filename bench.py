@@ -57,7 +57,7 @@ WORKLOADS = {
                                  "hkl log-uniform 1k-300k, P1/P-1/P21/P21c/P212121/C2c, HC l<=4, aniso U, "
                                  "dF/d(xyz,U,occ)"),
     "config2": dict(seed=2, multipoles=True, flops=195, fp64_frac=0.05, cpu_frac=0.002,
-                    traffic_key="sf_grad_kernel3<float,HC,MP,ANISO,8>@config2",
+                    traffic_key="sf_grad_kernel3<float,HC,MP,ANISO,8,CS4>@config2",
                     desc="config2: HC multipoles l<=4, 50000 atoms (300 types), P43212, all hkl d>=1.2A, aniso U "
                          "(H iso), dF/d(xyz,U,occ,Pv,Plm,kappa,kappa')"),
 }
@@ -482,7 +482,8 @@ def run_config4(args):
                 "h2d_bytes_per_step": sum(16 * st.n_hkl for st in sts),
                 "d2h_bytes_per_step": sum(16 * st.n_hkl + 80 * st.n_atoms for st in sts)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "frac": achieved / peak if peak else None,
+                     "traffic": kernel_traffic("sf_grad_batch3<float,TABLE,ISO+ANISO,4>@config4"),
                      "bytes_per_step": table_bytes + io_bytes, "timed": "whole batched step (CUDA events)"},
         "cpu_baseline": {"value": cpu_terms / t_cpu if t_cpu else None, "unit": "terms/s", "cores": 1,
                          "kind": "port",
