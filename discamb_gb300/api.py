@@ -120,6 +120,7 @@ def library():
         L.dsf_structure_create_tsc.argtypes = [C.c_void_p, _P(_Sym), _P(_Atoms), C.c_int, _P(C.c_int), C.c_char_p,
                                                _P(C.c_void_p)]
         L.dsf_tsc_load.argtypes = [C.c_char_p, _P(C.c_int), _P(C.c_int), _P(C.c_int), _P(C.c_double), C.c_int]
+        L.dsf_form_factors.argtypes = [C.c_void_p, _P(C.c_int), _P(C.c_int), _P(C.c_double)]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
@@ -358,6 +359,27 @@ class _Calculator:
         d_adp = a["d_adp"] + 1j * b["d_adp"]
         return dict(f=a["f"][0], d_xyz=a["d_xyz"] + 1j * b["d_xyz"],
                     d_adp=[d_adp[i, :nadp[i]] for i in range(self.n_atoms)], d_occ=a["d_occ"] + 1j * b["d_occ"])
+
+    def form_factors(self, hkl, include=None):
+        """The single-h calculateFormFactors of the reference
+        (SfCalculator.h:82-93; HansenCoppensStructureFactorCalculator.cpp:
+        1277-1304, AnyIamCalculator.cpp:223-233) through dsf_form_factors:
+        complex form factors of every atom at one reflection ([n_atoms]) or at
+        each of a list ([n][n_atoms]); no anomalous dispersion, 0 for atoms
+        with include[a] == 0.  HC and IAM calculators."""
+        h = np.asarray(hkl, dtype=np.int32)
+        single = h.ndim == 1
+        h = np.ascontiguousarray(h.reshape(-1, 3))
+        n = self.st.n_atoms
+        inc = None
+        if include is not None:
+            inc_arr, inc = _i(np.asarray(include).astype(np.int32))
+        out = np.zeros((len(h), n, 2))
+        for i in range(len(h)):
+            self.engine.check(self.lib.dsf_form_factors(self.h, h[i].ctypes.data_as(_P(C.c_int)), inc,
+                                                        out[i].ctypes.data_as(_P(C.c_double))), "form_factors")
+        ff = out[..., 0] + 1j * out[..., 1]
+        return ff[0] if single else ff
 
     def _out_arrays(self, multipoles):
         n, m = self.n_atoms, self.n_hkl

@@ -40,6 +40,8 @@ cudaError_t launch_global_plm(int n, int K, const int *perm, const int *atom_typ
                               const double *type_plm, const int *type_lmax, const double *fit, double *dmat,
                               double *pg_d, float *pg_f, cudaStream_t st);
 size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types, bool table);
+cudaError_t launch_form_factors(const DevStructure &S, const double *hc, const int *include, double2 *out,
+                                cudaStream_t st);
 cudaError_t launch_sf3(const K3Args &A, int model, bool fp64, bool mp, bool aniso);
 cudaError_t launch_sf_grad(const DevStructure &S, const CallBuffers &C, bool fp64, bool mp, int hkl_chunk, int ht,
                            cudaStream_t st);
@@ -2244,6 +2246,32 @@ int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf
                                                             per_type->d_plm, per_type->d_kappa,
                                                             per_type->d_kappa_prime);
     DSF_CUDA(cudaGetLastError());
+    return DSF_OK;
+}
+
+int dsf_form_factors(dsf_structure *s, const int *hkl, const int *include, double *ff)
+{
+    if (!s || !hkl || !ff) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (s->model == MODEL_TABLE)
+        return fail(e, DSF_ERR_UNSUPPORTED, "form factors at one reflection: HC and IAM structures only");
+    cudaSetDevice(e->device);
+    const int n = s->n_atoms;
+    double hc[3];
+    for (int j = 0; j < 3; j++) hc[j] = s->B[3 * j] * hkl[0] + s->B[3 * j + 1] * hkl[1] + s->B[3 * j + 2] * hkl[2];
+    struct Scratch {  // per call (not hot): freed on every return path
+        DevBuf inc, ff;
+        ~Scratch() { inc.release(); ff.release(); }
+    } sc;
+    DevBuf &d_inc = sc.inc, &d_ff = sc.ff;
+    if (include) {
+        DSF_CUDA(d_inc.alloc(sizeof(int) * (size_t)n));
+        DSF_CUDA(cudaMemcpyAsync(d_inc.p, include, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, e->stream));
+    }
+    DSF_CUDA(d_ff.alloc(sizeof(double2) * (size_t)n));
+    DSF_CUDA(launch_form_factors(s->dev, hc, include ? d_inc.as<int>() : nullptr, d_ff.as<double2>(), e->stream));
+    DSF_CUDA(cudaMemcpyAsync(ff, d_ff.p, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost, e->stream));
+    DSF_CUDA(cudaStreamSynchronize(e->stream));
     return DSF_OK;
 }
 

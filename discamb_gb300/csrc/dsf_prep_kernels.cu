@@ -252,4 +252,54 @@ cudaError_t launch_global_plm(int n, int K, const int *perm, const int *atom_typ
     return cudaGetLastError();
 }
 
+// Form factors of every atom at one reciprocal vector (Cartesian hc), in the
+// caller's atom order, without anomalous dispersion; excluded atoms get 0.
+// HC: f_core + P_val f_val(|h|/kappa) + sum_l i^l 4 pi N_l g_l(|h|/kappa')
+// sum_m P_lm d_lm(h/|h|) with the crystal-frame P_lm (no deformation term at
+// h = 0), as HansenCoppens_SF_Engine::calculateFormFactors
+// (src/Scattering/HansenCoppens_SF_Engine.cpp:383-500, which interpolates the
+// spherical part from splines where this evaluates it); IAM: the n-Gaussian
+// f0(|h|) (IamFormFactorCalculationsManager::calculateCart,
+// src/Scattering/IamFormFactorCalculationsManager.cpp:147-161).
+__global__ void form_factor_kernel(DevStructure S, double hx, double hy, double hz, const int *include,
+                                   double2 *out)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;  // engine (sorted) atom
+    if (a >= S.n_atoms) return;
+    const int orig = S.atom_orig[a];
+    if (include && !include[orig]) {
+        out[orig] = make_double2(0.0, 0.0);
+        return;
+    }
+    int lo = 0, hi = S.n_tiles - 1;  // the atom's tile: last with tile_begin <= a
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (S.tile_begin[mid] <= a) lo = mid;
+        else hi = mid - 1;
+    }
+    const int t = S.tile_types[lo * kMaxTileTypes + S.atom_ltype[a]];
+    const double h2 = hx * hx + hy * hy + hz * hz;
+    double base[8], mpv[8];
+    radial_terms2<double>(S, S.types_d[t], h2, base, mpv, false);
+    double fre = base[0], fim = 0.0;
+    if (S.model == MODEL_HC && h2 > 1e-20) {
+        const double inv = 1.0 / sqrt(h2);
+        double v[25];
+        harmonic_polys<double>(hx * inv, hy * inv, hz * inv, v);
+        const double *pg = S.atom_pg_d + 25 * (size_t)a;
+        double A[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int q = 0; q < 25; q++) A[q < 1 ? 0 : q < 4 ? 1 : q < 9 ? 2 : q < 16 ? 3 : 4] += pg[q] * v[q] * kDensityNorm[q];
+        fre += base[1] * A[0] + base[3] * A[2] + base[5] * A[4];  // signed radial terms r_l = base[1 + l]
+        fim += base[2] * A[1] + base[4] * A[3];
+    }
+    out[orig] = make_double2(fre, fim);
+}
+
+cudaError_t launch_form_factors(const DevStructure &S, const double *hc, const int *include, double2 *out,
+                                cudaStream_t st)
+{
+    form_factor_kernel<<<(S.n_atoms + 127) / 128, 128, 0, st>>>(S, hc[0], hc[1], hc[2], include, out);
+    return cudaGetLastError();
+}
+
 }  // namespace dsf

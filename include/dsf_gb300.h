@@ -34,6 +34,8 @@
  *                               TscFileBasedSfCalculator / tsc_io::read_tsc (the .tsc reader)
  *   dsf_structure_set_electron  HansenCoppensStructureFactorCalculator::setElectronScattering
  *   dsf_reduce_to_types         per-type multipole derivatives for TAAM callers (no reference counterpart)
+ *   dsf_form_factors            SfCalculator::calculateFormFactors(hkl, ff, includeAtom) (SfCalculator.h:82-93;
+ *                               HansenCoppensStructureFactorCalculator.cpp:1277-1304, AnyIamCalculator.cpp:223-233)
  *   dsf_last_error              on_error::throwException messages (include/discamb/BasicUtilities/on_error.h:24-36):
  *                               every function returns a status instead of throwing; the message is the
  *                               calling thread's last one
@@ -227,6 +229,10 @@ int dsf_structure_set_electron(dsf_structure *s, int on, const int *wfn_z, const
  * NULL members are skipped); asynchronous on `stream`.  The reference computes no multipole derivatives; its TAAM
  * callers refine per-type parameters (HcAtomBankStructureFactorCalculator.cpp:482-520). */
 int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf_outputs *per_type, void *stream);
+/* form factors of every atom at one reflection hkl[3] (the reference's single-h calculateFormFactors): ff[2 n_atoms]
+ * (re, im) in the caller's atom order, no anomalous dispersion, 0 for atoms with include[a] == 0 (include may be
+ * NULL); FP64, synchronous.  HC and IAM structures; DSF_ERR_UNSUPPORTED for the tabulated model. */
+int dsf_form_factors(dsf_structure *s, const int *hkl, const int *include, double *ff);
 /* the same with host buffers (dtdf[i] [n_hkl_i][2], include[i] NULL = all atoms, outputs on the host); one
  * stream synchronisation for the whole batch */
 int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int derivative_flags,

@@ -93,6 +93,8 @@ def lib():
         _lib.sfo_g.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double]
         _lib.sfo_g.restype = C.c_double
         _lib.sfo_dlm.argtypes = [_P(C.c_double), _P(C.c_double)]
+        _lib.sfo_form_factors.argtypes = [_P(_Problem), _P(C.c_double), _P(C.c_double)]
+        _lib.sfo_form_factors.restype = C.c_int
     return _lib
 
 
@@ -158,7 +160,7 @@ def hc_model_arrays(st):
 
 
 def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), multipoles=False,
-            iam=None, table=None, hkl_subset=None, loop="direct", electron_f000=None):
+            iam=None, table=None, hkl_subset=None, loop="direct", electron_f000=None, form_factors=False):
     """F and dT/dparam for a Structure at the API level (crystal conventions).
 
     model: 'hc' (HansenCoppens engine: symmetry subset, inversion and
@@ -172,6 +174,9 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     benchmark's CPU baseline).
     electron_f000: per wavefunction, the electron scattering factor at s = 0;
     given, the HC form factors are converted to electron scattering.
+    form_factors: instead, the single-h form factors of every atom at every
+    reflection (sfo_form_factors: no anomalous dispersion, 0 for excluded
+    atoms), complex [n_hkl][n_atoms].
     """
     from discamb_gb300.crystal import (centering_multipliers, convert_adp, convert_adp_gradient,
                                        convert_xyz_gradient)
@@ -263,6 +268,14 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
         pr.electron = 1
         pr.wfn_z = keep.i(np.array([w.atomic_number for w in st.wfns], dtype=np.int32))
         pr.wfn_f000 = keep.d(np.asarray(electron_f000, dtype=np.float64))
+    if form_factors:
+        ff = np.zeros((len(hkl), n, 2))
+        for i in range(len(hkl)):
+            hv = np.ascontiguousarray(hc[i], dtype=np.float64)
+            if lib().sfo_form_factors(C.byref(pr), hv.ctypes.data_as(_P(C.c_double)),
+                                      ff[i].ctypes.data_as(_P(C.c_double))) != 0:
+                raise RuntimeError("oracle form factors failed")
+        return ff[..., 0] + 1j * ff[..., 1]
     out = dict(f=np.zeros(2 * len(hkl)), d_xyz=np.zeros(3 * n), d_adp=np.zeros(6 * n), d_occ=np.zeros(n),
                d_pval=np.zeros(n), d_plm=np.zeros(25 * n), d_kappa=np.zeros(n), d_kappa_p=np.zeros(n))
     res = _Result()

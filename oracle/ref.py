@@ -158,6 +158,23 @@ def iam(st, labels, table="IT92", n_threads=1):
     return _pack(out, st, ms.value)
 
 
+def form_factors(st, labels=None, table="IT92"):
+    """The reference's single-h calculateFormFactors at every reflection of st:
+    complex [n_hkl][n_atoms] (include mask of st).  HC structures through
+    HansenCoppensStructureFactorCalculator; with labels, the IAM path of
+    AnyIamCalculator with that n-Gaussian table."""
+    ff = np.zeros((st.n_hkl, st.n_atoms, 2))
+    lib().ref_set_form_factor_out(ff.ctypes.data_as(C.POINTER(C.c_double)))
+    try:
+        if labels is None:
+            hc(st)
+        else:
+            iam(st, labels, table)
+    finally:
+        lib().ref_set_form_factor_out(None)
+    return ff[..., 0] + 1j * ff[..., 1]
+
+
 def table(st, keys, values):
     """keys: (k,3) int Miller indices, values: (k, n_atoms) complex.  The
     generic engine builds a default IAM manager from the atom labels before

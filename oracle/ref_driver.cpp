@@ -118,6 +118,15 @@ int ref_set_def_val_symm(int on)
     return 0;
 }
 
+// single-h form factors: while set, ref_hc_sf and ref_iam_sf also write calculateFormFactors(h_i) for every
+// input reflection into g_ff_out ([n_hkl][n_atoms][re, im], include mask of the call)
+static double *g_ff_out = nullptr;
+int ref_set_form_factor_out(double *ff_out)
+{
+    g_ff_out = ff_out;
+    return 0;
+}
+
 // Hansen-Coppens path through HansenCoppensStructureFactorCalculator ("CPU").
 // Wavefunctions as Slater orbitals: per wfn [orb_off[w], orb_off[w+1]) orbitals,
 // per orbital [sto_off[o], sto_off[o+1]) Slater functions.
@@ -201,6 +210,16 @@ int ref_hc_sf(const double *cell, const char *ops, int n_atoms, const double *xy
         auto t0 = std::chrono::steady_clock::now();
         calc.calculateStructureFactorsAndDerivatives(crystal.atoms, lcsm, h, f, d, g, inc);
         auto t1 = std::chrono::steady_clock::now();
+        if (g_ff_out) {
+            vector<complex<double> > ff;
+            for (int i = 0; i < n_hkl; i++) {
+                calc.calculateFormFactors(lcsm, h[i], ff, inc);
+                for (int a = 0; a < n_atoms; a++) {
+                    g_ff_out[2 * ((size_t)i * n_atoms + a)] = ff[a].real();
+                    g_ff_out[2 * ((size_t)i * n_atoms + a) + 1] = ff[a].imag();
+                }
+            }
+        }
         if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         write_out(f, d, f_out, d_xyz, d_adp, d_occ);
         return 0;
@@ -258,6 +277,16 @@ int ref_iam_sf(const double *cell, const char *ops, const char *labels, const ch
         auto t0 = std::chrono::steady_clock::now();
         calc.calculateStructureFactorsAndDerivatives(h, f, d, g, inc);
         auto t1 = std::chrono::steady_clock::now();
+        if (g_ff_out) {
+            vector<complex<double> > ff;
+            for (int i = 0; i < n_hkl; i++) {
+                calc.calculateFormFactors(h[i], ff, inc);
+                for (int a = 0; a < n_atoms; a++) {
+                    g_ff_out[2 * ((size_t)i * n_atoms + a)] = ff[a].real();
+                    g_ff_out[2 * ((size_t)i * n_atoms + a) + 1] = ff[a].imag();
+                }
+            }
+        }
         if (ms) *ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
         write_out(f, d, f_out, d_xyz, d_adp, d_occ);
         return 0;

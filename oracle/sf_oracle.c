@@ -166,6 +166,101 @@ static int type_lmax_used(const sfo_problem *p, int t, int w)
     return lp < lm ? lp : lm;
 }
 
+/* radial terms at |h| = hl per wavefunction / type: HC f_core[w], f_val[t] (and d/dkappa), the normalised
+ * deformation radial functions g_l[t][5] (and d/dkappa'); IAM: f0[t] in fval (the reference's pre_hkl_loop_sf_calc,
+ * HansenCoppens_SF_Engine3.cpp:195-256, and NGaussianFormFactor::calculate_h) */
+static void radial_terms(const sfo_problem *p, const int *type_wfn, double hl, double *fcore, double *fval,
+                         double *dfval, double *gl, double *dgl)
+{
+    if (p->model == SFO_MODEL_HC) {
+        for (int w = 0; w < p->n_wfn; w++) {
+            double s = 0.0;
+            for (int k = p->core_off[w]; k < p->core_off[w + 1]; k++)
+                s += p->core_coeff[k] * sfo_g(0, p->core_pow[k] + 2, hl, p->core_exp[k]);
+            fcore[w] = 4.0 * PI * s;
+        }
+        for (int ty = 0; ty < p->n_types; ty++) {
+            const int w = type_wfn[ty];
+            const double kap = p->type_kappa[ty], kp = p->type_kappa_p[ty];
+            double s = 0.0, ds = 0.0;
+            for (int k = p->val_off[w]; k < p->val_off[w + 1]; k++) {
+                s += p->val_coeff[k] * sfo_g(0, p->val_pow[k] + 2, hl / kap, p->val_exp[k]);
+                ds += p->val_coeff[k] * g_dh(0, p->val_pow[k] + 2, hl / kap, p->val_exp[k]);
+            }
+            fval[ty] = 4.0 * PI * s;
+            dfval[ty] = 4.0 * PI * ds * (-hl / (kap * kap)); /* d f_val / d kappa */
+            const double zeta = p->def_exp[w];
+            for (int l = 0; l < 5; l++) {
+                gl[ty * 5 + l] = 0.0;
+                dgl[ty * 5 + l] = 0.0;
+                if (l < p->def_npow[w]) {
+                    const int nl = p->def_pow[w * 5 + l];
+                    double norm = pow(zeta, nl + 3);
+                    for (int q = 2; q <= nl + 2; q++) norm /= q;
+                    gl[ty * 5 + l] = norm * sfo_g(l, nl + 2, hl / kp, zeta);
+                    dgl[ty * 5 + l] = norm * g_dh(l, nl + 2, hl / kp, zeta) * (-hl / (kp * kp));
+                }
+            }
+        }
+    } else if (p->model == SFO_MODEL_IAM) {
+        for (int ty = 0; ty < p->n_types; ty++) {
+            double s = p->iam_c[ty];
+            const double x2 = hl * hl / 4.0;
+            for (int q = 0; q < p->iam_ngauss[ty]; q++) s += p->iam_a[ty * 5 + q] * exp(-p->iam_b[ty * 5 + q] * x2);
+            fval[ty] = s;
+        }
+    }
+}
+
+/* form factors of every atom at one Cartesian reciprocal vector h (the reference's single-h calculateFormFactors:
+ * HansenCoppens_SF_Engine::calculateFormFactors, HansenCoppens_SF_Engine.cpp:383-500; IAM through
+ * IamFormFactorCalculationsManager::calculateCart, IamFormFactorCalculationsManager.cpp:147-161): no anomalous
+ * dispersion, no deformation term at h = 0, 0 for excluded atoms; ff [n_atoms][re, im] */
+int sfo_form_factors(const sfo_problem *p, const double h[3], double *ff)
+{
+    if (p->model != SFO_MODEL_HC && p->model != SFO_MODEL_IAM) return 1;
+    g_init();
+    const int nA = p->n_atoms;
+    const int nT = p->n_types > 0 ? p->n_types : 1, nW = p->n_wfn > 0 ? p->n_wfn : 1;
+    int *type_wfn = (int *)calloc((size_t)nT, sizeof(int));
+    double *fcore = (double *)calloc((size_t)nW, sizeof(double));
+    double *fval = (double *)calloc((size_t)nT, sizeof(double));
+    double *dfval = (double *)calloc((size_t)nT, sizeof(double));
+    double *gl = (double *)calloc((size_t)nT * 5, sizeof(double));
+    double *dgl = (double *)calloc((size_t)nT * 5, sizeof(double));
+    if (!type_wfn || !fcore || !fval || !dfval || !gl || !dgl) return 1;
+    for (int a = 0; a < nA; a++) type_wfn[p->atom_type[a]] = p->atom_wfn[a];
+    const double hl = sqrt(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]);
+    radial_terms(p, type_wfn, hl, fcore, fval, dfval, gl, dgl);
+    for (int a = 0; a < nA; a++) {
+        cplx f = {0.0, 0.0};
+        if (p->include[a]) {
+            const int w = p->atom_wfn[a], ty = p->atom_type[a];
+            if (p->model == SFO_MODEL_IAM) {
+                f.re = fval[ty];
+            } else {
+                f.re = fcore[w] + fval[ty] * p->type_pval[ty];
+                const int lmax_use = type_lmax_used(p, ty, w);
+                if (hl >= 1e-10 && type_lmax_params(p, ty, w) >= 0) {
+                    const double *L = p->lcs + 9 * a, *P = p->type_plm + 25 * ty;
+                    double u[3], d[25];
+                    for (int j = 0; j < 3; j++) u[j] = (L[0 + j] * h[0] + L[3 + j] * h[1] + L[6 + j] * h[2]) / hl;
+                    sfo_dlm(u, d);
+                    for (int l = 0; l <= lmax_use; l++) {
+                        double ang = 0.0;
+                        for (int m = 0; m < 2 * l + 1; m++) ang += P[l * l + m] * d[l * l + m];
+                        f = cadd(f, cscale(IPOW[l], 4.0 * PI * gl[ty * 5 + l] * ang));
+                    }
+                }
+            }
+        }
+        ff[2 * a] = f.re;
+        ff[2 * a + 1] = f.im;
+    }
+    free(type_wfn); free(fcore); free(fval); free(dfval); free(gl); free(dgl);
+    return 0;
+}
+
 int sfo_compute(const sfo_problem *p, sfo_result *r, int n_threads)
 {
     g_init();
@@ -211,46 +306,7 @@ int sfo_compute(const sfo_problem *p, sfo_result *r, int n_threads)
                 for (int j = 0; j < 3; j++) hr[3 * s + j] = h[0] * R[j] + h[1] * R[3 + j] + h[2] * R[6 + j];
                 tf[s] = h[0] * t[0] + h[1] * t[1] + h[2] * t[2];
             }
-            /* radial terms per wavefunction / type */
-            if (p->model == SFO_MODEL_HC) {
-                for (int w = 0; w < p->n_wfn; w++) {
-                    double s = 0.0;
-                    for (int k = p->core_off[w]; k < p->core_off[w + 1]; k++)
-                        s += p->core_coeff[k] * sfo_g(0, p->core_pow[k] + 2, hl, p->core_exp[k]);
-                    fcore[w] = 4.0 * PI * s;
-                }
-                for (int ty = 0; ty < p->n_types; ty++) {
-                    const int w = type_wfn[ty];
-                    const double kap = p->type_kappa[ty], kp = p->type_kappa_p[ty];
-                    double s = 0.0, ds = 0.0;
-                    for (int k = p->val_off[w]; k < p->val_off[w + 1]; k++) {
-                        s += p->val_coeff[k] * sfo_g(0, p->val_pow[k] + 2, hl / kap, p->val_exp[k]);
-                        ds += p->val_coeff[k] * g_dh(0, p->val_pow[k] + 2, hl / kap, p->val_exp[k]);
-                    }
-                    fval[ty] = 4.0 * PI * s;
-                    dfval[ty] = 4.0 * PI * ds * (-hl / (kap * kap)); /* d f_val / d kappa */
-                    const double zeta = p->def_exp[w];
-                    for (int l = 0; l < 5; l++) {
-                        gl[ty * 5 + l] = 0.0;
-                        dgl[ty * 5 + l] = 0.0;
-                        if (l < p->def_npow[w]) {
-                            const int nl = p->def_pow[w * 5 + l];
-                            double norm = pow(zeta, nl + 3);
-                            for (int q = 2; q <= nl + 2; q++) norm /= q;
-                            gl[ty * 5 + l] = norm * sfo_g(l, nl + 2, hl / kp, zeta);
-                            dgl[ty * 5 + l] = norm * g_dh(l, nl + 2, hl / kp, zeta) * (-hl / (kp * kp));
-                        }
-                    }
-                }
-            } else if (p->model == SFO_MODEL_IAM) {
-                for (int ty = 0; ty < p->n_types; ty++) {
-                    double s = p->iam_c[ty];
-                    const double x2 = hl * hl / 4.0;
-                    for (int q = 0; q < p->iam_ngauss[ty]; q++)
-                        s += p->iam_a[ty * 5 + q] * exp(-p->iam_b[ty * 5 + q] * x2);
-                    fval[ty] = s;
-                }
-            }
+            radial_terms(p, type_wfn, hl, fcore, fval, dfval, gl, dgl);
             /* centrosymmetric handling: e^{2 pi i h.t_inv} */
             double ph_inv = 2.0 * PI * (h[0] * p->inv_trans[0] + h[1] * p->inv_trans[1] + h[2] * p->inv_trans[2]);
             const cplx cinv = {cos(ph_inv), sin(ph_inv)};

@@ -104,6 +104,8 @@ int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sf
 
 /* int_0^inf r^n exp(-z r) j_l(2 pi h r) dr, 0<=l<=5, l+1<=n<=12 */
 double sfo_g(int l, int n, double h, double z);
+/* form factors of every atom at one Cartesian reciprocal vector h[3]: ff[n_atoms][re, im] (HC, IAM) */
+int sfo_form_factors(const sfo_problem *p, const double h[3], double *ff);
 
 /* density-normalised real spherical harmonics d_lm(u), l<=4, u normalised */
 void sfo_dlm(const double u[3], double out[25]);

@@ -2,7 +2,7 @@
 library's own CPU code (oracle/_ref/libref_driver.so, built from the
 reference sources by oracle/Makefile.ref) on seeded synthetic structures.
 
-    python tests/golden/make_golden.py [hc|def_val_symm|rest ...]   (default: all)
+    python tests/golden/make_golden.py [hc|def_val_symm|form_factors|rest ...]   (default: all)
 
 Each fixture (.npz) holds every input of the case (structure_to_arrays) and
 the reference outputs: F, d_xyz, d_adp, d_occ in the crystal's conventions.
@@ -223,7 +223,35 @@ def write_rest():
     print("wrote table_p21c")
 
 
-GROUPS = {"hc": write_hc, "def_val_symm": write_def_val_symm, "rest": write_rest}
+def write_form_factors():
+    """The reference's single-h calculateFormFactors (no anomalous dispersion,
+    0 for excluded atoms) at every reflection of a small HC structure (000
+    included) and of an IAM structure (IT92)."""
+    st = W.small_case("P21/c", n_atoms=5, stol_max=0.5, seed=801, improper_lcs=True)
+    st.hkl = np.concatenate([np.zeros((1, 3), dtype=np.int32), st.hkl[:40]])
+    st.dtdf = np.concatenate([[1.0 + 0j], st.dtdf[:40]])
+    st.include = np.array([1, 1, 0, 1, 1], dtype=bool)
+    out = structure_to_arrays(st)
+    out.update(ref_ff=R.form_factors(st))
+    np.savez_compressed(os.path.join(HERE, "ff_hc_p21c.npz"), **out)
+    print("wrote ff_hc_p21c", st.n_atoms, st.n_hkl)
+    st = W.small_case("C2/c", n_atoms=6, stol_max=0.6, seed=802)
+    st.hkl, st.dtdf = st.hkl[:40], st.dtdf[:40]
+    labels = [w.label for w in st.wfns]
+    ng, ga, gb, gc = [], np.zeros((len(labels), 5)), np.zeros((len(labels), 5)), []
+    for i, lab in enumerate(labels):
+        a_, b_, c_ = R.iam_coefficients(lab, "IT92")
+        ng.append(len(a_)); ga[i, :len(a_)] = a_; gb[i, :len(b_)] = b_; gc.append(c_)
+    st.atom_type = st.atom_wfn.copy()
+    out = structure_to_arrays(st)
+    out.update(iam_ngauss=np.array(ng), iam_a=ga, iam_b=gb, iam_c=np.array(gc),
+               ref_ff=R.form_factors(st, labels=[st.wfns[w].label for w in st.atom_wfn]))
+    np.savez_compressed(os.path.join(HERE, "ff_iam_c2c.npz"), **out)
+    print("wrote ff_iam_c2c", st.n_atoms, st.n_hkl)
+
+
+GROUPS = {"hc": write_hc, "def_val_symm": write_def_val_symm, "form_factors": write_form_factors,
+          "rest": write_rest}
 
 
 def main(groups):

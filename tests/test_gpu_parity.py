@@ -328,3 +328,26 @@ def test_single_reflection_derivatives(engine):
     again = calc.calculate(st.dtdf, precision=FP64, atoms=(st.xyz, st.adp, st.occupancy))
     assert rel_f(again["f"], full["f"]) < 1e-13
     calc.close()
+
+
+def test_single_h_form_factors(engine):
+    # dsf_form_factors against the reference's single-h calculateFormFactors (per atom at each reflection, 000
+    # included, one excluded atom) and, for one reflection with every atom included, against the oracle
+    st, d = load_fixture("ff_hc_p21c")
+    calc = api.HcCalculator(engine, st)
+    inc = st.include_mask().astype(np.int32)
+    ff = calc.form_factors(st.hkl, include=inc)
+    ref = d["ref_ff"]
+    assert np.abs(ff - ref).max() <= 1e-10 * np.abs(ref).max()
+    assert np.all(ff[:, inc == 0] == 0)
+    one = calc.form_factors(st.hkl[3])
+    st_all = copy.deepcopy(st)
+    st_all.include = None
+    o = O.compute(st_all, form_factors=True, hkl_subset=[3])[0]
+    assert np.abs(one - o).max() <= 1e-10 * np.abs(o).max()
+    calc.close()
+    st, d = load_fixture("ff_iam_c2c")
+    calc = api.IamCalculator(engine, st, iam_dict(d))
+    ff = calc.form_factors(st.hkl)
+    assert np.abs(ff - d["ref_ff"]).max() <= 1e-12 * np.abs(d["ref_ff"]).max()
+    calc.close()

@@ -126,3 +126,14 @@ def test_electron_multipole_derivatives_by_finite_differences():
                 ana = r["d_plm"][a][q]
             fd = (target(s1) - target(s2)) / (2 * h)
             assert abs(fd - ana) <= 1e-8 * max(1.0, abs(ana)), (a, q, fd, ana)
+
+
+def test_single_h_form_factors_match_reference():
+    # the reference's single-h calculateFormFactors (HC: 000 included, one excluded atom; IAM: IT92)
+    st, d = load_fixture("ff_hc_p21c")
+    o = O.compute(st, form_factors=True)
+    assert np.abs(o - d["ref_ff"]).max() <= 1e-11 * np.abs(d["ref_ff"]).max()
+    assert np.all(o[:, ~st.include_mask()] == 0)
+    st, d = load_fixture("ff_iam_c2c")
+    o = O.compute(st, model="iam", iam=iam_dict(d), form_factors=True)
+    assert np.abs(o - d["ref_ff"]).max() <= 1e-13 * np.abs(d["ref_ff"]).max()
