@@ -67,6 +67,21 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def aggregate_ranks(terms, times_ms, world, device=None):
+    """Weak-scaling replicas (every rank runs its own structure; no data
+    exchange): the whole job's terms (sum over ranks) and each timing as the
+    max over ranks (one all-reduce each; NCCL on GPUs, gloo on CPU).  Returns
+    (total_terms, [max times])."""
+    import torch
+    t = torch.tensor(list(times_ms), dtype=torch.float64, device=device)
+    n = torch.tensor([float(terms)], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return n.item(), t.tolist()
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle samples while the timed region runs."""
 
@@ -644,12 +659,8 @@ def run_gpu(args):
     step64 = statistics.mean(ms64)
     k32 = statistics.mean(kern32)
     # weak scaling: every rank runs its own replica; max time over ranks
-    tot = torch.tensor([step32, statistics.mean(e2e) * 1e3, k32], dtype=torch.float64, device=dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(tot, op=dist.ReduceOp.MAX)
-    step32, e2e_ms, k32 = tot.tolist()
-    value = world * terms / (step32 * 1e-3)
+    job_terms, (step32, e2e_ms, k32) = aggregate_ranks(terms, [step32, statistics.mean(e2e) * 1e3, k32], world, dev)
+    value = job_terms / (step32 * 1e-3)
     if rank != 0:
         return 0
     achieved = wl["flops"] * terms / (k32 * 1e-3) * 1e-12
@@ -667,7 +678,7 @@ def run_gpu(args):
                  "kernel_ms": statistics.mean(kern64),
                  "fp32_over_fp64": (terms / step32) / (terms64 / step64),
                  "sample": "all reflections" if frac64 >= 1.0 else f"first {frac64:.0%} of the reflections"},
-        "e2e": {"value": world * terms / (e2e_ms * 1e-3), "unit": "terms/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": job_terms / (e2e_ms * 1e-3), "unit": "terms/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": kernel_traffic(wl["traffic_key"]),
