@@ -911,7 +911,7 @@ void refresh_dev(dsf_structure *s);
 int ensure_tables(dsf_structure *s, bool fp64, bool mp)
 {
     dsf_engine *e = s->eng;
-    if (!s->have_hkl) return DSF_OK;
+    if (!s->have_hkl || s->n_hkl == 0) return DSF_OK;  // an empty reflection set has no tables
     const int p = fp64 ? 1 : 0;
     const size_t esz = fp64 ? sizeof(double) : sizeof(float);
     const size_t row = 8 * (size_t)s->n_hkl_pad * std::max(1, s->n_types);
@@ -1521,10 +1521,20 @@ int dsf_structure_set_hkl(dsf_structure *s, int n_hkl, const int *hkl)
 {
     if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
-    if (n_hkl < 1 || !hkl) return fail(e, DSF_ERR_ARGUMENT, "need at least one reflection");
+    if (n_hkl < 0 || (n_hkl > 0 && !hkl)) return fail(e, DSF_ERR_ARGUMENT, "bad reflection list");
     if (s->model == MODEL_TABLE && s->have_hkl && n_hkl != s->n_hkl)
         return fail(e, DSF_ERR_ARGUMENT, "tabulated structures keep the reflection set of their table");
     cudaSetDevice(e->device);
+    if (n_hkl == 0) {
+        // an empty set, as the reference accepts it: calls return no F and zero derivatives
+        s->hperm.clear();
+        s->n_hkl = 0;
+        s->n_hkl_pad = 0;
+        s->have_hkl = true;
+        for (int p = 0; p < 2; p++) s->rs_ok[p] = s->tr_ok[p] = s->trm_ok[p] = false;
+        refresh_dev(s);
+        return DSF_OK;
+    }
     // tables and per-reflection arrays padded with zero rows to whole sub-tiles (ht divides kMaxHT)
     const int n_pad = (n_hkl + kMaxHT - 1) / kMaxHT * kMaxHT;
     // line order: sorted by (h, k, l) so runs of l + 1 share a lattice line
@@ -1745,7 +1755,8 @@ static int call_check(dsf_structure *s, int precision, int flags, const double *
     dsf_engine *e = s->eng;
     if (!s->have_hkl) return fail(e, DSF_ERR_STATE, "no reflections set");
     if (!s->have_atoms) return fail(e, DSF_ERR_STATE, "atomic parameters not uploaded");
-    if (!out || !out->f || !dtdf_device) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
+    if (!out || (s->n_hkl > 0 && (!out->f || !dtdf_device)))
+        return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
     if (precision != DSF_FP64 && precision != DSF_FP32_BULK) return fail(e, DSF_ERR_ARGUMENT, "unknown precision");
     const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
     return ensure_tables(s, precision == DSF_FP64, mp);
@@ -1860,6 +1871,24 @@ static int call_post(dsf_structure *s, int flags, const dsf_outputs *out, cudaSt
     return DSF_OK;
 }
 
+// a call on an empty reflection set: no F, the requested derivatives zero (the reference's engines sum over no
+// reflections); no kernels
+static int empty_call(dsf_structure *s, int flags, const dsf_outputs *out, cudaStream_t st)
+{
+    dsf_engine *e = s->eng;
+    const size_t n = (size_t)s->n_atoms;
+    const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
+    struct { double *p; size_t len; bool want; } z[] = {
+        {out->d_xyz, 3 * n, (flags & DSF_D_XYZ) != 0}, {out->d_adp, 6 * n, (flags & DSF_D_ADP) != 0},
+        {out->d_occ, n, (flags & DSF_D_OCC) != 0},     {out->d_pval, n, mp},
+        {out->d_plm, 25 * n, mp},                       {out->d_kappa, n, mp},
+        {out->d_kappa_prime, n, mp}};
+    for (auto &q : z)
+        if (q.want && q.p) DSF_CUDA(cudaMemsetAsync(q.p, 0, sizeof(double) * q.len, st));
+    s->last_launches = 0;
+    return DSF_OK;
+}
+
 int dsf_calculate_device(dsf_structure *s, int precision, int flags, const double *dtdf_device,
                          const dsf_outputs *out, void *stream)
 {
@@ -1869,6 +1898,7 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     if (rc) return rc;
     cudaSetDevice(e->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    if (s->n_hkl == 0) return empty_call(s, flags, out, st);
     const bool fp64 = precision == DSF_FP64;
     const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
     if ((rc = call_pre(s, dtdf_device, st))) return rc;
@@ -1923,14 +1953,33 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
     if (!structures || n < 1 || !dtdf_device || !out_device) return DSF_ERR_ARGUMENT;
     dsf_engine *e = structures[0] ? structures[0]->eng : nullptr;
     if (!e) return DSF_ERR_ARGUMENT;
+    int n_empty = 0;
     for (int i = 0; i < n; i++) {
         if (!structures[i] || structures[i]->eng != e)
             return fail(e, DSF_ERR_ARGUMENT, "batch structures must belong to one engine");
         int rc = call_check(structures[i], precision, flags, dtdf_device[i], &out_device[i]);
         if (rc) return rc;
+        n_empty += structures[i]->n_hkl == 0;
     }
     cudaSetDevice(e->device);
     cudaStream_t st = stream ? (cudaStream_t)stream : e->stream;
+    if (n_empty) {  // structures with an empty reflection set: zero derivatives; the rest as a batch
+        std::vector<dsf_structure *> sv;
+        std::vector<const double *> dv;
+        std::vector<dsf_outputs> ov;
+        for (int i = 0; i < n; i++) {
+            if (structures[i]->n_hkl == 0) {
+                int rc = empty_call(structures[i], flags, &out_device[i], st);
+                if (rc) return rc;
+            } else {
+                sv.push_back(structures[i]);
+                dv.push_back(dtdf_device[i]);
+                ov.push_back(out_device[i]);
+            }
+        }
+        if (sv.empty()) return DSF_OK;
+        return dsf_calculate_batch_device(sv.data(), (int)sv.size(), precision, flags, dv.data(), ov.data(), st);
+    }
     const bool fp64 = precision == DSF_FP64;
     int launches = 0, rc;
     // adjoint weights and zeroed accumulators of all structures, kPrePostItems per launch
@@ -2115,8 +2164,8 @@ static int host_stage(dsf_structure *s, const double *xyz, const double *adp, co
 {
     if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
-    if (!out || !out->f || !dtdf) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
     if (!s->have_hkl) return fail(e, DSF_ERR_STATE, "no reflections set");
+    if (!out || (s->n_hkl > 0 && (!out->f || !dtdf))) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
     if ((xyz != nullptr) != (occ != nullptr)) return fail(e, DSF_ERR_ARGUMENT, "xyz and occupancy go together");
     cudaSetDevice(e->device);
     const int n_hkl = s->n_hkl, n = s->n_atoms;
@@ -2165,8 +2214,10 @@ static int host_stage(dsf_structure *s, const double *xyz, const double *adp, co
         DSF_CUDA(cudaGetLastError());
         s->have_atoms = true;
     }
-    std::memcpy(pg, dtdf, sizeof(double) * 2 * (size_t)n_hkl);
-    DSF_CUDA(cudaMemcpyAsync(s->d_dtdf.p, pg, 16 * (size_t)n_hkl, cudaMemcpyHostToDevice, e->stream));
+    if (n_hkl > 0) {
+        std::memcpy(pg, dtdf, sizeof(double) * 2 * (size_t)n_hkl);
+        DSF_CUDA(cudaMemcpyAsync(s->d_dtdf.p, pg, 16 * (size_t)n_hkl, cudaMemcpyHostToDevice, e->stream));
+    }
     double *base = s->d_out.as<double>();
     dsf_outputs &d = hc.d;
     d.f = base;
@@ -2203,7 +2254,7 @@ static int host_finish(dsf_structure *s, int flags, const HostCall &hc, const ds
         cudaMemsetAsync(s->d_err.p, 0, sizeof(int), e->stream);
         return fail(e, DSF_ERR_TIMEOUT, "a shared-memory pipeline wait of the kernel ran out");
     }
-    std::memcpy(out->f, hc.po, sizeof(double) * hc.nf);
+    if (hc.nf) std::memcpy(out->f, hc.po, sizeof(double) * hc.nf);
     const double *q = hc.po + hc.nf;
     struct { double *dst; size_t off, n; } cp[] = {
         {out->d_xyz, 0, 3 * (size_t)n}, {out->d_adp, 3 * (size_t)n, 6 * (size_t)n},

@@ -351,3 +351,28 @@ def test_single_h_form_factors(engine):
     ff = calc.form_factors(st.hkl)
     assert np.abs(ff - d["ref_ff"]).max() <= 1e-12 * np.abs(d["ref_ff"]).max()
     calc.close()
+
+
+def test_empty_reflection_set(engine):
+    # the reference sums over no reflections: no F, zero derivatives (HansenCoppens_SF_Engine3.cpp:678-950 with an
+    # empty hkl list); here alone, in a batch beside a full structure, and switching back to the full set
+    st = W.small_case("P21/c", n_atoms=5, stol_max=0.4, seed=61)
+    calc = api.HcCalculator(engine, st)
+    full = calc.calculate(st.dtdf, precision=FP64)
+    calc.set_hkl(np.zeros((0, 3), dtype=np.int32))
+    for prec in (FP64, FP32):
+        r = calc.calculate(np.zeros(0, dtype=complex), precision=prec, multipoles=True)
+        assert r["f"].shape == (0,)
+        for k in ("d_xyz", "d_occ", "d_pval", "d_plm", "d_kappa", "d_kappa_p"):
+            assert np.all(np.asarray(r[k]) == 0), k
+        assert all(np.all(v == 0) for v in r["d_adp"])
+    other = api.HcCalculator(engine, st)
+    b = engine.calculate_batch([calc, other], [np.zeros(0, dtype=complex), st.dtdf], precision=FP64)
+    assert b[0]["f"].shape == (0,) and np.all(b[0]["d_xyz"] == 0)
+    assert rel_f(b[1]["f"], full["f"]) < 1e-13
+    calc.set_hkl(st.hkl)
+    again = calc.calculate(st.dtdf, precision=FP64)
+    assert rel_f(again["f"], full["f"]) < 1e-13
+    assert rel_norm(again["d_xyz"], full["d_xyz"]) < 1e-13
+    other.close()
+    calc.close()
