@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdsf_gb300.so")
 PEAK_LIB = os.path.join(HERE, "libdsf_peak_probe.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["dsf_kernels.cu", "dsf_k3_f32_hc.cu", "dsf_k3_f32_hc_mp.cu", "dsf_k3_f32_other.cu", "dsf_k3b_f32.cu", "dsf_k3_f64.cu", "dsf_prep_kernels.cu", "dsf_engine.cu", "dsf_noalloc.cu", "dsf_tsc.cu"]
+SOURCES = ["dsf_kernels.cu", "dsf_k3_f32_hc.cu", "dsf_k3_f32_hc_mp.cu", "dsf_k3_f32_other.cu", "dsf_k3b_f32.cu", "dsf_k3_f64.cu", "dsf_prep_kernels.cu", "dsf_engine.cu", "dsf_noalloc.cu", "dsf_tsc.cu", "dsf_k3f_hc.cu", "dsf_k3f_other.cu"]
 
 
 def _nvcc():

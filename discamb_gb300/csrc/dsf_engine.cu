@@ -1933,6 +1933,7 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         A.n_chunks = n_chunks;
         A.smem = smem;
         A.st = st;
+        A.grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
         DSF_CUDA(launch_sf3(A, s->model, fp64, mp, kind == 1));
         launches++;
     }

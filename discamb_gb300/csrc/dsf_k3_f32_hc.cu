@@ -8,10 +8,10 @@ cudaError_t launch_k3_f32_hc(const K3Args &A, bool mp, bool aniso)
 {
     if (mp) return launch_k3_f32_hc_mp(A, aniso);
     if (A.coset)
-        return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
-                     : dispatch_coset<false, float, MODEL_HC, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);
-    return aniso ? dispatch_k3<false, float, MODEL_HC, false, true, 2, 4, 8>(A)
-                 : dispatch_k3<false, float, MODEL_HC, false, false, 2, 4, 8>(A);
+        return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
+                     : dispatch_coset<false, float, MODEL_HC, false, false, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);
+    return aniso ? dispatch_k3<false, float, MODEL_HC, false, true, true, 2, 4, 8>(A)
+                 : dispatch_k3<false, float, MODEL_HC, false, false, true, 2, 4, 8>(A);
 }
 
 size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types, bool table)
@@ -25,6 +25,7 @@ cudaError_t launch_sf3(const K3Args &A, int model, bool fp64, bool mp, bool anis
 {
     const bool mp_hc = mp && model == MODEL_HC;
     if (fp64) return launch_k3_f64(A, model, mp_hc, aniso);
+    if (!A.grad && !mp_hc) return model == MODEL_HC ? launch_k3f_hc(A, aniso) : launch_k3f_other(A, model, aniso);
     if (model == MODEL_HC) return launch_k3_f32_hc(A, mp_hc, aniso);
     return launch_k3_f32_other(A, model, aniso);
 }

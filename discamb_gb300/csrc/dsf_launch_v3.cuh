@@ -18,6 +18,7 @@ struct K3Args {
     const SignTable *G = nullptr;
     const SfBatch *B = nullptr;
     int n_sym = 0, coset = 0;
+    bool grad = true;  // false: structure factors only (single-structure FP32 kernels without the adjoint)
     int n_tiles = 0, n_chunks = 0, blocks = 0;
     size_t smem = 0;
     cudaStream_t st = nullptr;
@@ -32,12 +33,19 @@ cudaError_t launch_with(K k, dim3 grid, size_t smem, cudaStream_t st, const Args
     return cudaGetLastError();
 }
 
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, int NSC, int CS = 0>
 cudaError_t launch_k3(const K3Args &A)
 {
     constexpr bool OCC4 = occ4_kernel<R, MODEL, NSC>();
     const dim3 grid = BATCH ? dim3(A.blocks) : dim3(A.n_tiles, A.n_chunks);
-    if constexpr (BATCH && OCC4)
+    static_assert(GRAD || !BATCH, "structure-factor-only kernels: single structures");
+    if constexpr (!GRAD && OCC4)
+        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS, false>, grid, A.smem, A.st, *A.S, *A.C,
+                           *A.L, *A.G);
+    else if constexpr (!GRAD)
+        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS, false>, grid, A.smem, A.st, *A.S, *A.C, *A.L,
+                           *A.G);
+    else if constexpr (BATCH && OCC4)
         return launch_with(sf_grad_batch3_occ4<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.B, *A.G);
     else if constexpr (BATCH)
         return launch_with(sf_grad_batch3<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.B, *A.G);
@@ -48,33 +56,33 @@ cudaError_t launch_k3(const K3Args &A)
 }
 
 // compiled operation counts first, runtime count last
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD>
 cudaError_t dispatch_k3(const K3Args &A)
 {
-    return launch_k3<BATCH, R, MODEL, MP, ANISO, 0>(A);
+    return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, 0>(A);
 }
 
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, int N0, int... NS>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, int N0, int... NS>
 cudaError_t dispatch_k3(const K3Args &A)
 {
-    if (A.n_sym == N0) return launch_k3<BATCH, R, MODEL, MP, ANISO, N0>(A);
-    return dispatch_k3<BATCH, R, MODEL, MP, ANISO, NS...>(A);
+    if (A.n_sym == N0) return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, N0>(A);
+    return dispatch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, NS...>(A);
 }
 
 // operations in sign-diagonal cosets: the coset kernels of the compiled
 // (operation count, coset size) pairs; the engine sets L.coset only for those
 // pairs (coset_form_compiled)
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD>
 cudaError_t dispatch_coset(const K3Args &)
 {
     return cudaErrorInvalidValue;
 }
 
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, int N0, int CS0, int... NC>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, int N0, int CS0, int... NC>
 cudaError_t dispatch_coset(const K3Args &A)
 {
-    if (A.n_sym == N0 && A.coset == CS0) return launch_k3<BATCH, R, MODEL, MP, ANISO, N0, CS0>(A);
-    return dispatch_coset<BATCH, R, MODEL, MP, ANISO, NC...>(A);
+    if (A.n_sym == N0 && A.coset == CS0) return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, N0, CS0>(A);
+    return dispatch_coset<BATCH, R, MODEL, MP, ANISO, GRAD, NC...>(A);
 }
 
 // (operation count, coset size) pairs with compiled coset kernels.  HC: both
@@ -98,5 +106,7 @@ cudaError_t launch_k3_f32_hc_mp(const K3Args &A, bool aniso);
 cudaError_t launch_k3_f32_other(const K3Args &A, int model, bool aniso);
 cudaError_t launch_k3_f64(const K3Args &A, int model, bool mp, bool aniso);
 cudaError_t launch_k3b_f32(const K3Args &A, int model, bool aniso);
+cudaError_t launch_k3f_hc(const K3Args &A, bool aniso);
+cudaError_t launch_k3f_other(const K3Args &A, int model, bool aniso);
 
 }  // namespace dsf

@@ -283,7 +283,10 @@ struct PhaseOps<double> {
 // build up.
 constexpr int kAnchorF32 = 4;
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS>
+// GRAD = false: structure factors only (the reference's calculateStructureFactors, which runs its engine with
+// every derivative switched off, HansenCoppensStructureFactorCalculator.cpp:305-326): the derivative sums are
+// never stored, so the compiler drops the whole adjoint
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS, bool GRAD = true>
 __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBuffers &C, const SfLaunch &L,
                                              const SignTable &G, const int tile_rel, const int chunk)
 {
@@ -300,6 +303,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     constexpr bool DIAG = CS > 0 && MODEL == MODEL_HC;
     constexpr bool ADIAG = CS > 0 && ANISO;
     static_assert(CS == 0 || (NSC > 0 && NSC <= 8 && NSC % CS == 0), "coset form: compiled count <= 8");
+    static_assert(GRAD || !MP, "the multipole adjoint needs the derivative pass");
     using R2 = typename Vec2<R>::T;
     constexpr bool F32 = sizeof(R) == 4;
     constexpr int NT = n_channels<R, MP>();
@@ -341,10 +345,11 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     int *sTypes = reinterpret_cast<int *>(sCmp + NT * kTileAtoms);     // [nT]
 
     for (int i = tid; i < nT; i += blockDim.x) sTypes[i] = S.tile_types[tile * kMaxTileTypes + i];
-    for (int q = 0; q < NT; q++) {
-        sTot[q * kTileAtoms + tid] = R(0);
-        sCmp[q * kTileAtoms + tid] = R(0);
-    }
+    if constexpr (GRAD)
+        for (int q = 0; q < NT; q++) {
+            sTot[q * kTileAtoms + tid] = R(0);
+            sCmp[q * kTileAtoms + tid] = R(0);
+        }
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
@@ -888,7 +893,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             }
         }
         // fold the partial sums into the Kahan totals (each thread its own column)
-        if ((k + 1) % fold == 0 || h0 + ht >= h_end) {
+        if (GRAD && ((k + 1) % fold == 0 || h0 + ht >= h_end)) {
 #pragma unroll
             for (int q = 0; q < NT; q++) {
                 R sum = sTot[q * kTileAtoms + tid], comp = sCmp[q * kTileAtoms + tid];
@@ -914,7 +919,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
         }
         __syncthreads();
     }
-    if (active) {
+    if (GRAD && active) {
         double *G = C.g_acc + (size_t)a * kNch;
         auto total = [&](int q) {
             return (double)sTot[q * kTileAtoms + tid] - (double)sCmp[q * kTileAtoms + tid];
@@ -936,22 +941,22 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 }
 
 // one structure: block (tile, reflection chunk)
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true>
 __global__ void __launch_bounds__(kTileAtoms)
 sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 {
-    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(S, C, L, G, blockIdx.x, blockIdx.y);
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD>(S, C, L, G, blockIdx.x, blockIdx.y);
 }
 
 // the same with at least four blocks per SM: the tabulated model with up to
 // four compiled operations (HBM streaming: occupancy over registers).  The
 // other kernels keep the compiler's own register choice, which an explicit
 // minimum of one block would change.
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true>
 __global__ void __launch_bounds__(kTileAtoms, 4)
 sf_grad_kernel3_occ4(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 {
-    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(S, C, L, G, blockIdx.x, blockIdx.y);
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD>(S, C, L, G, blockIdx.x, blockIdx.y);
 }
 
 // many structures of one kernel shape (and one sign table) in one launch: the

@@ -155,6 +155,9 @@ def test_sign_coset_forms_match_oracle(engine, sg, rep, prec):
         check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
         for k in ("d_pval", "d_plm", "d_kappa", "d_kappa_p"):
             assert rel_norm(r[k], o[k]) < TOL[prec][1], (k, rel_norm(r[k], o[k]))
+        # structure factors only (no derivative flags: the FP32 kernels without the adjoint)
+        r = calc.calculate(st.dtdf, precision=prec, derivatives=())
+        assert rel_f(r["f"], o["f"]) < TOL[prec][0]
         calc.close()
 
 
@@ -375,4 +378,25 @@ def test_empty_reflection_set(engine):
     assert rel_f(again["f"], full["f"]) < 1e-13
     assert rel_norm(again["d_xyz"], full["d_xyz"]) < 1e-13
     other.close()
+    calc.close()
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_structure_factors_only_iam_and_tabulated(engine, prec):
+    # calculateStructureFactors of the generic engine: F without derivatives equals the F of the full call
+    st, d = load_fixture("iam_it92")
+    calc = api.IamCalculator(engine, st, iam_dict(d))
+    r = calc.calculate(st.dtdf, precision=prec, derivatives=())
+    assert rel_f(r["f"], d["ref_f"]) < TOL[prec][0]
+    calc.close()
+    st, d = load_fixture("table_p21c")
+    lut = {tuple(k): v for k, v in zip(d["table_keys"], d["table_values"])}
+    rot, _ = api.all_ops_mod_centering(st.sg)
+    t = np.zeros((st.n_hkl, len(rot), st.n_atoms), dtype=complex)
+    for i, h in enumerate(st.hkl):
+        for s_, r_ in enumerate(rot):
+            t[i, s_] = lut[tuple(int(v) for v in h @ r_)]
+    calc = api.TabulatedCalculator(engine, st, t)
+    r = calc.calculate(st.dtdf, precision=prec, derivatives=())
+    assert rel_f(r["f"], d["ref_f"]) < TOL[prec][0]
     calc.close()
