@@ -76,7 +76,7 @@ enum dsf_adp_convention { DSF_ADP_U_CIF = 0, DSF_ADP_U_CART = 1, DSF_ADP_U_STAR 
 /* derivative selection (DerivativesSelector, include/discamb/Scattering/SF_CalcDataTypes.h:22-27,
  * plus the multipole-model parameters the reference does not differentiate).  0: structure factors only
  * (calculateStructureFactors, HansenCoppensStructureFactorCalculator.cpp:305-326): the FP32 single-structure
- * kernels then run without the adjoint; dtdf is not read by the kernels but must point to n_hkl values */
+ * kernels then run without the adjoint; dtdf must still point to n_hkl values (any, e.g. 1) */
 enum dsf_derivative_flags {
     DSF_D_XYZ = 1, DSF_D_ADP = 2, DSF_D_OCC = 4,
     DSF_D_MULTIPOLE = 8   /* P_val, P_lm, kappa, kappa' per atom */
