@@ -229,7 +229,9 @@ int sfo_form_factors(const sfo_problem *p, const double h[3], double *ff)
     double *gl = (double *)calloc((size_t)nT * 5, sizeof(double));
     double *dgl = (double *)calloc((size_t)nT * 5, sizeof(double));
     if (!type_wfn || !fcore || !fval || !dfval || !gl || !dgl) return 1;
-    for (int a = 0; a < nA; a++) type_wfn[p->atom_type[a]] = p->atom_wfn[a];
+    for (int a = 0; a < nA; a++) /* HC types only: the other models carry no per-type wavefunctions */
+        if (p->model == SFO_MODEL_HC && p->atom_type[a] >= 0 && p->atom_type[a] < p->n_types)
+            type_wfn[p->atom_type[a]] = p->atom_wfn[a];
     const double hl = sqrt(h[0] * h[0] + h[1] * h[1] + h[2] * h[2]);
     radial_terms(p, type_wfn, hl, fcore, fval, dfval, gl, dgl);
     for (int a = 0; a < nA; a++) {
@@ -274,7 +276,9 @@ int sfo_compute(const sfo_problem *p, sfo_result *r, int n_threads)
     /* type -> wfn (HC): the wfn of any atom using the type */
     int *type_wfn = (int *)malloc(sizeof(int) * (p->n_types > 0 ? p->n_types : 1));
     for (int t = 0; t < p->n_types; t++) type_wfn[t] = 0;
-    for (int a = 0; a < nA; a++) type_wfn[p->atom_type[a]] = p->atom_wfn[a];
+    for (int a = 0; a < nA; a++) /* HC types only: the other models carry no per-type wavefunctions */
+        if (p->model == SFO_MODEL_HC && p->atom_type[a] >= 0 && p->atom_type[a] < p->n_types)
+            type_wfn[p->atom_type[a]] = p->atom_wfn[a];
 
 #pragma omp parallel num_threads(n_threads)
     {
@@ -609,7 +613,9 @@ int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sf
     /* per atom: crystal-frame P_lm and rotation blocks */
     int *type_wfn = (int *)malloc(sizeof(int) * nT);
     for (int t = 0; t < nT; t++) type_wfn[t] = 0;
-    for (int a = 0; a < nA; a++) type_wfn[p->atom_type[a]] = p->atom_wfn[a];
+    for (int a = 0; a < nA; a++) /* HC types only: the other models carry no per-type wavefunctions */
+        if (p->model == SFO_MODEL_HC && p->atom_type[a] >= 0 && p->atom_type[a] < p->n_types)
+            type_wfn[p->atom_type[a]] = p->atom_wfn[a];
     double *pg = (double *)calloc((size_t)nA * 25, sizeof(double));
     double *Dm = (double *)calloc((size_t)nA * 165, sizeof(double));
     int *lmu = (int *)malloc(sizeof(int) * nA), *lmp = (int *)malloc(sizeof(int) * nA);

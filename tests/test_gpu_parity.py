@@ -400,3 +400,26 @@ def test_structure_factors_only_iam_and_tabulated(engine, prec):
     r = calc.calculate(st.dtdf, precision=prec, derivatives=())
     assert rel_f(r["f"], d["ref_f"]) < TOL[prec][0]
     calc.close()
+
+
+@pytest.mark.parametrize("sg", ["P1", "P-1", "P21", "P21/c", "P212121", "C2/c", "P41", "P43212", "Pbca"])
+def test_tabulated_operation_counts_match_oracle(engine, sg):
+    # every kernel shape of the tabulated model: runtime count (1 operation, form factors staged in shared memory),
+    # compiled 2 / 4 / 8 (form factors in registers), sign-diagonal cosets and not; with and without derivatives
+    for aniso in (False, True):
+        st = W.small_case(sg, n_atoms=9, stol_max=0.5, seed=71, aniso=aniso)
+        rot, _ = api.all_ops_mod_centering(st.sg)
+        rng = np.random.default_rng(72)
+        t = (rng.normal(2, 1, (st.n_hkl, len(rot), st.n_atoms))
+             + 1j * rng.normal(0, 0.3, (st.n_hkl, len(rot), st.n_atoms))).astype(np.complex64)
+        # the oracle sums over every operation (centering included): each takes the form factors of the
+        # operation modulo centering with the same rotation
+        same = [next(k for k, r_ in enumerate(rot) if np.array_equal(r_, r8)) for r8 in st.sg.rot]
+        o = O.compute(st, model="table", table=t[:, same, :].astype(np.complex128))
+        calc = api.TabulatedCalculator(engine, st, table=t, fp32_table=True)
+        for prec in (FP64, FP32):
+            r = calc.calculate(st.dtdf, precision=prec)
+            check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
+            r = calc.calculate(st.dtdf, precision=prec, derivatives=())
+            assert rel_f(r["f"], o["f"]) < TOL[prec][0]
+        calc.close()
