@@ -423,3 +423,26 @@ def test_tabulated_operation_counts_match_oracle(engine, sg):
             r = calc.calculate(st.dtdf, precision=prec, derivatives=())
             assert rel_f(r["f"], o["f"]) < TOL[prec][0]
         calc.close()
+
+
+@pytest.mark.parametrize("sg", ["P1", "P-1", "P21", "P21/c", "P212121", "C2/c", "P41", "P43212", "Pbca"])
+def test_iam_operation_counts_match_oracle(engine, sg):
+    # every kernel shape of the IAM model (generic engine, all operations modulo centering), n-Gaussian form
+    # factors per element; with and without derivatives
+    for aniso in (False, True):
+        st = W.small_case(sg, n_atoms=9, stol_max=0.5, seed=73, aniso=aniso)
+        st.atom_type = st.atom_wfn.copy()
+        rng = np.random.default_rng(74)
+        nt = len(st.wfns)
+        iam = dict(ngauss=np.full(nt, 4, dtype=np.int32), a=np.zeros((nt, 5)), b=np.zeros((nt, 5)),
+                   c=rng.uniform(0.0, 0.5, nt))
+        iam["a"][:, :4] = rng.uniform(0.5, 3.0, (nt, 4))
+        iam["b"][:, :4] = rng.uniform(1.0, 40.0, (nt, 4))
+        o = O.compute(st, model="iam", iam=iam)
+        calc = api.IamCalculator(engine, st, iam)
+        for prec in (FP64, FP32):
+            r = calc.calculate(st.dtdf, precision=prec)
+            check(r, o["f"], o["d_xyz"], o["d_adp"], o["d_occ"], prec)
+            r = calc.calculate(st.dtdf, precision=prec, derivatives=())
+            assert rel_f(r["f"], o["f"]) < TOL[prec][0]
+        calc.close()
