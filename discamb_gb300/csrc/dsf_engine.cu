@@ -27,6 +27,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace dsf {
@@ -1141,6 +1142,27 @@ cudaError_t launch_grad_epilogue(int n_atoms, int xyz_conv, const double *Minv, 
 // ==========================================================================
 // C ABI
 // ==========================================================================
+// host-side work of many structures on several threads when the bytes are worth it (batches of large
+// reflection sets: the staging and copy-out memcpys dominate the host time); f(i) must only touch structure i
+template <class F>
+static void host_parallel(int n, size_t bytes, F f)
+{
+    unsigned nt = bytes < (8u << 20) ? 1u : std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    nt = std::min<unsigned>(nt, (unsigned)std::max(1, n));
+    if (nt <= 1) {
+        for (int i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    auto work = [&] {
+        for (int i; (i = next.fetch_add(1)) < n;) f(i);
+    };
+    std::vector<std::thread> th;
+    for (unsigned k = 1; k < nt; k++) th.emplace_back(work);
+    work();
+    for (auto &t : th) t.join();
+}
+
 extern "C" {
 
 int dsf_abi_version(void) { return DSF_ABI_VERSION; }
@@ -2148,20 +2170,21 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
     return DSF_OK;
 }
 
-// host-buffer calls, staged through one pinned buffer per structure:
-// host_stage enqueues the inclusion mask, the optional atom upload and dT/dF
-// on the engine stream; host_readback enqueues F, the derivatives and the
-// error flag back; host_finish (after the stream sync) checks the flag and
-// copies the results out
+// host-buffer calls, staged through one pinned buffer per structure
 struct HostCall {
     dsf_outputs d;      // device output block
     double *po = nullptr;
     int *pk = nullptr;
+    double *raw = nullptr, *pg = nullptr;  // pinned staging of the atoms and of dT/dF
     size_t nf = 0, nout = 0;
 };
 
-static int host_stage(dsf_structure *s, const double *xyz, const double *adp, const double *occ,
-                      const double *dtdf, const int *include, const dsf_outputs *out, HostCall &hc)
+// a host-buffer call in phases: checks and buffers (host_begin), the CPU copies into pinned staging
+// (host_fill: no CUDA calls, thread-safe per structure), the asynchronous uploads and the atom conversion
+// (host_send), then after the kernels the readback (host_readback), the status (host_status) and the
+// copy-out (host_copy_out: no CUDA calls, thread-safe per structure)
+static int host_begin(dsf_structure *s, const double *xyz, const double *occ, const double *dtdf, const int *include,
+                      const dsf_outputs *out, HostCall &hc)
 {
     if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
@@ -2192,17 +2215,52 @@ static int host_stage(dsf_structure *s, const double *xyz, const double *adp, co
         DSF_CUDA(cudaHostAlloc(&s->pinned, stage_bytes, cudaHostAllocDefault));
         s->pinned_bytes = stage_bytes;
     }
-    double *raw = (double *)s->pinned, *pg = raw + 10 * (size_t)n, *po = pg + 2 * (size_t)n_hkl;
+    hc.raw = (double *)s->pinned;
+    hc.pg = hc.raw + 10 * (size_t)n;
+    hc.po = hc.pg + 2 * (size_t)n_hkl;
+    hc.pk = (int *)(hc.po + nout);
+    hc.nf = nf;
+    hc.nout = nout;
+    double *base = s->d_out.as<double>();
+    dsf_outputs &d = hc.d;
+    d.f = base;
+    d.d_xyz = base + nf;
+    d.d_adp = d.d_xyz + 3 * (size_t)n;
+    d.d_occ = d.d_adp + 6 * (size_t)n;
+    d.d_pval = d.d_occ + n;
+    d.d_plm = d.d_pval + n;
+    d.d_kappa = d.d_plm + 25 * (size_t)n;
+    d.d_kappa_prime = d.d_kappa + n;
+    return DSF_OK;
+}
+
+// 0, or 1 with a non-finite coordinate
+static int host_fill(const dsf_structure *s, const double *xyz, const double *adp, const double *occ,
+                     const double *dtdf, const HostCall &hc)
+{
+    const int n = s->n_atoms;
     if (xyz) {
+        double *raw = hc.raw;
         for (int i = 0; i < n; i++) {
             for (int j = 0; j < 3; j++) {
-                if (!std::isfinite(xyz[3 * i + j])) return fail(e, DSF_ERR_ARGUMENT, "non-finite coordinate");
+                if (!std::isfinite(xyz[3 * i + j])) return 1;
                 raw[10 * i + j] = xyz[3 * i + j];
             }
             for (int j = 0; j < 6; j++) raw[10 * i + 3 + j] = (adp && j < s->adpk[i]) ? adp[6 * i + j] : 0.0;
             raw[10 * i + 9] = occ[i];
         }
-        DSF_CUDA(cudaMemcpyAsync(s->d_raw.p, raw, sizeof(double) * 10 * (size_t)n, cudaMemcpyHostToDevice, e->stream));
+    }
+    if (s->n_hkl > 0) std::memcpy(hc.pg, dtdf, sizeof(double) * 2 * (size_t)s->n_hkl);
+    return 0;
+}
+
+static int host_send(dsf_structure *s, bool atoms, const HostCall &hc)
+{
+    dsf_engine *e = s->eng;
+    const int n = s->n_atoms, n_hkl = s->n_hkl;
+    if (atoms) {
+        DSF_CUDA(cudaMemcpyAsync(s->d_raw.p, hc.raw, sizeof(double) * 10 * (size_t)n, cudaMemcpyHostToDevice,
+                                 e->stream));
         AtomParams P;
         P.n_atoms = n;
         P.xyz_conv = s->xyz_conv;
@@ -2215,25 +2273,18 @@ static int host_stage(dsf_structure *s, const double *xyz, const double *adp, co
         DSF_CUDA(cudaGetLastError());
         s->have_atoms = true;
     }
-    if (n_hkl > 0) {
-        std::memcpy(pg, dtdf, sizeof(double) * 2 * (size_t)n_hkl);
-        DSF_CUDA(cudaMemcpyAsync(s->d_dtdf.p, pg, 16 * (size_t)n_hkl, cudaMemcpyHostToDevice, e->stream));
-    }
-    double *base = s->d_out.as<double>();
-    dsf_outputs &d = hc.d;
-    d.f = base;
-    d.d_xyz = base + nf;
-    d.d_adp = d.d_xyz + 3 * (size_t)n;
-    d.d_occ = d.d_adp + 6 * (size_t)n;
-    d.d_pval = d.d_occ + n;
-    d.d_plm = d.d_pval + n;
-    d.d_kappa = d.d_plm + 25 * (size_t)n;
-    d.d_kappa_prime = d.d_kappa + n;
-    hc.po = po;
-    hc.pk = (int *)(po + nout);
-    hc.nf = nf;
-    hc.nout = nout;
+    if (n_hkl > 0)
+        DSF_CUDA(cudaMemcpyAsync(s->d_dtdf.p, hc.pg, 16 * (size_t)n_hkl, cudaMemcpyHostToDevice, e->stream));
     return DSF_OK;
+}
+
+static int host_stage(dsf_structure *s, const double *xyz, const double *adp, const double *occ,
+                      const double *dtdf, const int *include, const dsf_outputs *out, HostCall &hc)
+{
+    int rc = host_begin(s, xyz, occ, dtdf, include, out, hc);
+    if (rc) return rc;
+    if (host_fill(s, xyz, adp, occ, dtdf, hc)) return fail(s->eng, DSF_ERR_ARGUMENT, "non-finite coordinate");
+    return host_send(s, xyz != nullptr, hc);
 }
 
 static int host_readback(dsf_structure *s, int flags, HostCall &hc)
@@ -2246,15 +2297,21 @@ static int host_readback(dsf_structure *s, int flags, HostCall &hc)
     return DSF_OK;
 }
 
-static int host_finish(dsf_structure *s, int flags, const HostCall &hc, const dsf_outputs *out)
+// a timed-out kernel wait of the call (DSF_ERR_TIMEOUT), after the stream synchronisation
+static int host_status(dsf_structure *s, const HostCall &hc)
 {
-    dsf_engine *e = s->eng;
+    if (*hc.pk) {
+        cudaMemsetAsync(s->d_err.p, 0, sizeof(int), s->eng->stream);
+        return fail(s->eng, DSF_ERR_TIMEOUT, "a shared-memory pipeline wait of the kernel ran out");
+    }
+    return DSF_OK;
+}
+
+// copy-out of the pinned results (no CUDA calls, thread-safe per structure)
+static void host_copy_out(const dsf_structure *s, int flags, const HostCall &hc, const dsf_outputs *out)
+{
     const int n = s->n_atoms;
     const bool mp = (flags & DSF_D_MULTIPOLE) != 0;
-    if (*hc.pk) {
-        cudaMemsetAsync(s->d_err.p, 0, sizeof(int), e->stream);
-        return fail(e, DSF_ERR_TIMEOUT, "a shared-memory pipeline wait of the kernel ran out");
-    }
     if (hc.nf) std::memcpy(out->f, hc.po, sizeof(double) * hc.nf);
     const double *q = hc.po + hc.nf;
     struct { double *dst; size_t off, n; } cp[] = {
@@ -2264,7 +2321,6 @@ static int host_finish(dsf_structure *s, int flags, const HostCall &hc, const ds
         {out->d_kappa_prime, 37 * (size_t)n, (size_t)n}};
     for (auto &c : cp)
         if (c.dst && (c.off < 10 * (size_t)n || mp)) std::memcpy(c.dst, q + c.off, sizeof(double) * c.n);
-    return DSF_OK;
 }
 
 static int calculate_host(dsf_structure *s, int precision, int flags, const double *xyz, const double *adp,
@@ -2277,7 +2333,9 @@ static int calculate_host(dsf_structure *s, int precision, int flags, const doub
     if ((rc = dsf_calculate_device(s, precision, flags, s->d_dtdf.as<double>(), &hc.d, e->stream))) return rc;
     if ((rc = host_readback(s, flags, hc))) return rc;
     DSF_CUDA(cudaStreamSynchronize(e->stream));
-    return host_finish(s, flags, hc, out);
+    if ((rc = host_status(s, hc))) return rc;
+    host_copy_out(s, flags, hc, out);
+    return DSF_OK;
 }
 
 int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf_outputs *per_type, void *stream)
@@ -2342,15 +2400,29 @@ int dsf_calculate_batch_atoms(dsf_structure *const *structures, int n, int preci
     std::vector<HostCall> hc(n);
     std::vector<dsf_outputs> d(n);
     std::vector<const double *> g(n);
+    size_t bytes_in = 0, bytes_out = 0;
     for (int i = 0; i < n; i++) {
         if (!structures[i] || structures[i]->eng != e)
             return fail(e, DSF_ERR_ARGUMENT, "batch structures must belong to one engine");
-        int rc = host_stage(structures[i], xyz ? xyz[i] : nullptr, adp ? adp[i] : nullptr,
-                            occupancy ? occupancy[i] : nullptr, dtdf[i], include ? include[i] : nullptr, &out[i],
-                            hc[i]);
+        int rc = host_begin(structures[i], xyz ? xyz[i] : nullptr, occupancy ? occupancy[i] : nullptr, dtdf[i],
+                            include ? include[i] : nullptr, &out[i], hc[i]);
         if (rc) return rc;
+        bytes_in += 16 * (size_t)structures[i]->n_hkl + (xyz ? 80 * (size_t)structures[i]->n_atoms : 0);
+        bytes_out += 8 * hc[i].nout;
         d[i] = hc[i].d;
         g[i] = structures[i]->d_dtdf.as<double>();
+    }
+    // the CPU copies into the structures' pinned staging, in parallel for large batches
+    std::vector<int> bad(n, 0);
+    host_parallel(n, bytes_in, [&](int i) {
+        bad[i] = host_fill(structures[i], xyz ? xyz[i] : nullptr, adp ? adp[i] : nullptr,
+                           occupancy ? occupancy[i] : nullptr, dtdf[i], hc[i]);
+    });
+    for (int i = 0; i < n; i++)
+        if (bad[i]) return fail(e, DSF_ERR_ARGUMENT, "non-finite coordinate");
+    for (int i = 0; i < n; i++) {
+        int rc = host_send(structures[i], xyz != nullptr && xyz[i] != nullptr, hc[i]);
+        if (rc) return rc;
     }
     int rc = dsf_calculate_batch_device(structures, n, precision, flags, g.data(), d.data(), e->stream);
     if (rc) return rc;
@@ -2358,7 +2430,8 @@ int dsf_calculate_batch_atoms(dsf_structure *const *structures, int n, int preci
         if ((rc = host_readback(structures[i], flags, hc[i]))) return rc;
     DSF_CUDA(cudaStreamSynchronize(e->stream));
     for (int i = 0; i < n; i++)
-        if ((rc = host_finish(structures[i], flags, hc[i], &out[i]))) return rc;
+        if ((rc = host_status(structures[i], hc[i]))) return rc;
+    host_parallel(n, bytes_out, [&](int i) { host_copy_out(structures[i], flags, hc[i], &out[i]); });
     return DSF_OK;
 }
 
