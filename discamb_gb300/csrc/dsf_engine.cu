@@ -203,6 +203,7 @@ struct dsf_structure {
     // vector; sym_sign: that map's signs relative to the coset's first operation
     int electron = 0;            // HC: Mott-Bethe electron scattering
     int coset_size = 0;
+    int inv_pairs = 0;  // generic models: operations n/2 .. n-1 are the images of 0 .. n/2-1 under -1 at the origin
     std::vector<int> sym_sign;   // [n_sym][3] Cartesian
     std::vector<int> sym_fsign;  // [n_sym][3] fractional h' components
     // tabulated model: column of sorted atom a = a + (a >= table_split ? table_shift : 0), table_stride
@@ -634,6 +635,15 @@ int sym_from_desc(dsf_engine *e, dsf_structure *s, const dsf_symmetry *sym)
         // one coset when every operation is a sign-diagonal image of the first
         s->coset_size = (s->n_sym >= 2 && fractional_signs(s, s->n_sym)) ? s->n_sym : 0;
         s->sym_sign.assign(3 * (size_t)s->n_sym, 1);
+        // the caller's order as n/2 operations and then their images under an inversion at the origin
+        // (x -> -R x - t), as the standard operation lists of centrosymmetric groups come
+        const int n = s->n_sym, h = n / 2;
+        bool pairs = n >= 2 && n % 2 == 0;
+        for (int k = 0; pairs && k < h; k++) {
+            for (int j = 0; j < 9; j++) pairs = pairs && s->sym_rot[9 * (k + h) + j] == -s->sym_rot[9 * k + j];
+            for (int j = 0; j < 3; j++) pairs = pairs && (s->sym_t24[3 * (k + h) + j] + s->sym_t24[3 * k + j]) % 24 == 0;
+        }
+        s->inv_pairs = pairs ? 1 : 0;
     }
     s->centro_mode = 0;
     if (sym->centrosymmetric) {
@@ -1893,6 +1903,12 @@ static int call_post(dsf_structure *s, int flags, const dsf_outputs *out, cudaSt
     return DSF_OK;
 }
 
+// the inversion-pair kernels: FP32 tabulated model with a compiled operation count
+static bool inv_kernel(const dsf_structure *s, bool fp64)
+{
+    return s->inv_pairs && !fp64 && s->model == MODEL_TABLE && table_count_compiled(s->n_sym);
+}
+
 // a call on an empty reflection set: no F, the requested derivatives zero (the reference's engines sum over no
 // reflections); no kernels
 static int empty_call(dsf_structure *s, int flags, const dsf_outputs *out, cudaStream_t st)
@@ -1956,6 +1972,7 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         A.smem = smem;
         A.st = st;
         A.grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
+        A.inv = inv_kernel(s, fp64);
         DSF_CUDA(launch_sf3(A, s->model, fp64, mp, kind == 1));
         launches++;
     }
@@ -2065,6 +2082,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
     // about eight times
     struct Group {
         int model, aniso, n_sym, coset;
+        bool inv;
         SignTable G;
         size_t smem = 0;
         std::vector<SfBatchItem> items;
@@ -2105,7 +2123,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
             Group *g = nullptr;
             for (auto &x : groups)
                 if (x.model == s->model && x.aniso == kind && x.n_sym == s->n_sym && x.coset == L.coset &&
-                    (L.coset == 0 || std::memcmp(&x.G, &G, sizeof(G)) == 0)) {
+                    x.inv == inv_kernel(s, fp64) && (L.coset == 0 || std::memcmp(&x.G, &G, sizeof(G)) == 0)) {
                     g = &x;
                     break;
                 }
@@ -2116,6 +2134,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
                 g->aniso = kind;
                 g->n_sym = s->n_sym;
                 g->coset = L.coset;
+                g->inv = inv_kernel(s, fp64);
                 g->G = G;
             }
             SfBatchItem it;
@@ -2159,6 +2178,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
             A.G = &g.G;
             A.n_sym = g.n_sym;
             A.coset = g.coset;
+            A.inv = g.inv;
             A.blocks = blocks;
             A.smem = g.smem;
             A.st = st;

@@ -8,10 +8,10 @@ cudaError_t launch_k3_f32_hc(const K3Args &A, bool mp, bool aniso)
 {
     if (mp) return launch_k3_f32_hc_mp(A, aniso);
     if (A.coset)
-        return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
-                     : dispatch_coset<false, float, MODEL_HC, false, false, true, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);
-    return aniso ? dispatch_k3<false, float, MODEL_HC, false, true, true, 2, 4, 8>(A)
-                 : dispatch_k3<false, float, MODEL_HC, false, false, true, 2, 4, 8>(A);
+        return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, true, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
+                     : dispatch_coset<false, float, MODEL_HC, false, false, true, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);
+    return aniso ? dispatch_k3<false, float, MODEL_HC, false, true, true, false, 2, 4, 8>(A)
+                 : dispatch_k3<false, float, MODEL_HC, false, false, true, false, 2, 4, 8>(A);
 }
 
 size_t sf3_smem_bytes(bool fp64, bool mp, int ht, int n_sym, int max_types, bool table)

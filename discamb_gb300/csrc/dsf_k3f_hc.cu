@@ -10,10 +10,10 @@ namespace dsf {
 cudaError_t launch_k3f_hc(const K3Args &A, bool aniso)
 {
     if (A.coset)
-        return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
-                     : dispatch_coset<false, float, MODEL_HC, false, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);
-    return aniso ? dispatch_k3<false, float, MODEL_HC, false, true, false, 2, 4, 8>(A)
-                 : dispatch_k3<false, float, MODEL_HC, false, false, false, 2, 4, 8>(A);
+        return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
+                     : dispatch_coset<false, float, MODEL_HC, false, false, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);
+    return aniso ? dispatch_k3<false, float, MODEL_HC, false, true, false, false, 2, 4, 8>(A)
+                 : dispatch_k3<false, float, MODEL_HC, false, false, false, false, 2, 4, 8>(A);
 }
 
 }  // namespace dsf

@@ -19,6 +19,7 @@ struct K3Args {
     const SfBatch *B = nullptr;
     int n_sym = 0, coset = 0;
     bool grad = true;  // false: structure factors only (single-structure FP32 kernels without the adjoint)
+    bool inv = false;  // operations as n/2 plus their images under an inversion at the origin (generic models)
     int n_tiles = 0, n_chunks = 0, blocks = 0;
     size_t smem = 0;
     cudaStream_t st = nullptr;
@@ -33,56 +34,60 @@ cudaError_t launch_with(K k, dim3 grid, size_t smem, cudaStream_t st, const Args
     return cudaGetLastError();
 }
 
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, int NSC, int CS = 0>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV, int NSC, int CS = 0>
 cudaError_t launch_k3(const K3Args &A)
 {
     constexpr bool OCC4 = occ4_kernel<R, MODEL, NSC>();
     const dim3 grid = BATCH ? dim3(A.blocks) : dim3(A.n_tiles, A.n_chunks);
     static_assert(GRAD || !BATCH, "structure-factor-only kernels: single structures");
     if constexpr (!GRAD && OCC4)
-        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS, false>, grid, A.smem, A.st, *A.S, *A.C,
-                           *A.L, *A.G);
+        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS, false, INV>, grid, A.smem, A.st, *A.S,
+                           *A.C, *A.L, *A.G);
     else if constexpr (!GRAD)
-        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS, false>, grid, A.smem, A.st, *A.S, *A.C, *A.L,
-                           *A.G);
+        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS, false, INV>, grid, A.smem, A.st, *A.S, *A.C,
+                           *A.L, *A.G);
     else if constexpr (BATCH && OCC4)
-        return launch_with(sf_grad_batch3_occ4<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.B, *A.G);
+        return launch_with(sf_grad_batch3_occ4<R, MODEL, MP, ANISO, NSC, CS, INV>, grid, A.smem, A.st, *A.B, *A.G);
     else if constexpr (BATCH)
-        return launch_with(sf_grad_batch3<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.B, *A.G);
+        return launch_with(sf_grad_batch3<R, MODEL, MP, ANISO, NSC, CS, INV>, grid, A.smem, A.st, *A.B, *A.G);
     else if constexpr (OCC4)
-        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.S, *A.C, *A.L, *A.G);
+        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS, true, INV>, grid, A.smem, A.st, *A.S,
+                           *A.C, *A.L, *A.G);
     else
-        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS>, grid, A.smem, A.st, *A.S, *A.C, *A.L, *A.G);
+        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS, true, INV>, grid, A.smem, A.st, *A.S, *A.C,
+                           *A.L, *A.G);
 }
 
-// compiled operation counts first, runtime count last
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD>
+// compiled operation counts first, runtime count last (INV kernels exist only for compiled counts: the
+// runtime one is never reached with A.inv set, the engine sets it only for those counts)
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV>
 cudaError_t dispatch_k3(const K3Args &A)
 {
-    return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, 0>(A);
+    if constexpr (INV) return cudaErrorInvalidValue;
+    else return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, false, 0>(A);
 }
 
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, int N0, int... NS>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV, int N0, int... NS>
 cudaError_t dispatch_k3(const K3Args &A)
 {
-    if (A.n_sym == N0) return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, N0>(A);
-    return dispatch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, NS...>(A);
+    if (A.n_sym == N0) return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, INV, N0>(A);
+    return dispatch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, INV, NS...>(A);
 }
 
 // operations in sign-diagonal cosets: the coset kernels of the compiled
 // (operation count, coset size) pairs; the engine sets L.coset only for those
 // pairs (coset_form_compiled)
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV>
 cudaError_t dispatch_coset(const K3Args &)
 {
     return cudaErrorInvalidValue;
 }
 
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, int N0, int CS0, int... NC>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV, int N0, int CS0, int... NC>
 cudaError_t dispatch_coset(const K3Args &A)
 {
-    if (A.n_sym == N0 && A.coset == CS0) return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, N0, CS0>(A);
-    return dispatch_coset<BATCH, R, MODEL, MP, ANISO, GRAD, NC...>(A);
+    if (A.n_sym == N0 && A.coset == CS0) return launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, INV, N0, CS0>(A);
+    return dispatch_coset<BATCH, R, MODEL, MP, ANISO, GRAD, INV, NC...>(A);
 }
 
 // (operation count, coset size) pairs with compiled coset kernels.  HC: both

@@ -286,7 +286,10 @@ constexpr int kAnchorF32 = 4;
 // GRAD = false: structure factors only (the reference's calculateStructureFactors, which runs its engine with
 // every derivative switched off, HansenCoppensStructureFactorCalculator.cpp:305-326): the derivative sums are
 // never stored, so the compiler drops the whole adjoint
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS, bool GRAD = true>
+// INV = true (FP32 tabulated and IAM models, the caller's operations as n/2 operations followed by their
+// images under an inversion at the origin, x -> -R x - t): the images' phase factors are the conjugates of their
+// partners' and their temperature factors equal, so only half the operations run the phase and exp work
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS, bool GRAD = true, bool INV = false>
 __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBuffers &C, const SfLaunch &L,
                                              const SignTable &G, const int tile_rel, const int chunk)
 {
@@ -304,6 +307,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     constexpr bool ADIAG = CS > 0 && ANISO;
     static_assert(CS == 0 || (NSC > 0 && NSC <= 8 && NSC % CS == 0), "coset form: compiled count <= 8");
     static_assert(GRAD || !MP, "the multipole adjoint needs the derivative pass");
+    static_assert(!INV || (MODEL != MODEL_HC && NSC > 0 && NSC % 2 == 0), "inversion pairs: generic models, even count");
     using R2 = typename Vec2<R>::T;
     constexpr bool F32 = sizeof(R) == 4;
     constexpr int NT = n_channels<R, MP>();
@@ -450,7 +454,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             // line steps in FP64, rounded once
             const double xa = S.atom_xd[3 * a], xb = S.atom_xd[3 * a + 1], xc = S.atom_xd[3 * a + 2];
 #pragma unroll
-            for (int s = 0; s < NR; s++) {
+            for (int s = 0; s < (INV ? NR / 2 : NR); s++) {  // INV: the images need no line steps
                 const int *Rm = S.sym_rot + 9 * s;
                 double ph = Rm[6] * xa + Rm[7] * xb + Rm[8] * xc + S.sym_t24[3 * s + 2] / 24.0;
                 ph -= rint(ph);
@@ -664,38 +668,54 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         }
                         }
                     };
+                    // INV: e^{i theta} T of the first half of the operations, for their inversion images
+                    R zT_re[INV ? NR / 2 : 1], zT_im[INV ? NR / 2 : 1];
                     auto term = [&](int s) {
                         const RsRec<R> &rec = recs[s];
                         const R h0f = rec.hf[0], h1f = rec.hf[1], h2f = rec.hf[2];
-                        R cs, sn;
-                        if constexpr (REC) {
-                            if (anchor) {
-                                PhaseOps<R>::exact(rec, xq0, xq1, xq2, x0, x1, x2, &sn, &cs);
-                            } else {
-                                cs = e_re[s] * step_re[s] - e_im[s] * step_im[s];
-                                sn = e_re[s] * step_im[s] + e_im[s] * step_re[s];
-                            }
-                            e_re[s] = cs;
-                            e_im[s] = sn;
-                        } else {
-                            PhaseOps<R>::exact(rec, xq0, xq1, xq2, x0, x1, x2, &sn, &cs);
-                        }
-                        R zre = cs, zim = sn;  // e^{i theta} T_s
+                        R zre, zim;  // e^{i theta} T_s
                         R m6[ANISO ? 6 : 1];
+                        if constexpr (ANISO && !ADIAG) {
+                            m6[0] = h0f * h0f; m6[1] = h1f * h1f; m6[2] = h2f * h2f;
+                            m6[3] = R(2) * h0f * h1f; m6[4] = R(2) * h0f * h2f; m6[5] = R(2) * h1f * h2f;
+                        }
                         const auto xs = [&](int c) -> R {
                             if constexpr (F32) return G.xf[s][c]; else return G.xd[s][c];
                         };
-                        if constexpr (ADIAG) {
-                            const R q = qd + xs(3) * qc[0] + xs(5) * qc[1] + xs(6) * qc[2];
-                            const R T = texp<R>(-q);
-                            zre *= T; zim *= T;
-                        } else if constexpr (ANISO) {
-                            m6[0] = h0f * h0f; m6[1] = h1f * h1f; m6[2] = h2f * h2f;
-                            m6[3] = R(2) * h0f * h1f; m6[4] = R(2) * h0f * h2f; m6[5] = R(2) * h1f * h2f;
-                            const R q = adp[0] * m6[0] + adp[1] * m6[1] + adp[2] * m6[2] + adp[3] * m6[3] +
-                                        adp[4] * m6[4] + adp[5] * m6[5];
-                            const R T = texp<R>(-q);
-                            zre *= T; zim *= T;
+                        if (INV && s >= NR / 2) {
+                            // the inversion image of operation s - n/2 (inversion at the origin): h' -> -h',
+                            // the same translation sign-reversed, so the conjugate phase and the same T
+                            zre = zT_re[INV ? s - NR / 2 : 0];
+                            zim = -zT_im[INV ? s - NR / 2 : 0];
+                        } else {
+                            R cs, sn;
+                            if constexpr (REC) {
+                                if (anchor) {
+                                    PhaseOps<R>::exact(rec, xq0, xq1, xq2, x0, x1, x2, &sn, &cs);
+                                } else {
+                                    cs = e_re[s] * step_re[s] - e_im[s] * step_im[s];
+                                    sn = e_re[s] * step_im[s] + e_im[s] * step_re[s];
+                                }
+                                e_re[s] = cs;
+                                e_im[s] = sn;
+                            } else {
+                                PhaseOps<R>::exact(rec, xq0, xq1, xq2, x0, x1, x2, &sn, &cs);
+                            }
+                            zre = cs; zim = sn;
+                            if constexpr (ADIAG) {
+                                const R q = qd + xs(3) * qc[0] + xs(5) * qc[1] + xs(6) * qc[2];
+                                const R T = texp<R>(-q);
+                                zre *= T; zim *= T;
+                            } else if constexpr (ANISO) {
+                                const R q = adp[0] * m6[0] + adp[1] * m6[1] + adp[2] * m6[2] + adp[3] * m6[3] +
+                                            adp[4] * m6[4] + adp[5] * m6[5];
+                                const R T = texp<R>(-q);
+                                zre *= T; zim *= T;
+                            }
+                            if constexpr (INV) {
+                                zT_re[s < NR / 2 ? s : 0] = zre;
+                                zT_im[s < NR / 2 ? s : 0] = zim;
+                            }
                         }
                         R fre, fim;
                         R A0 = 0, A1 = 0, A2 = 0, A3 = 0, A4 = 0;
@@ -941,27 +961,27 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 }
 
 // one structure: block (tile, reflection chunk)
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true, bool INV = false>
 __global__ void __launch_bounds__(kTileAtoms)
 sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 {
-    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD>(S, C, L, G, blockIdx.x, blockIdx.y);
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD, INV>(S, C, L, G, blockIdx.x, blockIdx.y);
 }
 
 // the same with at least four blocks per SM: the tabulated model with up to
 // four compiled operations (HBM streaming: occupancy over registers).  The
 // other kernels keep the compiler's own register choice, which an explicit
 // minimum of one block would change.
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true, bool INV = false>
 __global__ void __launch_bounds__(kTileAtoms, 4)
 sf_grad_kernel3_occ4(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 {
-    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD>(S, C, L, G, blockIdx.x, blockIdx.y);
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD, INV>(S, C, L, G, blockIdx.x, blockIdx.y);
 }
 
 // many structures of one kernel shape (and one sign table) in one launch: the
 // block's item is the last with block_begin <= blockIdx.x
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS, bool INV>
 __device__ __forceinline__ void sf_grad_batch_body(const SfBatch &B, const SignTable &G)
 {
     const int b = blockIdx.x;
@@ -973,21 +993,21 @@ __device__ __forceinline__ void sf_grad_batch_body(const SfBatch &B, const SignT
     }
     const SfBatchItem &it = B.item[lo];
     const int lb = b - B.block_begin[lo];
-    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS>(it.S, it.C, it.L, G, lb % it.n_tiles, lb / it.n_tiles);
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, true, INV>(it.S, it.C, it.L, G, lb % it.n_tiles, lb / it.n_tiles);
 }
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool INV = false>
 __global__ void __launch_bounds__(kTileAtoms)
 sf_grad_batch3(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
 {
-    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS>(B, G);
+    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS, INV>(B, G);
 }
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool INV = false>
 __global__ void __launch_bounds__(kTileAtoms, 4)
 sf_grad_batch3_occ4(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
 {
-    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS>(B, G);
+    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS, INV>(B, G);
 }
 
 // kernels that take the four-block minimum: FP32 tabulated, form factors in registers
