@@ -1903,10 +1903,10 @@ static int call_post(dsf_structure *s, int flags, const dsf_outputs *out, cudaSt
     return DSF_OK;
 }
 
-// the inversion-pair kernels: FP32 tabulated model with a compiled operation count
+// the inversion-pair kernels: FP32 generic models (tabulated, IAM) with a compiled operation count
 static bool inv_kernel(const dsf_structure *s, bool fp64)
 {
-    return s->inv_pairs && !fp64 && s->model == MODEL_TABLE && table_count_compiled(s->n_sym);
+    return s->inv_pairs && !fp64 && s->model != MODEL_HC && table_count_compiled(s->n_sym);
 }
 
 // a call on an empty reflection set: no F, the requested derivatives zero (the reference's engines sum over no

@@ -14,6 +14,12 @@ cudaError_t launch_k3b_f32(const K3Args &A, int model, bool aniso)
                      : dispatch_k3<true, float, MODEL_HC, false, false, true, false, 1, 2, 4, 8>(A);
     }
     if (model == MODEL_IAM) {
+        if (A.inv) {  // operations as n/2 plus their inversion images
+            if (aniso && A.coset)
+                return dispatch_coset<true, float, MODEL_IAM, false, true, true, true, 2, 2, 4, 4, 8, 8>(A);
+            return aniso ? dispatch_k3<true, float, MODEL_IAM, false, true, true, true, 2, 4, 8>(A)
+                         : dispatch_k3<true, float, MODEL_IAM, false, false, true, true, 2, 4, 8>(A);
+        }
         if (aniso && A.coset) return dispatch_coset<true, float, MODEL_IAM, false, true, true, false, 2, 2, 4, 4, 8, 8>(A);
         return aniso ? dispatch_k3<true, float, MODEL_IAM, false, true, true, false, 2, 4, 8>(A)
                      : dispatch_k3<true, float, MODEL_IAM, false, false, true, false, 2, 4, 8>(A);

@@ -10,6 +10,12 @@ namespace dsf {
 cudaError_t launch_k3f_other(const K3Args &A, int model, bool aniso)
 {
     if (model == MODEL_IAM) {
+        if (A.inv) {  // operations as n/2 plus their inversion images
+            if (aniso && A.coset)
+                return dispatch_coset<false, float, MODEL_IAM, false, true, false, true, 2, 2, 4, 4, 8, 8>(A);
+            return aniso ? dispatch_k3<false, float, MODEL_IAM, false, true, false, true, 2, 4, 8>(A)
+                         : dispatch_k3<false, float, MODEL_IAM, false, false, false, true, 2, 4, 8>(A);
+        }
         if (aniso && A.coset) return dispatch_coset<false, float, MODEL_IAM, false, true, false, false, 2, 2, 4, 4, 8, 8>(A);
         return aniso ? dispatch_k3<false, float, MODEL_IAM, false, true, false, false, 2, 4, 8>(A)
                      : dispatch_k3<false, float, MODEL_IAM, false, false, false, false, 2, 4, 8>(A);

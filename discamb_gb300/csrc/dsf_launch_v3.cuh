@@ -100,9 +100,11 @@ __host__ inline bool coset_form_compiled(bool fp64, int model, int n_sym, int cs
     return (n_sym == 2 && cs == 2) || (n_sym == 4 && (cs == 4 || cs == 2)) || (n_sym == 8 && (cs == 8 || cs == 4));
 }
 
-// operation counts with compiled FP32 tabulated kernels: those read the form
-// factors straight into registers; the runtime-count kernel stages them in
-// shared memory (the dispatch lists of dsf_k3_f32_other.cu and dsf_k3b_f32.cu)
+// operation counts with compiled FP32 kernels of the generic models (tabulated,
+// IAM; the dispatch lists of dsf_k3_f32_other.cu and dsf_k3b_f32.cu): the
+// tabulated ones read the form factors straight into registers (the
+// runtime-count kernel stages them in shared memory), and both have the
+// inversion-pair form
 __host__ inline bool table_count_compiled(int n_sym) { return n_sym == 2 || n_sym == 4 || n_sym == 8; }
 
 // per-translation-unit entries (model, multipole adjoint and ADP kind resolved at run time)
