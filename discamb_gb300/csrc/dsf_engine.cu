@@ -78,6 +78,9 @@ struct dsf_engine {
     int n_sm = 0;
     size_t max_smem = 0;
     double *d_rotfit = nullptr;  // rotation-block fit (pinv blocks + sample directions) on this device
+    // batched launches alternate between the call's stream and this one (under the batch launch lock)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -1205,6 +1208,9 @@ int dsf_engine_destroy(dsf_engine *e)
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamDestroy(e->stream);
     if (e->setup) cudaStreamDestroy(e->setup);
+    if (e->side) cudaStreamDestroy(e->side);
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
     if (e->d_rotfit) cudaFree(e->d_rotfit);
     delete e;
     return DSF_OK;
@@ -2149,6 +2155,16 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
     static SfBatch B;  // host staging of the launch parameters (copied at launch)
     static std::mutex mtx;
     std::lock_guard<std::mutex> lock(mtx);
+    // consecutive batched launches alternate between the call's stream and the engine's side stream, so the
+    // last wave of one launch overlaps the start of the next; the side stream forks from and joins the call's
+    if (!e->side) {
+        DSF_CUDA(cudaStreamCreateWithFlags(&e->side, cudaStreamNonBlocking));
+        DSF_CUDA(cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming));
+        DSF_CUDA(cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming));
+    }
+    DSF_CUDA(cudaEventRecord(e->ev_fork, st));
+    DSF_CUDA(cudaStreamWaitEvent(e->side, e->ev_fork, 0));
+    int lane = 0;
     for (auto &g : groups)
         for (size_t b0 = 0; b0 < g.items.size(); b0 += kBatchItems) {
             const int m = (int)std::min<size_t>(kBatchItems, g.items.size() - b0);
@@ -2181,10 +2197,12 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
             A.inv = g.inv;
             A.blocks = blocks;
             A.smem = g.smem;
-            A.st = st;
+            A.st = (lane++ & 1) ? e->side : st;
             DSF_CUDA(launch_k3b_f32(A, g.model, g.aniso == 1));
             launches++;
         }
+    DSF_CUDA(cudaEventRecord(e->ev_join, e->side));
+    DSF_CUDA(cudaStreamWaitEvent(st, e->ev_join, 0));
     if ((rc = launch_prepost(true))) return rc;
     for (int i = 0; i < n; i++) structures[i]->last_launches = launches;
     return DSF_OK;
