@@ -1156,11 +1156,13 @@ cudaError_t launch_grad_epilogue(int n_atoms, int xyz_conv, const double *Minv, 
 // C ABI
 // ==========================================================================
 // host-side work of many structures on several threads when the bytes are worth it (batches of large
-// reflection sets: the staging and copy-out memcpys dominate the host time); f(i) must only touch structure i
+// reflection sets: the staging and copy-out memcpys dominate the host time); f(i) must only touch structure i.
+// At most half the host's cores, and only above 32 MB, so a serving loop's other threads (structure set-up)
+// keep theirs.
 template <class F>
 static void host_parallel(int n, size_t bytes, F f)
 {
-    unsigned nt = bytes < (8u << 20) ? 1u : std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    unsigned nt = bytes < (32u << 20) ? 1u : std::min(8u, std::max(1u, std::thread::hardware_concurrency() / 2));
     nt = std::min<unsigned>(nt, (unsigned)std::max(1, n));
     if (nt <= 1) {
         for (int i = 0; i < n; i++) f(i);
