@@ -167,18 +167,25 @@ def fp32_peak_tflops(device):
     return out.value
 
 
-def cpu_baseline(st, sample_frac, threads, multipoles=False):
+def cpu_baseline(st, sample_frac, threads, multipoles=False, check_linear=False):
     """The reference engine's algorithm on the host cores: the oracle's
     line-ordered restatement of its loop (recurrences along reflection lines),
     which runs at the reference's own speed (same 3,000 reflections of config 1
-    on x86: 1.87 s vs 1.90 s single-threaded)."""
+    on x86: 1.87 s vs 1.90 s single-threaded).  check_linear: the sample is
+    also timed at half its size, and the ratio of the two times (2 for linear
+    scaling in the reflections) returned."""
     from oracle import oracle as O
+
+    def timed(m):
+        t0 = time.perf_counter()
+        O.compute(st, hkl_subset=np.arange(m), n_threads=threads, multipoles=multipoles, loop="lines")
+        return time.perf_counter() - t0
+
     m = max(1, int(st.n_hkl * sample_frac))
-    sel = np.arange(m)
-    t0 = time.perf_counter()
-    O.compute(st, hkl_subset=sel, n_threads=threads, multipoles=multipoles, loop="lines")
-    dt = time.perf_counter() - t0
+    dt = timed(m)
     terms = st.n_atoms * st.sg.point_group_order * m
+    if check_linear:
+        return terms / dt, dt, m, dt / timed(max(1, m // 2))
     return terms / dt, dt, m
 
 
@@ -665,7 +672,13 @@ def run_gpu(args):
         return 0
     achieved = wl["flops"] * terms / (k32 * 1e-3) * 1e-12
     peak = fp32_peak_tflops(device)
-    cpu_v, cpu_dt, cpu_m = cpu_baseline(st, wl["cpu_frac"], os.cpu_count() or 1, multipoles=mpd)
+    # a sample well below the whole set (config 2): also timed at half its size, to show the linear scaling
+    lin = None
+    if wl["cpu_frac"] < 0.05:
+        cpu_v, cpu_dt, cpu_m, lin = cpu_baseline(st, wl["cpu_frac"], os.cpu_count() or 1, multipoles=mpd,
+                                                 check_linear=True)
+    else:
+        cpu_v, cpu_dt, cpu_m = cpu_baseline(st, wl["cpu_frac"], os.cpu_count() or 1, multipoles=mpd)
     mp = measured_peaks()
     line = {
         "metric": "atom*symop*hkl terms/s (SF+grad)", "value": value, "unit": "terms/s", "n_gpus": world,
@@ -687,7 +700,8 @@ def run_gpu(args):
                      "flops_per_term": wl["flops"], "kernel_ms": k32,
                      "hbm_peak_gbs_measured": mp.get("hbm_gbs")},
         "cpu_baseline": {"value": cpu_v, "unit": "terms/s", "cores": os.cpu_count() or 1, "kind": "port",
-                         "sample": f"{args.workload} atoms x first {cpu_m} reflections, one call ({cpu_dt:.1f} s)"},
+                         "sample": f"{args.workload} atoms x first {cpu_m} reflections, one call ({cpu_dt:.1f} s)"
+                                   + (f"; time ratio to the first {cpu_m // 2}: {lin:.2f} (2 = linear)" if lin else "")},
         "gpu_launches": launches32,
         "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
         "wall_s_timed_region": wall32,
