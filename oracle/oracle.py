@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import time
 import subprocess
 import math
 
@@ -281,6 +282,7 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     res = _Result()
     for k, v in out.items():
         setattr(res, k, _ptr(v, C.c_double))
+    t_c = time.perf_counter()
     if loop == "lines" and model == "hc":
         hk = np.ascontiguousarray(np.asarray(hkl, dtype=np.int32).reshape(-1))
         b3 = np.ascontiguousarray(bm[:, 2], dtype=np.float64)
@@ -288,6 +290,7 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
                                      C.byref(res), int(n_threads))
     else:
         rc = lib().sfo_compute(C.byref(pr), C.byref(res), int(n_threads))
+    t_c = time.perf_counter() - t_c
     if rc != 0:
         raise RuntimeError("oracle failed")
     f = (out["f"][0::2] + 1j * out["f"][1::2]) * mult
@@ -298,7 +301,8 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     for i in range(n):
         if nadp[i] == 6:
             d_adp[i] = convert_adp_gradient(cell, d_adp[i], "U_cart", st.adp_convention)
-    res_d = dict(f=f, d_xyz=d_xyz, d_adp=[d_adp[i, :nadp[i]] for i in range(n)], d_occ=out["d_occ"])
+    # c_seconds: the C computation alone (the algorithm's own time, without this wrapper's array set-up)
+    res_d = dict(f=f, d_xyz=d_xyz, d_adp=[d_adp[i, :nadp[i]] for i in range(n)], d_occ=out["d_occ"], c_seconds=t_c)
     if multipoles:
         res_d.update(d_pval=out["d_pval"], d_plm=out["d_plm"].reshape(n, 25), d_kappa=out["d_kappa"],
                      d_kappa_p=out["d_kappa_p"])

@@ -610,6 +610,31 @@ int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sf
     line_start[n_lines] = nH;
     for (int q = 0; q < n_lines; q++)
         if (line_start[q + 1] - line_start[q] > max_len) max_len = line_start[q + 1] - line_start[q];
+    /* one contiguous share of the ordered reflections per thread, lines cut at the share boundaries (the
+     * reference's splitHklLines, scattering_utilities.cpp:463-513): segments [seg_i0, seg_i0 + seg_len),
+     * thread c takes segments share[c] .. share[c + 1] - 1 */
+    int *seg_i0 = (int *)malloc(sizeof(int) * (n_lines + n_threads + 1));
+    int *seg_len = (int *)malloc(sizeof(int) * (n_lines + n_threads + 1));
+    int *share = (int *)malloc(sizeof(int) * (n_threads + 1));
+    int n_seg = 0;
+    {
+        int q = 0;
+        for (int c = 0; c < n_threads; c++) {
+            const int b0 = (int)((long long)nH * c / n_threads), b1 = (int)((long long)nH * (c + 1) / n_threads);
+            share[c] = n_seg;
+            while (q < n_lines && line_start[q + 1] <= b0) q++;
+            for (int k = q; k < n_lines && line_start[k] < b1; k++) {
+                const int i0 = line_start[k] > b0 ? line_start[k] : b0;
+                const int i1 = line_start[k + 1] < b1 ? line_start[k + 1] : b1;
+                if (i1 > i0) {
+                    seg_i0[n_seg] = i0;
+                    seg_len[n_seg] = i1 - i0;
+                    n_seg++;
+                }
+            }
+        }
+        share[n_threads] = n_seg;
+    }
     /* per atom: crystal-frame P_lm and rotation blocks */
     int *type_wfn = (int *)malloc(sizeof(int) * nT);
     for (int t = 0; t < nT; t++) type_wfn[t] = 0;
@@ -662,9 +687,10 @@ int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sf
         double *Trho = (double *)malloc(sizeof(double) * nS);
         int *is000 = (int *)malloc(sizeof(int) * L);
 
-#pragma omp for schedule(dynamic, 4)
-        for (int q = 0; q < n_lines; q++) {
-            const int i0 = line_start[q], len = line_start[q + 1] - i0;
+#pragma omp for schedule(static, 1)
+        for (int c = 0; c < n_threads; c++)
+        for (int q = share[c]; q < share[c + 1]; q++) {
+            const int i0 = seg_i0[q], len = seg_len[q];
             for (int j = 0; j < len; j++) {
                 const double *h = p->h + 3 * key[i0 + j].idx;
                 const double h2 = h[0] * h[0] + h[1] * h[1] + h[2] * h[2], hl = sqrt(h2);
@@ -892,5 +918,6 @@ int sfo_compute_lines(const sfo_problem *p, const int *hkl, const double *b3, sf
         }
     }
     free(acc); free(pg); free(Dm); free(lmu); free(lmp); free(type_wfn); free(key); free(line_start);
+    free(seg_i0); free(seg_len); free(share);
     return 0;
 }
