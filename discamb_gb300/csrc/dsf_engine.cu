@@ -1911,6 +1911,15 @@ static int call_post(dsf_structure *s, int flags, const dsf_outputs *out, cudaSt
     return DSF_OK;
 }
 
+// reflection chunks of one structure's launch over ntk tiles: many blocks (about 75 per SM over the grid) so the
+// blocks of unequal tiles even out across the SMs, but at least 256 reflections (16 sub-tiles) per block so the
+// per-block set-up (atom loads, line steps, the final derivative commits) stays small
+static int chunk_count(const dsf_engine *e, int ntk, int n_hkl)
+{
+    const int by_sm = std::max(1, e->n_sm) * 75 / std::max(1, ntk);
+    return std::max(1, std::min(by_sm, n_hkl / 256));
+}
+
 // the inversion-pair kernels: FP32 generic models (tabulated, IAM) with a compiled operation count
 static bool inv_kernel(const dsf_structure *s, bool fp64)
 {
@@ -1958,13 +1967,13 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         DSF_CUDA(cudaEventCreate(&s->ev_end));
     }
     DSF_CUDA(cudaEventRecord(s->ev_begin, st));
-    // one launch per ADP kind (tiles [0, n_tiles_plain) without anisotropic ADPs); the
-    // reflection chunks make the grid cover the SMs about eight times
+    // one launch per ADP kind (tiles [0, n_tiles_plain) without anisotropic ADPs), reflection chunks of
+    // chunk_count
     for (int kind = 0; kind < 2; kind++) {
         int nt, n_chunks;
         size_t smem;
         const int ntk = kind ? s->n_tiles - s->n_tiles_plain : s->n_tiles_plain;
-        const int n_chunks0 = std::max(1, std::max(1, e->n_sm) * 8 / std::max(1, ntk));
+        const int n_chunks0 = chunk_count(e, ntk, s->n_hkl);
         const double block_terms = (double)kTileAtoms * ((s->n_hkl + n_chunks0 - 1) / n_chunks0);
         if ((rc = kind_shape(s, kind, fp64, mp, block_terms, L, nt, n_chunks, smem))) return rc;
         if (nt <= 0) continue;
@@ -2108,7 +2117,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
             size_t smem;
             // per-structure launches size their chunks as dsf_calculate_device does
             const int ntk = kind ? s->n_tiles - s->n_tiles_plain : s->n_tiles_plain;
-            const int n_chunks0 = std::max(1, std::max(1, e->n_sm) * 8 / std::max(1, ntk));
+            const int n_chunks0 = chunk_count(e, ntk, s->n_hkl);
             const double own_terms = (double)kTileAtoms * ((s->n_hkl + n_chunks0 - 1) / n_chunks0);
             if ((rc = kind_shape(s, kind, fp64, mp, own_terms, L, nt, n_chunks, smem))) return rc;
             if (nt <= 0) continue;
@@ -2171,13 +2180,14 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
         for (size_t b0 = 0; b0 < g.items.size(); b0 += kBatchItems) {
             const int m = (int)std::min<size_t>(kBatchItems, g.items.size() - b0);
             B.n = m;
-            // atom x reflection pairs per block for this launch: about eight blocks per SM
+            // atom x reflection pairs per block for this launch: about 24 blocks per SM, so blocks of unequal
+            // items even out across the SMs
             double pairs = 0;
             for (int k = 0; k < m; k++) {
                 const SfBatchItem &it = g.items[b0 + k];
                 pairs += (double)it.n_tiles * kTileAtoms * it.S.n_hkl;
             }
-            const double block_terms = std::max<double>(kTileAtoms * 64.0, pairs / (std::max(1, e->n_sm) * 8.0));
+            const double block_terms = std::max<double>(kTileAtoms * 64.0, pairs / (std::max(1, e->n_sm) * 24.0));
             int blocks = 0;
             for (int k = 0; k < m; k++) {
                 B.item[k] = g.items[b0 + k];
