@@ -83,6 +83,10 @@ struct DevStructure {
     int table_split, table_shift;  // column of sorted atom a: a + (a >= split ? shift : 0) (even tile starts)
     const int *atom_orig;        // sorted -> original atom index
     const int *atom_plm_lmax;    // highest l of the atom's P_lm parameters (-1: none)
+    // per (sorted atom, operation): the line step e^{2 pi i ((R^T e_l).x + t_l)}, computed in FP64 with the
+    // atom conversion (once per atom upload, not per block)
+    const float2 *atom_step_f;
+    const double2 *atom_step_d;
 };
 
 struct CallBuffers {

@@ -229,7 +229,7 @@ struct dsf_structure {
         d_types_f, d_tcoeff, d_texp, d_tpow, d_texp_f, d_tpre_f, d_hkl, d_h2, d_h2f, d_hmult, d_cinv, d_table_f, d_table_d, d_perm, d_multw, d_dmat,
         d_raw, d_dtdf, d_gw_d, d_gw_f, d_facc, d_gacc, d_out, d_plm_lmax,
         d_rs_f, d_rs_d, d_tr_f, d_tr_d, d_trm_f, d_trm_d, d_err, d_hperm, d_cont, d_tile_lmax,
-        d_lcs, d_type_plm, d_type_lmax, d_atom_type0;
+        d_lcs, d_type_plm, d_type_lmax, d_atom_type0, d_step_f, d_step_d;
     std::vector<int> hperm;  // line-ordered reflection -> caller's index
     int n_hkl_pad = 0;
     // resident tables per precision (0: FP32, 1: FP64), built when a call first needs them
@@ -468,7 +468,8 @@ struct AtomParams {
 // raw atoms (original order: xyz[3], adp[6], occ) -> kernel representation (sorted order)
 __global__ void atom_convert_kernel(AtomParams P, const double *raw, const int *perm, const int *adpk,
                                     const double *mult_w, uint32_t *xq, float *xlo, double *xd, float *adp_f,
-                                    double *adp_d, float *w_f, double *w_d)
+                                    double *adp_d, float *w_f, double *w_d, int n_sym, const int *sym_rot,
+                                    const int *sym_t24, float2 *step_f, double2 *step_d)
 {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= P.n_atoms) return;
@@ -486,6 +487,16 @@ __global__ void atom_convert_kernel(AtomParams P, const double *raw, const int *
         const double q = rint(xr * 4294967296.0);
         xlo[3 * a + i] = (float)(xr - q * (1.0 / 4294967296.0));
         xq[3 * a + i] = (uint32_t)(unsigned long long)q;  // 2^32 wraps to 0
+    }
+    // line steps of the reflection-line recurrence: h -> h + e_l changes h'.x + h.t by row 3 of R times x plus t_z
+    for (int op = 0; op < n_sym; op++) {
+        const int *Rm = sym_rot + 9 * op;
+        double ph = Rm[6] * x[0] + Rm[7] * x[1] + Rm[8] * x[2] + sym_t24[3 * op + 2] / 24.0;
+        ph -= rint(ph);
+        double sn, cs;
+        sincospi(2.0 * ph, &sn, &cs);
+        step_d[(size_t)a * n_sym + op] = make_double2(cs, sn);
+        step_f[(size_t)a * n_sym + op] = make_float2((float)cs, (float)sn);
     }
     const double two_pi2 = 2.0 * DSF_PI * DSF_PI;
     const int k = adpk[a];
@@ -1052,6 +1063,8 @@ void refresh_dev(dsf_structure *s)
     d.table_split = s->table_split;
     d.table_shift = s->table_shift;
     d.atom_orig = s->d_perm.as<int>();
+    d.atom_step_f = s->d_step_f.as<float2>();
+    d.atom_step_d = s->d_step_d.as<double2>();
     d.atom_plm_lmax = s->d_plm_lmax.as<int>();
 }
 
@@ -1104,6 +1117,8 @@ int finish_create(dsf_engine *e, dsf_structure *s)
     if ((rc = upload(e, s->d_sym_rot, s->sym_rot.data(), s->sym_rot.size()))) return rc;
     if ((rc = upload(e, s->d_sym_t24, s->sym_t24.data(), s->sym_t24.size()))) return rc;
     if ((rc = upload_types(s))) return rc;
+    DSF_CUDA(s->d_step_f.alloc(sizeof(float2) * (size_t)s->n_atoms * s->n_sym));
+    DSF_CUDA(s->d_step_d.alloc(sizeof(double2) * (size_t)s->n_atoms * s->n_sym));
     refresh_dev(s);
     DSF_CUDA(cudaStreamSynchronize(e->setup));
     return DSF_OK;
@@ -1547,7 +1562,7 @@ int dsf_structure_destroy(dsf_structure *s)
                       &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc, &s->d_out, &s->d_plm_lmax,
                       &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d, &s->d_trm_f, &s->d_trm_d, &s->d_err,
                       &s->d_hperm, &s->d_cont, &s->d_tile_lmax, &s->d_lcs, &s->d_type_plm, &s->d_type_lmax,
-                      &s->d_atom_type0};
+                      &s->d_atom_type0, &s->d_step_f, &s->d_step_d};
     for (DevBuf *b : bufs) b->release();
     if (s->ev_begin) cudaEventDestroy(s->ev_begin);
     if (s->ev_end) cudaEventDestroy(s->ev_end);
@@ -1680,7 +1695,8 @@ int dsf_structure_update_atoms(dsf_structure *s, const double *xyz, const double
     atom_convert_kernel<<<(n + 127) / 128, 128, 0, e->stream>>>(
         P, s->d_raw.as<double>(), s->d_perm.as<int>(), s->d_atom_adpk.as<int>(), s->d_multw.as<double>(),
         s->d_xq.as<uint32_t>(), s->d_xlo.as<float>(), s->d_xd.as<double>(), s->d_adp_f.as<float>(),
-        s->d_adp_d.as<double>(), s->d_w_f.as<float>(), s->d_w_d.as<double>());
+        s->d_adp_d.as<double>(), s->d_w_f.as<float>(), s->d_w_d.as<double>(), s->n_sym, s->d_sym_rot.as<int>(),
+        s->d_sym_t24.as<int>(), s->d_step_f.as<float2>(), s->d_step_d.as<double2>());
     DSF_CUDA(cudaGetLastError());
     DSF_CUDA(cudaStreamSynchronize(e->stream));
     s->have_atoms = true;
@@ -1766,7 +1782,7 @@ int64_t dsf_structure_device_bytes(const dsf_structure *s)
                             &s->d_dmat, &s->d_raw, &s->d_dtdf, &s->d_gw_d, &s->d_gw_f, &s->d_facc, &s->d_gacc,
                             &s->d_out, &s->d_plm_lmax, &s->d_rs_f, &s->d_rs_d, &s->d_tr_f, &s->d_tr_d,
                             &s->d_trm_f, &s->d_trm_d, &s->d_err, &s->d_hperm, &s->d_cont, &s->d_tile_lmax,
-                            &s->d_lcs, &s->d_type_plm, &s->d_type_lmax, &s->d_atom_type0};
+                            &s->d_lcs, &s->d_type_plm, &s->d_type_lmax, &s->d_atom_type0, &s->d_step_f, &s->d_step_d};
     int64_t b = 0;
     for (const DevBuf *p : bufs) b += (int64_t)p->bytes;
     return b;
@@ -2319,7 +2335,8 @@ static int host_send(dsf_structure *s, bool atoms, const HostCall &hc)
         atom_convert_kernel<<<(n + 127) / 128, 128, 0, e->stream>>>(
             P, s->d_raw.as<double>(), s->d_perm.as<int>(), s->d_atom_adpk.as<int>(), s->d_multw.as<double>(),
             s->d_xq.as<uint32_t>(), s->d_xlo.as<float>(), s->d_xd.as<double>(), s->d_adp_f.as<float>(),
-            s->d_adp_d.as<double>(), s->d_w_f.as<float>(), s->d_w_d.as<double>());
+            s->d_adp_d.as<double>(), s->d_w_f.as<float>(), s->d_w_d.as<double>(), s->n_sym, s->d_sym_rot.as<int>(),
+            s->d_sym_t24.as<int>(), s->d_step_f.as<float2>(), s->d_step_d.as<double2>());
         DSF_CUDA(cudaGetLastError());
         s->have_atoms = true;
     }

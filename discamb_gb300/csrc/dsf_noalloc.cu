@@ -402,7 +402,7 @@ extern "C" int dsf_iam_calculate_noalloc(const dsf_symmetry *sym, const dsf_iam_
     if ((ce = cudaMemsetAsync(S.f_acc, 0, sizeof(double2) * (size_t)n_hkl, st)) != cudaSuccess ||
         (ce = cudaMemsetAsync(S.g_acc, 0, sizeof(double) * kNch * (size_t)n_atoms, st)) != cudaSuccess)
         return report(err, err_len, DSF_ERR_CUDA, cudaGetErrorString(ce));
-    DevStructure D;
+    DevStructure D{};
     std::memset(&D, 0, sizeof D);
     D.model = MODEL_IAM;
     D.n_atoms = n_atoms;

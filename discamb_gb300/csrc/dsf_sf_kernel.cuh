@@ -451,17 +451,18 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                 for (int q = 0; q < 25; q++) pg[q] = S.atom_pg_d[25 * a + q];
         }
         if constexpr (REC) {
-            // line steps in FP64, rounded once
-            const double xa = S.atom_xd[3 * a], xb = S.atom_xd[3 * a + 1], xc = S.atom_xd[3 * a + 2];
+            // line steps (computed in FP64 with the atom conversion, once per atom upload)
 #pragma unroll
             for (int s = 0; s < (INV ? NR / 2 : NR); s++) {  // INV: the images need no line steps
-                const int *Rm = S.sym_rot + 9 * s;
-                double ph = Rm[6] * xa + Rm[7] * xb + Rm[8] * xc + S.sym_t24[3 * s + 2] / 24.0;
-                ph -= rint(ph);
-                double sn, cs;
-                sincospi(2.0 * ph, &sn, &cs);
-                step_re[s] = R(cs);
-                step_im[s] = R(sn);
+                if constexpr (F32) {
+                    const float2 st = S.atom_step_f[(size_t)a * NR + s];
+                    step_re[s] = st.x;
+                    step_im[s] = st.y;
+                } else {
+                    const double2 st = S.atom_step_d[(size_t)a * NR + s];
+                    step_re[s] = st.x;
+                    step_im[s] = st.y;
+                }
             }
         }
     }
