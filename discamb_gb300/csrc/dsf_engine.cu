@@ -1929,11 +1929,12 @@ static int call_post(dsf_structure *s, int flags, const dsf_outputs *out, cudaSt
 
 // reflection chunks of one structure's launch over ntk tiles: many blocks (about 75 per SM over the grid) so the
 // blocks of unequal tiles even out across the SMs, but at least 256 reflections (16 sub-tiles) per block so the
-// per-block set-up (atom loads, line steps, the final derivative commits) stays small
+// per-block set-up (atom loads, the final derivative commits) stays small -- unless that leaves fewer than four
+// blocks per SM (small structures)
 static int chunk_count(const dsf_engine *e, int ntk, int n_hkl)
 {
-    const int by_sm = std::max(1, e->n_sm) * 75 / std::max(1, ntk);
-    return std::max(1, std::min(by_sm, n_hkl / 256));
+    const int sm = std::max(1, e->n_sm), t = std::max(1, ntk);
+    return std::max(1, std::max(std::min(sm * 75 / t, n_hkl / 256), sm * 4 / t));
 }
 
 // the inversion-pair kernels: FP32 generic models (tabulated, IAM) with a compiled operation count
