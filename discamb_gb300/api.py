@@ -121,6 +121,7 @@ def library():
                                                _P(C.c_void_p)]
         L.dsf_tsc_load.argtypes = [C.c_char_p, _P(C.c_int), _P(C.c_int), _P(C.c_int), _P(C.c_double), C.c_int]
         L.dsf_form_factors.argtypes = [C.c_void_p, _P(C.c_int), _P(C.c_int), _P(C.c_double)]
+        L.dsf_debug_stall_next_call.argtypes = [C.c_void_p]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
@@ -359,6 +360,12 @@ class _Calculator:
         d_adp = a["d_adp"] + 1j * b["d_adp"]
         return dict(f=a["f"][0], d_xyz=a["d_xyz"] + 1j * b["d_xyz"],
                     d_adp=[d_adp[i, :nadp[i]] for i in range(self.n_atoms)], d_occ=a["d_occ"] + 1j * b["d_occ"])
+
+    def debug_stall_next_call(self):
+        """Test hook of the failure path (dsf_debug_stall_next_call): the
+        next call's kernel waits run out and the call raises DsfError
+        (DSF_ERR_TIMEOUT) after about 4 s; the engine stays usable."""
+        self.engine.check(self.lib.dsf_debug_stall_next_call(self.h), "debug_stall_next_call")
 
     def form_factors(self, hkl, include=None):
         """The single-h calculateFormFactors of the reference

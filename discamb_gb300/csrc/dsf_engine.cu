@@ -207,6 +207,7 @@ struct dsf_structure {
     int electron = 0;            // HC: Mott-Bethe electron scattering
     int coset_size = 0;
     int inv_pairs = 0;  // generic models: operations n/2 .. n-1 are the images of 0 .. n/2-1 under -1 at the origin
+    int debug_stall = 0;  // dsf_debug_stall_next_call: the next call's kernel waits run out (timeout test)
     std::vector<int> sym_sign;   // [n_sym][3] Cartesian
     std::vector<int> sym_fsign;  // [n_sym][3] fractional h' components
     // tabulated model: column of sorted atom a = a + (a >= table_split ? table_shift : 0), table_stride
@@ -1844,6 +1845,8 @@ static void call_buffers(dsf_structure *s, bool fp64, CallBuffers &C, SfLaunch &
     L.tr = fp64 ? s->d_tr_d.p : s->d_tr_f.p;
     L.trm = fp64 ? s->d_trm_d.p : s->d_trm_f.p;
     L.error = s->d_err.as<int>();
+    L.stall_first = s->debug_stall;
+    s->debug_stall = 0;
     L.cont = s->d_cont.as<int>();
     L.tile_lmax = s->d_tile_lmax.as<int>();
     // coset kernels: operations in sign-diagonal cosets (HC: harmonics and ADPs; other models: ADPs)
@@ -2424,6 +2427,13 @@ int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf
                                                             per_type->d_plm, per_type->d_kappa,
                                                             per_type->d_kappa_prime);
     DSF_CUDA(cudaGetLastError());
+    return DSF_OK;
+}
+
+int dsf_debug_stall_next_call(dsf_structure *s)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    s->debug_stall = 1;
     return DSF_OK;
 }
 

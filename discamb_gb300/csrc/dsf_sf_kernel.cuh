@@ -132,13 +132,14 @@ __device__ __forceinline__ uint64_t global_ns()
     return t;
 }
 
-// wait for phase `parity` of the barrier; false after ~2 s (the kernel then
-// reports DSF_ERR_TIMEOUT instead of hanging)
+// wait for phase `parity` of the barrier; false after ~2 s of %globaltimer,
+// or after 2^26 polls whatever the timer says (the kernel then reports
+// DSF_ERR_TIMEOUT instead of hanging)
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
 {
     const uint32_t a = smem_u32(bar);
     uint64_t t0 = 0;
-    for (uint32_t it = 0;; it++) {
+    for (uint32_t it = 0; it < (1u << 26); it++) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
@@ -149,6 +150,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
         if (it == 0) t0 = global_ns();
         else if ((it & 63u) == 0 && global_ns() - t0 > 2000000000ull) return false;
     }
+    return false;
 }
 
 // ---------------------------------------------------------------------------
@@ -166,6 +168,8 @@ struct SfLaunch {
     const int *cont;       // [n_hkl_pad] 1: reflection = previous one + (0,0,1) (reflections in line order)
     const int *tile_lmax;  // [n_tiles] highest l of the angular sums of the tile's atoms
     int *error;            // set to 1 on a timed-out wait
+    int stall_first;       // test hook (dsf_debug_stall_next_call): the first sub-tile's copies are not issued, so
+                           // its waits run out and the call returns DSF_ERR_TIMEOUT
     int coset;             // size of the sign-diagonal cosets the operations are ordered in (0: none)
 };
 
@@ -488,7 +492,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     };
     tab_load(h_begin);
 
-    if (tid == 0) issue(0, h_begin);
+    if (tid == 0 && !L.stall_first) issue(0, h_begin);
     uint32_t parity[2] = {0u, 0u};
     int k = 0;
     // per-thread partial derivative sums, folded into the compensated totals

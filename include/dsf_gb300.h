@@ -235,6 +235,11 @@ int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf
  * (re, im) in the caller's atom order, no anomalous dispersion, 0 for atoms with include[a] == 0 (include may be
  * NULL); FP64, synchronous.  HC and IAM structures; DSF_ERR_UNSUPPORTED for the tabulated model. */
 int dsf_form_factors(dsf_structure *s, const int *hkl, const int *include, double *ff);
+/* test hook of the failure path: the next single-structure FP32/FP64 call of s issues no copies for its first
+ * reflection sub-tile, so every block's bounded wait runs out (about 4 s), the kernel sets its error flag and exits,
+ * and a host-buffer call returns DSF_ERR_TIMEOUT; the engine stays usable.  No reference counterpart (the reference
+ * GPU code exit()s on errors, src/GPU/cuda/globals.h:22). */
+int dsf_debug_stall_next_call(dsf_structure *s);
 /* the same with host buffers (dtdf[i] [n_hkl_i][2], include[i] NULL = all atoms, outputs on the host); one
  * stream synchronisation for the whole batch */
 int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int derivative_flags,
