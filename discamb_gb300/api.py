@@ -33,6 +33,7 @@ _P = C.POINTER
 
 DSF_FP64 = 0
 DSF_FP32_BULK = 1
+DSF_PENDING = 7
 DSF_D_XYZ, DSF_D_ADP, DSF_D_OCC, DSF_D_MULTIPOLE = 1, 2, 4, 8
 _ADP = {"U_cif": 0, "U_cart": 1, "U_star": 2}
 _XYZ = {"fractional": 0, "cartesian": 1}
@@ -122,6 +123,9 @@ def library():
         L.dsf_tsc_load.argtypes = [C.c_char_p, _P(C.c_int), _P(C.c_int), _P(C.c_int), _P(C.c_double), C.c_int]
         L.dsf_form_factors.argtypes = [C.c_void_p, _P(C.c_int), _P(C.c_int), _P(C.c_double)]
         L.dsf_debug_stall_next_call.argtypes = [C.c_void_p]
+        L.dsf_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_double),
+                                 _P(C.c_double), _P(C.c_int), _P(_Out), _P(C.c_void_p)]
+        L.dsf_poll.argtypes = [C.c_void_p, C.c_int]
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
@@ -141,6 +145,33 @@ def _d(a):
 def _i(a):
     a = np.ascontiguousarray(a, dtype=np.int32)
     return a, a.ctypes.data_as(_P(C.c_int))
+
+
+class Ticket:
+    """A submitted call (dsf_submit): poll(timeout_ms) returns the result
+    dict once the call is done, None while it is pending; it raises DsfError
+    if the call failed."""
+
+    def __init__(self, calc, handle, out, multipoles, adp_layout, keep):
+        self._calc, self._h, self._out = calc, handle, out
+        self._mp, self._layout, self._keep = multipoles, adp_layout, keep
+        self.result = None
+
+    def poll(self, timeout_ms=0):
+        if self.result is not None:
+            return self.result
+        rc = self._calc.lib.dsf_poll(self._h, int(timeout_ms))
+        if rc == DSF_PENDING:
+            return None
+        self._keep = None
+        self._calc.engine.check(rc, "poll")
+        self.result = self._calc._result(self._out, self._mp, self._layout)
+        return self.result
+
+    def wait(self):
+        while self.poll(1000) is None:
+            pass
+        return self.result
 
 
 class Engine:
@@ -441,6 +472,30 @@ class _Calculator:
             self.engine.check(self.lib.dsf_calculate_atoms(self.h, int(precision), flags, p1, p2, p3, gp, inc,
                                                            C.byref(o)), "calculate")
         return self._result(r, multipoles, adp_layout)
+
+    def submit(self, dtdf, precision=DSF_FP64, derivatives=("xyz", "adp", "occ"), multipoles=False,
+               include=None, atoms=None, adp_layout="list"):
+        """The same call, asynchronous (dsf_submit): returns a Ticket at once;
+        Ticket.poll(timeout_ms) gives the result dict when the call is done
+        (None while it is pending).  One pending call per calculator."""
+        flags = _flags(derivatives, multipoles)
+        g = np.ascontiguousarray(dtdf, dtype=np.complex128).view(np.float64)
+        r = self._out_arrays(multipoles)
+        o = _Out()
+        self._fill_out(o, r, multipoles)
+        inc, keep = None, [g]
+        if include is not None:
+            incarr, inc = _i(np.asarray(include, dtype=np.int32))
+            keep.append(incarr)
+        ps = (None, None, None)
+        if atoms is not None:
+            (x1, p1), (x2, p2), (x3, p3) = self._atom_arrays(*atoms)
+            keep += [x1, x2, x3]
+            ps = (p1, p2, p3)
+        t = C.c_void_p()
+        self.engine.check(self.lib.dsf_submit(self.h, int(precision), flags, *ps, g.ctypes.data_as(_P(C.c_double)),
+                                              inc, C.byref(o), C.byref(t)), "submit")
+        return Ticket(self, t, r, multipoles, adp_layout, keep + [o])
 
     def calculate_structure_factors_and_derivatives(self, xyz, adp, occupancy, hkl, dtdf, include=None,
                                                     precision=DSF_FP64, multipoles=False):

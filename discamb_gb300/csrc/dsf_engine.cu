@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -208,6 +209,7 @@ struct dsf_structure {
     int coset_size = 0;
     int inv_pairs = 0;  // generic models: operations n/2 .. n-1 are the images of 0 .. n/2-1 under -1 at the origin
     int debug_stall = 0;  // dsf_debug_stall_next_call: the next call's kernel waits run out (timeout test)
+    int pending = 0;      // a dsf_submit call of this structure not yet completed by dsf_poll
     std::vector<int> sym_sign;   // [n_sym][3] Cartesian
     std::vector<int> sym_fsign;  // [n_sym][3] fractional h' components
     // tabulated model: column of sorted atom a = a + (a >= table_split ? table_shift : 0), table_stride
@@ -1552,6 +1554,7 @@ int dsf_structure_create_tsc(dsf_engine *e, const dsf_symmetry *sym, const dsf_a
 int dsf_structure_destroy(dsf_structure *s)
 {
     if (!s) return DSF_ERR_ARGUMENT;
+    if (s->pending) return fail(s->eng, DSF_ERR_STATE, "a submitted call of this structure is still pending (dsf_poll)");
     cudaSetDevice(s->eng->device);
     cudaStreamSynchronize(s->eng->stream);
     cudaStreamSynchronize(s->eng->setup);
@@ -2259,6 +2262,7 @@ static int host_begin(dsf_structure *s, const double *xyz, const double *occ, co
     if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
     if (!s->have_hkl) return fail(e, DSF_ERR_STATE, "no reflections set");
+    if (s->pending) return fail(e, DSF_ERR_STATE, "a submitted call of this structure is still pending (dsf_poll)");
     if (!out || (s->n_hkl > 0 && (!out->f || !dtdf))) return fail(e, DSF_ERR_ARGUMENT, "dtdf and f are required");
     if ((xyz != nullptr) != (occ != nullptr)) return fail(e, DSF_ERR_ARGUMENT, "xyz and occupancy go together");
     cudaSetDevice(e->device);
@@ -2407,6 +2411,69 @@ static int calculate_host(dsf_structure *s, int precision, int flags, const doub
     if ((rc = host_status(s, hc))) return rc;
     host_copy_out(s, flags, hc, out);
     return DSF_OK;
+}
+
+// an asynchronous host-buffer call (dsf_submit / dsf_poll)
+struct dsf_ticket {
+    dsf_structure *s = nullptr;
+    int flags = 0;
+    HostCall hc;
+    dsf_outputs out{};
+    cudaEvent_t done = nullptr;
+};
+
+int dsf_submit(dsf_structure *s, int precision, int flags, const double *xyz, const double *adp,
+               const double *occupancy, const double *dtdf, const int *include, const dsf_outputs *out,
+               dsf_ticket **ticket)
+{
+    if (!s || !ticket || !out) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    *ticket = nullptr;
+    auto *t = new dsf_ticket;
+    int rc = host_stage(s, xyz, adp, occupancy, dtdf, include, out, t->hc);
+    if (!rc) rc = dsf_calculate_device(s, precision, flags, s->d_dtdf.as<double>(), &t->hc.d, e->stream);
+    if (!rc) rc = host_readback(s, flags, t->hc);
+    if (!rc && (cudaEventCreateWithFlags(&t->done, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventRecord(t->done, e->stream) != cudaSuccess))
+        rc = fail(e, DSF_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    if (rc) {
+        if (t->done) cudaEventDestroy(t->done);
+        delete t;
+        return rc;
+    }
+    t->s = s;
+    t->flags = flags;
+    t->out = *out;
+    s->pending = 1;
+    *ticket = t;
+    return DSF_OK;
+}
+
+int dsf_poll(dsf_ticket *t, int timeout_ms)
+{
+    if (!t) return DSF_ERR_ARGUMENT;
+    dsf_structure *s = t->s;
+    cudaSetDevice(s->eng->device);
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t q = cudaEventQuery(t->done);
+        if (q == cudaSuccess) break;
+        if (q != cudaErrorNotReady) {  // the call failed on the device: release the ticket, report
+            s->pending = 0;
+            cudaEventDestroy(t->done);
+            delete t;
+            return fail(s->eng, DSF_ERR_CUDA, cudaGetErrorString(q));
+        }
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (ms >= timeout_ms) return DSF_PENDING;
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    int rc = host_status(s, t->hc);
+    if (!rc) host_copy_out(s, t->flags, t->hc, &t->out);
+    s->pending = 0;
+    cudaEventDestroy(t->done);
+    delete t;
+    return rc;
 }
 
 int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf_outputs *per_type, void *stream)

@@ -34,6 +34,7 @@
  *                               TscFileBasedSfCalculator / tsc_io::read_tsc (the .tsc reader)
  *   dsf_structure_set_electron  HansenCoppensStructureFactorCalculator::setElectronScattering
  *   dsf_reduce_to_types         per-type multipole derivatives for TAAM callers (no reference counterpart)
+ *   dsf_submit, dsf_poll        asynchronous form of dsf_calculate_atoms for serving (no reference counterpart)
  *   dsf_form_factors            SfCalculator::calculateFormFactors(hkl, ff, includeAtom) (SfCalculator.h:82-93;
  *                               HansenCoppensStructureFactorCalculator.cpp:1277-1304, AnyIamCalculator.cpp:223-233)
  *   dsf_last_error              on_error::throwException messages (include/discamb/BasicUtilities/on_error.h:24-36):
@@ -66,7 +67,8 @@ enum dsf_status {
     DSF_ERR_MEMORY = 3,     /* device or host allocation failed, or over the memory budget */
     DSF_ERR_STATE = 4,      /* call not valid in the current state (e.g. no reflections set) */
     DSF_ERR_TIMEOUT = 5,    /* a bounded wait ran out */
-    DSF_ERR_UNSUPPORTED = 6
+    DSF_ERR_UNSUPPORTED = 6,
+    DSF_PENDING = 7         /* dsf_poll: the submitted call has not finished within the timeout; poll again */
 };
 
 enum dsf_precision { DSF_FP64 = 0, DSF_FP32_BULK = 1 };
@@ -84,6 +86,7 @@ enum dsf_derivative_flags {
 
 typedef struct dsf_engine dsf_engine;
 typedef struct dsf_structure dsf_structure;
+typedef struct dsf_ticket dsf_ticket;
 
 /* Crystal symmetry as the engine consumes it.  Either the engine subset
  * (operations modulo inversion and lattice centering, centrosymmetric = 1,
@@ -240,6 +243,17 @@ int dsf_form_factors(dsf_structure *s, const int *hkl, const int *include, doubl
  * and a host-buffer call returns DSF_ERR_TIMEOUT; the engine stays usable.  No reference counterpart (the reference
  * GPU code exit()s on errors, src/GPU/cuda/globals.h:22). */
 int dsf_debug_stall_next_call(dsf_structure *s);
+/* asynchronous dsf_calculate_atoms for serving (xyz/adp/occupancy may be NULL: the resident atoms): the inputs are
+ * staged before the call returns (the caller may reuse its input buffers at once), the kernels and the readback
+ * are queued on the engine's stream, and *ticket identifies the call.  The output buffers are written by dsf_poll.
+ * One pending call per structure (DSF_ERR_STATE otherwise); other structures of the engine may be submitted
+ * meanwhile.  The reference calls synchronously (SfCalculator.h:45-67); a serving caller overlaps its own work. */
+int dsf_submit(dsf_structure *s, int precision, int derivative_flags, const double *xyz, const double *adp,
+               const double *occupancy, const double *dtdf, const int *include, const dsf_outputs *out,
+               dsf_ticket **ticket);
+/* waits up to timeout_ms (0: test only) for a submitted call: DSF_OK with the outputs written (the ticket is
+ * released), DSF_PENDING (the ticket stays valid: poll again), or the call's error (the ticket is released) */
+int dsf_poll(dsf_ticket *ticket, int timeout_ms);
 /* the same with host buffers (dtdf[i] [n_hkl_i][2], include[i] NULL = all atoms, outputs on the host); one
  * stream synchronisation for the whole batch */
 int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int derivative_flags,

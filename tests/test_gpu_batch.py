@@ -242,3 +242,26 @@ def test_multipole_derivatives_reduced_to_types(engine):
         got = pt[k].cpu().numpy().reshape(ref.shape)
         assert rel_norm(got, ref) < 1e-10, k
     calc.close()
+
+
+def test_submit_and_poll(engine):
+    # asynchronous calls (dsf_submit / dsf_poll) on two structures at once equal the synchronous ones; a second
+    # submit on a structure with a pending call is refused; a failed call (stalled producer) reports through poll
+    sts = [W.small_case("P212121", n_atoms=40, stol_max=0.6, seed=91), W.config1(n_atoms=800)]
+    calcs = [api.HcCalculator(engine, st) for st in sts]
+    want = [c.calculate(st.dtdf, precision=FP32, adp_layout="padded") for c, st in zip(calcs, sts)]
+    atoms = [(st.xyz, st.adp_array(), st.occupancy) for st in sts]
+    tickets = [c.submit(st.dtdf, precision=FP32, atoms=a, adp_layout="padded") for c, st, a in zip(calcs, sts, atoms)]
+    with pytest.raises(api.DsfError, match="pending"):
+        calcs[0].submit(sts[0].dtdf, precision=FP32)
+    got = [t.wait() for t in tickets]
+    for g, w in zip(got, want):
+        assert rel_f(g["f"], w["f"]) < 1e-12
+        assert rel_norm(g["d_xyz"], w["d_xyz"]) < 1e-12 and rel_norm(g["d_adp"], w["d_adp"]) < 1e-12
+    calcs[0].debug_stall_next_call()
+    t = calcs[0].submit(sts[0].dtdf, precision=FP32)
+    with pytest.raises(api.DsfError, match="ran out"):
+        t.wait()
+    assert rel_f(calcs[0].calculate(sts[0].dtdf, precision=FP32)["f"], want[0]["f"]) < 1e-12
+    for c in calcs:
+        c.close()
