@@ -123,6 +123,7 @@ def library():
         L.dsf_tsc_load.argtypes = [C.c_char_p, _P(C.c_int), _P(C.c_int), _P(C.c_int), _P(C.c_double), C.c_int]
         L.dsf_form_factors.argtypes = [C.c_void_p, _P(C.c_int), _P(C.c_int), _P(C.c_double)]
         L.dsf_debug_stall_next_call.argtypes = [C.c_void_p]
+        L.dsf_structure_set_anomalous.argtypes = [C.c_void_p, _P(C.c_double)]
         L.dsf_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_double), _P(C.c_double), _P(C.c_double),
                                  _P(C.c_double), _P(C.c_int), _P(_Out), _P(C.c_void_p)]
         L.dsf_poll.argtypes = [C.c_void_p, C.c_int]
@@ -391,6 +392,13 @@ class _Calculator:
         d_adp = a["d_adp"] + 1j * b["d_adp"]
         return dict(f=a["f"][0], d_xyz=a["d_xyz"] + 1j * b["d_xyz"],
                     d_adp=[d_adp[i, :nadp[i]] for i in range(self.n_atoms)], d_occ=a["d_occ"] + 1j * b["d_occ"])
+
+    def set_anomalous(self, anomalous):
+        """Per-atom anomalous dispersion f' + i f'' (complex [n_atoms]),
+        replacing the values given at creation (SfCalculator::setAnomalous)."""
+        a = np.asarray(anomalous, dtype=np.complex128).reshape(-1)
+        v, p = _d(np.stack([a.real, a.imag], axis=1).reshape(-1))
+        self.engine.check(self.lib.dsf_structure_set_anomalous(self.h, p), "set_anomalous")
 
     def debug_stall_next_call(self):
         """Test hook of the failure path (dsf_debug_stall_next_call): the

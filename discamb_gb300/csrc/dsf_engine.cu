@@ -2497,6 +2497,36 @@ int dsf_reduce_to_types(dsf_structure *s, const dsf_outputs *per_atom, const dsf
     return DSF_OK;
 }
 
+int dsf_structure_set_anomalous(dsf_structure *s, const double *anomalous)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (!anomalous) return fail(e, DSF_ERR_ARGUMENT, "anomalous dispersion [n_atoms][2] is required");
+    const int n = s->n_atoms;
+    std::vector<double> an_d(2 * (size_t)n);
+    std::vector<float> an_f(2 * (size_t)n);
+    for (int i = 0; i < n; i++) {
+        for (int k = 0; k < 2; k++) {
+            if (!std::isfinite(anomalous[2 * i + k])) return fail(e, DSF_ERR_ARGUMENT, "non-finite anomalous dispersion");
+            s->anom[2 * i + k] = anomalous[2 * i + k];
+        }
+    }
+    for (int i = 0; i < n; i++) {  // engine (sorted) order
+        const int o = s->perm[i];
+        an_d[2 * i] = s->anom[2 * o];
+        an_d[2 * i + 1] = s->anom[2 * o + 1];
+        an_f[2 * i] = (float)an_d[2 * i];
+        an_f[2 * i + 1] = (float)an_d[2 * i + 1];
+    }
+    cudaSetDevice(e->device);
+    DSF_CUDA(cudaStreamSynchronize(e->stream));  // no call of the engine's stream still reads the old values
+    int rc;
+    if ((rc = upload(e, s->d_anom_d, an_d.data(), an_d.size()))) return rc;
+    if ((rc = upload(e, s->d_anom_f, an_f.data(), an_f.size()))) return rc;
+    DSF_CUDA(cudaStreamSynchronize(e->setup));
+    return DSF_OK;
+}
+
 int dsf_debug_stall_next_call(dsf_structure *s)
 {
     if (!s) return DSF_ERR_ARGUMENT;

@@ -8,7 +8,7 @@
  *   calculateStructureFactorsAndDerivatives(hkl, f, SfDerivativesAtHkl,
  *       countAtomContribution)    (single h)        SfCalculator.h:82-86
  *   calculateFormFactors(hkl, ff, includeAtom)      SfCalculator.h:89
- *   update(atoms), setN_threads(n)
+ *   update(atoms), setAnomalous(anomalous), setN_threads(n)
  *
  * The reflection set stays resident on the GPU between calls (it is re-sent
  * only when the caller passes another one), the atoms' parameters travel with
@@ -109,6 +109,14 @@ public:
 
     // the atoms of the following single-h and form-factor calls
     void update(const std::vector<AtomInCrystal> &atoms) { atoms_ = atoms; }
+
+    // per-atom anomalous dispersion f' + i f'' (SfCalculator::setAnomalous)
+    void setAnomalous(const std::vector<cplx> &anomalous)
+    {
+        if (anomalous.size() != (size_t)n_atoms_) throw Error("anomalous dispersion size differs from the atom count");
+        engine_->check(dsf_structure_set_anomalous(s_, reinterpret_cast<const double *>(anomalous.data())),
+                       "setAnomalous");
+    }
 
     // F and dF/dparam at one reflection, with the atoms of the last call or update: two one-reflection calls
     // (dT/dF = 1 gives dA/dp, dT/dF = i gives dB/dp); the resident reflection set is restored afterwards

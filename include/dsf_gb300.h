@@ -17,6 +17,7 @@
  *   dsf_structure_update_atoms  SfCalculator::update / the atoms argument
  *                               (prepareDataForEngine_part, HansenCoppensStructureFactorCalculator.cpp:897-990)
  *   dsf_structure_update_types  HC_ModelParameters::type_parameters (P_lm, P_val, kappa, kappa')
+ *   dsf_structure_set_anomalous SfCalculator::setAnomalous (per-atom f', f'')
  *   dsf_structure_set_lcs       the localCoordinateSystems argument
  *                               (include/discamb/Scattering/HansenCoppensStructureFactorCalculator.h:148-165)
  *   dsf_calculate               calculateStructureFactorsAndDerivatives(atoms, [lcs,] hkl, f,
@@ -203,6 +204,10 @@ int dsf_structure_update_atoms(dsf_structure *s, const double *xyz, const double
 int dsf_structure_update_types(dsf_structure *s, const double *type_plm, const double *type_pval,
                                const double *type_kappa, const double *type_kappa_prime);
 int dsf_structure_set_lcs(dsf_structure *s, const double *lcs);
+/* per-atom anomalous dispersion [n_atoms][2] (f', f'') in the caller's atom order, replacing the values given at
+ * creation (SfCalculator::setAnomalous, include/discamb/Scattering/SfCalculator.h:43; the HC calculator's
+ * set_anomalous_dispersion_per_atom, HansenCoppensStructureFactorCalculator.h:49) */
+int dsf_structure_set_anomalous(dsf_structure *s, const double *anomalous);
 /* bytes of device memory the structure holds */
 int64_t dsf_structure_device_bytes(const dsf_structure *s);
 

@@ -446,3 +446,17 @@ def test_iam_operation_counts_match_oracle(engine, sg):
             r = calc.calculate(st.dtdf, precision=prec, derivatives=())
             assert rel_f(r["f"], o["f"]) < TOL[prec][0]
         calc.close()
+
+
+@pytest.mark.parametrize("prec", [FP64, FP32])
+def test_set_anomalous_matches_reference(engine, prec):
+    # per-atom anomalous dispersion set after creation (setAnomalous) gives the reference's result with those values
+    st, d = load_fixture("hc_anomalous_mask")
+    plain = copy.deepcopy(st)
+    plain.anomalous = None  # created with the wavefunctions' values
+    calc = api.HcCalculator(engine, plain)
+    calc.set_anomalous(st.anomalous)
+    inc = st.include.astype(np.int32)
+    r = calc.calculate(st.dtdf, precision=prec, include=inc)
+    check(r, d["ref_f"], d["ref_d_xyz"], ref_adp_list(st, d), d["ref_d_occ"], prec)
+    calc.close()
