@@ -8,7 +8,7 @@
  *   calculateStructureFactorsAndDerivatives(hkl, f, SfDerivativesAtHkl,
  *       countAtomContribution)    (single h)        SfCalculator.h:82-86
  *   calculateFormFactors(hkl, ff, includeAtom)      SfCalculator.h:89
- *   update(atoms), setAnomalous(anomalous), setN_threads(n)
+ *   update(atoms), setAnomalous(anomalous), setN_threads(n), getModelInformation(info), name()
  *
  * The reflection set stays resident on the GPU between calls (it is re-sent
  * only when the caller passes another one), the atoms' parameters travel with
@@ -29,6 +29,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace dsf {
@@ -160,6 +161,13 @@ public:
                        "calculateFormFactors");
     }
 
+    // (key, value) pairs describing the model (SfCalculator::getModelInformation, SfCalculator.h:41)
+    virtual void getModelInformation(std::vector<std::pair<std::string, std::string> > &modelInfo) const
+    {
+        modelInfo.clear();
+    }
+    virtual std::string name() const { return "undefined"; }
+
     int64_t deviceBytes() const { return dsf_structure_device_bytes(s_); }
     dsf_structure *structure() const { return s_; }
 
@@ -244,17 +252,33 @@ public:
     }
     // the point-group split of the deformation valence (EngineSymm) is always applied; nothing to switch
     void set_def_val_symm(bool) {}
+    // AnyHcCalculator::getModelInformation (src/Scattering/AnyHcCalculator.cpp:28-34)
+    void getModelInformation(std::vector<std::pair<std::string, std::string> > &modelInfo) const override
+    {
+        modelInfo.assign(1, {"SCATTERING MODEL", "Hansen-Coppens multipole model"});
+    }
+    std::string name() const override { return "hc_gb300"; }
 };
 
 // AnyIamCalculator (src/Scattering/AnyIamCalculator.cpp:49-154)
 class IamCalculator : public SfCalculator {
 public:
+    // table: the name of the Gaussian parameterisation the caller filled dsf_iam_model from
     IamCalculator(std::shared_ptr<Engine> engine, const dsf_symmetry &sym, const dsf_iam_model &model,
-                  const dsf_atoms &atoms)
-        : SfCalculator(std::move(engine), atoms)
+                  const dsf_atoms &atoms, const std::string &table = std::string())
+        : SfCalculator(std::move(engine), atoms), table_(table)
     {
         engine_->check(dsf_structure_create_iam(engine_->get(), &sym, &model, &atoms, &s_), "create_iam");
     }
+    // AnyIamCalculator's model information (src/Scattering/AnyIamCalculator.cpp:55-56, 147)
+    void getModelInformation(std::vector<std::pair<std::string, std::string> > &modelInfo) const override
+    {
+        modelInfo = {{"SCATTERING MODEL", "IAM"}, {"FORM FACTORS PARAMETERISATION", table_}};
+    }
+    std::string name() const override { return "iam_gb300"; }
+
+private:
+    std::string table_;
 };
 
 // TscFileBasedSfCalculator (src/Scattering/TscFileBasedSfCalculator.cpp:17-123): the reflection set of the
@@ -271,6 +295,8 @@ public:
         hkl_ = hkl;
         have_hkl_ = true;
     }
+    // TscFileBasedSfCalculator reports no model information (TscFileBasedSfCalculator.h:27)
+    std::string name() const override { return "tsc_gb300"; }
 };
 
 }  // namespace dsf

@@ -3,6 +3,8 @@
 // tests/test_cpp_host.py through one extern "C" entry.
 #include "dsf_calculator.hpp"
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -19,7 +21,7 @@ const char *drv_error() { return g_err.c_str(); }
 // atoms: xyz [n][3], adp [n][6] (first nadp used), occ [n]; hkl [m][3], dtdf [m][2]; include [n] (0/1)
 // outputs: f [m][2] and the derivatives [n][3], [n][6], [n] of the whole-set call; f_only [m][2] of
 // calculateStructureFactors; f1 [2], d1_xyz [n][3][2], d1_adp [n][6][2], d1_occ [n][2] of the single-h call at
-// hkl[0]; ff [n][2] of calculateFormFactors at hkl[1]
+// hkl[0]; ff [n][2] of calculateFormFactors at hkl[1]; checks setAnomalous and getModelInformation itself
 int drv_hc(int device, const dsf_symmetry *sym, const dsf_hc_model *model, const dsf_atoms *atoms, int precision,
            const double *xyz, const double *adp, const double *occ, int m, const int *hkl, const double *dtdf,
            const int *include, double *f, double *d_xyz, double *d_adp, double *d_occ, double *f_only, double *f1,
@@ -83,6 +85,23 @@ int drv_hc(int device, const dsf_symmetry *sym, const dsf_hc_model *model, const
         calc.calculateStructureFactors(at, h, f3, count);
         for (int i = 0; i < m; i++)
             if (std::abs(f3[i] - f2[i]) > 1e-9 * (1.0 + std::abs(f2[i]))) throw dsf::Error("set not restored");
+        // setAnomalous: zero f', f'' changes F, the creation values bring it back
+        if (atoms->anomalous) {
+            calc.setAnomalous(std::vector<dsf::cplx>(n, dsf::cplx(0.0, 0.0)));
+            calc.calculateStructureFactors(at, h, f3, count);
+            double diff = 0.0;
+            for (int i = 0; i < m; i++) diff = std::max(diff, std::abs(f3[i] - f2[i]));
+            if (diff == 0.0) throw dsf::Error("setAnomalous had no effect");
+            std::vector<dsf::cplx> an(n);
+            for (int a = 0; a < n; a++) an[a] = dsf::cplx(atoms->anomalous[2 * a], atoms->anomalous[2 * a + 1]);
+            calc.setAnomalous(an);
+            calc.calculateStructureFactors(at, h, f3, count);
+            for (int i = 0; i < m; i++)
+                if (std::abs(f3[i] - f2[i]) > 1e-9 * (1.0 + std::abs(f2[i]))) throw dsf::Error("setAnomalous not restored");
+        }
+        std::vector<std::pair<std::string, std::string> > info;
+        calc.getModelInformation(info);
+        if (info.size() != 1 || info[0].second != "Hansen-Coppens multipole model") throw dsf::Error("model information");
         // an error of the reference's kind: mismatched dT/dF size
         try {
             std::vector<dsf::cplx> bad(m + 1);

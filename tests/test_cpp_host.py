@@ -1,6 +1,6 @@
 """The C++ host layer (include/dsf_calculator.hpp): the reference's
 SfCalculator calls (whole set, structure factors only, single h, form factors,
-error on a size mismatch) on a reference fixture, through a small C++ driver
+setAnomalous, getModelInformation, error on a size mismatch) on a reference fixture, through a small C++ driver
 (tests/cpp/calculator_driver.cpp) built with g++ against the engine library."""
 import ctypes as C
 import os
