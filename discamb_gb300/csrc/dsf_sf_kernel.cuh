@@ -285,7 +285,7 @@ struct PhaseOps<double> {
 // re-anchored at every line start, at every sub-tile start and, in the FP32
 // form, every kAnchorF32 reflections so the FP32 rounding of the step cannot
 // build up.
-constexpr int kAnchorF32 = 4;
+constexpr int kAnchorF32 = 8;
 
 // GRAD = false: structure factors only (the reference's calculateStructureFactors, which runs its engine with
 // every derivative switched off, HansenCoppensStructureFactorCalculator.cpp:305-326): the derivative sums are
@@ -307,8 +307,13 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     // quadratic form is q_s = q_diag + signed cross terms, and the position and
     // ADP adjoints need six signed sums of u per coset instead of h' and m6 per
     // operation (ADIAG).
+    // The position adjoint in the coset form (XDIAG): the fractional h' of operation s is
+    // the coset's first h' with signs, so the x, y, z adjoint sums are the first h' times
+    // three signed sums of u per coset.
     constexpr bool DIAG = CS > 0 && MODEL == MODEL_HC;
     constexpr bool ADIAG = CS > 0 && ANISO;
+    constexpr bool XDIAG = CS > 0;
+    constexpr int NSG = ADIAG ? 6 : (XDIAG ? 3 : 1);  // signed sums of u per coset
     static_assert(CS == 0 || (NSC > 0 && NSC <= 8 && NSC % CS == 0), "coset form: compiled count <= 8");
     static_assert(GRAD || !MP, "the multipole adjoint needs the derivative pass");
     static_assert(!INV || (MODEL != MODEL_HC && NSC > 0 && NSC % 2 == 0), "inversion pairs: generic models, even count");
@@ -544,8 +549,19 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     R fsre = anre, fsim = anim, r0 = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0;
                     const R *rad = sTr + (size_t)(lt * ht + hl) * 8;
                     if constexpr (!TABLE) {
-                        fsre += rad[0];
-                        r0 = rad[1]; r1 = rad[2]; r2 = rad[3]; r3 = rad[4]; r4 = rad[5];
+                        // rows of 8 values, 32-byte aligned (16-byte stage offsets, 16-byte record sizes)
+                        if constexpr (F32) {
+                            const float4 ra = reinterpret_cast<const float4 *>(rad)[0];
+                            const float2 rb = reinterpret_cast<const float2 *>(rad)[2];
+                            fsre += ra.x;
+                            r0 = ra.y; r1 = ra.z; r2 = ra.w; r3 = rb.x; r4 = rb.y;
+                        } else {
+                            const double2 ra = reinterpret_cast<const double2 *>(rad)[0];
+                            const double2 rb = reinterpret_cast<const double2 *>(rad)[1];
+                            const double2 rc = reinterpret_cast<const double2 *>(rad)[2];
+                            fsre += ra.x;
+                            r0 = ra.y; r1 = rb.x; r2 = rb.y; r3 = rc.x; r4 = rc.y;
+                        }
                     }
                     R Tiso = R(1);
                     if (!ANISO && has_adp) Tiso = texp<R>(-adp[0] * sH2[hl]);
@@ -557,28 +573,35 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     for (int q = 0; q < (ANISO ? 6 : 1); q++) { Are[q] = R(0); Aim[q] = R(0); }
                     R Ere = 0, Eim = 0, Kre = 0, Kim = 0;
                     const RsRec<R> *recs = sRs + (size_t)hl * nS;
-                    // ADIAG: the coset's first h', its m6, the split quadratic form, and the signed
-                    // sums of u: x y z (classes 1 2 4) and xy xz yz (classes 3 5 6), and plain U
+                    // XDIAG: the coset's first h' and the signed sums of u: x y z (classes 1 2 4);
+                    // ADIAG adds its m6, the split quadratic form, the signed sums xy xz yz
+                    // (classes 3 5 6) and plain U
                     R hr[3] = {0, 0, 0}, m6r[ADIAG ? 6 : 1], qd = 0, qc[3] = {0, 0, 0};
-                    R Sre[ADIAG ? 6 : 1], Sim[ADIAG ? 6 : 1], Ucre = 0, Ucim = 0;
+                    R Sre[NSG], Sim[NSG], Ucre = 0, Ucim = 0;
 #pragma unroll
-                    for (int q = 0; q < (ADIAG ? 6 : 1); q++) { m6r[q] = R(0); Sre[q] = R(0); Sim[q] = R(0); }
+                    for (int q = 0; q < (ADIAG ? 6 : 1); q++) m6r[q] = R(0);
+#pragma unroll
+                    for (int q = 0; q < NSG; q++) { Sre[q] = R(0); Sim[q] = R(0); }
                     auto adp_coset_begin = [&](const RsRec<R> &rec) {
-                        if constexpr (ADIAG) {
+                        if constexpr (XDIAG) {
                             hr[0] = rec.hf[0]; hr[1] = rec.hf[1]; hr[2] = rec.hf[2];
+#pragma unroll
+                            for (int q = 0; q < NSG; q++) { Sre[q] = R(0); Sim[q] = R(0); }
+                        }
+                        if constexpr (ADIAG) {
                             m6r[0] = hr[0] * hr[0]; m6r[1] = hr[1] * hr[1]; m6r[2] = hr[2] * hr[2];
                             m6r[3] = R(2) * hr[0] * hr[1]; m6r[4] = R(2) * hr[0] * hr[2]; m6r[5] = R(2) * hr[1] * hr[2];
                             qd = adp[0] * m6r[0] + adp[1] * m6r[1] + adp[2] * m6r[2];
                             qc[0] = adp[3] * m6r[3]; qc[1] = adp[4] * m6r[4]; qc[2] = adp[5] * m6r[5];
-#pragma unroll
-                            for (int q = 0; q < 6; q++) { Sre[q] = R(0); Sim[q] = R(0); }
                             Ucre = R(0); Ucim = R(0);
                         }
                     };
                     auto adp_coset_end = [&]() {
-                        if constexpr (ADIAG) {
+                        if constexpr (XDIAG) {
 #pragma unroll
                             for (int c = 0; c < 3; c++) { Xre[c] += hr[c] * Sre[c]; Xim[c] += hr[c] * Sim[c]; }
+                        }
+                        if constexpr (ADIAG) {
 #pragma unroll
                             for (int q = 0; q < 3; q++) { Are[q] -= m6r[q] * Ucre; Aim[q] -= m6r[q] * Ucim; }
 #pragma unroll
@@ -779,15 +802,20 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         const R ure = fre * zre - fim * zim;
                         const R uim = fre * zim + fim * zre;
                         Ure += ure; Uim += uim;
-                        if constexpr (ADIAG) {
-                            Ucre += ure; Ucim += uim;
-                            // signed sums: x y z -> slots 0 1 2 (classes 1 2 4), xy xz yz -> 3 4 5 (3 5 6)
-                            Sre[0] += xs(1) * ure; Sim[0] += xs(1) * uim;
-                            Sre[1] += xs(2) * ure; Sim[1] += xs(2) * uim;
-                            Sre[2] += xs(4) * ure; Sim[2] += xs(4) * uim;
-                            Sre[3] += xs(3) * ure; Sim[3] += xs(3) * uim;
-                            Sre[4] += xs(5) * ure; Sim[4] += xs(5) * uim;
-                            Sre[5] += xs(6) * ure; Sim[5] += xs(6) * uim;
+                        if constexpr (XDIAG) {
+                            // signed sums: x y z -> slots 0 1 2 (classes 1 2 4), xy xz yz -> 3 4 5 (3 5 6);
+                            // the coset's first operation has every sign +1 (s is a compile-time index here)
+                            const bool first = s % (CS > 0 ? CS : 1) == 0;
+                            constexpr int cls[6] = {1, 2, 4, 3, 5, 6};
+#pragma unroll
+                            for (int q = 0; q < NSG; q++) {
+                                if (first) {
+                                    Sre[q] = ure; Sim[q] = uim;
+                                } else {
+                                    Sre[q] += xs(cls[q]) * ure; Sim[q] += xs(cls[q]) * uim;
+                                }
+                            }
+                            if constexpr (ADIAG) { Ucre += ure; Ucim += uim; }
                         } else {
                             Xre[0] += h0f * ure; Xim[0] += h0f * uim;
                             Xre[1] += h1f * ure; Xim[1] += h1f * uim;
