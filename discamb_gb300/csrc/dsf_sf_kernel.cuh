@@ -501,11 +501,11 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     uint32_t parity[2] = {0u, 0u};
     int k = 0;
     // per-thread partial derivative sums, folded into the compensated totals
-    // every `fold` sub-tiles (about 16 reflections)
+    // every `fold` sub-tiles (about 32 reflections)
     R part[NT];
 #pragma unroll
     for (int q = 0; q < NT; q++) part[q] = R(0);
-    const int fold = ht >= 16 ? 1 : 16 / ht;
+    const int fold = ht >= 32 ? 1 : 32 / ht;
     for (int h0 = h_begin; h0 < h_end; h0 += ht, k++) {
         const int buf = k & 1;
         if (tid == 0 && h0 + ht < h_end) issue(buf ^ 1, h0 + ht);
@@ -801,7 +801,11 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         }
                         const R ure = fre * zre - fim * zim;
                         const R uim = fre * zim + fim * zre;
-                        Ure += ure; Uim += uim;
+                        if (NSC > 0 && s == 0) {  // compile-time with a compiled operation count
+                            Ure = ure; Uim = uim;
+                        } else {
+                            Ure += ure; Uim += uim;
+                        }
                         if constexpr (XDIAG) {
                             // signed sums: x y z -> slots 0 1 2 (classes 1 2 4), xy xz yz -> 3 4 5 (3 5 6);
                             // the coset's first operation has every sign +1 (s is a compile-time index here)
@@ -945,10 +949,12 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                 dst[idx & 1] = v1;
             }
         }
-        // fold the partial sums into the Kahan totals (each thread its own column)
+        // fold the partial sums into the Kahan totals (each thread its own column;
+        // isotropic tiles use one ADP channel of six)
         if (GRAD && ((k + 1) % fold == 0 || h0 + ht >= h_end)) {
 #pragma unroll
             for (int q = 0; q < NT; q++) {
+                if (!ANISO && q > CH_ADP && q < CH_OCC) continue;
                 R sum = sTot[q * kTileAtoms + tid], comp = sCmp[q * kTileAtoms + tid];
                 const R yv = part[q] - comp;
                 const R tv = sum + yv;
