@@ -884,37 +884,33 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 #pragma unroll 1
                         for (int s = 0; s < nS; s++) term(s);
                     }
-                    if (!ANISO && has_adp) {
-                        Ure *= Tiso; Uim *= Tiso;
-#pragma unroll
-                        for (int q = 0; q < 3; q++) { Xre[q] *= Tiso; Xim[q] *= Tiso; }
-                        if constexpr (MP && !DIAG) { Ere *= Tiso; Eim *= Tiso; Kre *= Tiso; Kim *= Tiso; }
-                    }
+                    // the isotropic factor rides in the weights: w T for F, g T (gre, gim) for the adjoint
+                    const R wT = w * Tiso;
                     if constexpr (ROLL_J) {
-                        const R fv0 = w * Ure, fv1 = w * Uim;
+                        const R fv0 = wT * Ure, fv1 = wT * Uim;
 #pragma unroll
                         for (int q = 0; q < 4; q++)
                             if (q == j) { Fv[2 * q] = fv0; Fv[2 * q + 1] = fv1; }
                     } else {
-                        Fv[2 * j] = w * Ure;
-                        Fv[2 * j + 1] = w * Uim;
+                        Fv[2 * j] = wT * Ure;
+                        Fv[2 * j + 1] = wT * Uim;
                     }
-                    const R gU = g.x * Ure - g.y * Uim;  // Re(g U)
+                    const R gU = gre * Ure - gim * Uim;  // Re(g T U)
                     part[CH_OCC] += gU;
                     if constexpr (ANISO) {
 #pragma unroll
-                        for (int q = 0; q < 6; q++) part[CH_ADP + q] += g.x * Are[q] - g.y * Aim[q];
+                        for (int q = 0; q < 6; q++) part[CH_ADP + q] += gre * Are[q] - gim * Aim[q];
                     } else {
                         part[CH_ADP] -= sH2[hl] * gU;
                     }
 #pragma unroll
-                    for (int q = 0; q < 3; q++) part[CH_XYZ + q] -= g.x * Xim[q] + g.y * Xre[q];  // -Im(g X)
+                    for (int q = 0; q < 3; q++) part[CH_XYZ + q] -= gre * Xim[q] + gim * Xre[q];  // -Im(g T X)
                     if constexpr (MP && !DIAG) {
                         const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
-                        const R gE = g.x * Ere - g.y * Eim;
+                        const R gE = gre * Ere - gim * Eim;
                         part[CH_PV] += dr[0] * gE;
                         part[CH_KAPPA] += dr[1] * gE;
-                        part[CH_KAPPA_P] += g.x * Kre - g.y * Kim;
+                        part[CH_KAPPA_P] += gre * Kre - gim * Kim;
                     }
                 }
             };
