@@ -216,7 +216,7 @@ class Engine:
                 inc = np.ascontiguousarray(includes[i], dtype=np.int32)
                 keep.append(inc)
                 ip[i] = inc.ctypes.data
-            r = c._out_arrays(multipoles)
+            r = c._out_arrays(multipoles, flags)
             res.append(r)
             c._fill_out(outs[i], r, multipoles)
         self.check(self.lib.dsf_calculate_batch_atoms(hs, n, int(precision), flags, xp, ap, op, gp,
@@ -427,11 +427,16 @@ class _Calculator:
         ff = out[..., 0] + 1j * out[..., 1]
         return ff[0] if single else ff
 
-    def _out_arrays(self, multipoles):
+    def _out_arrays(self, multipoles, flags=DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC):
+        """Output arrays of one call: the engine writes F and every requested
+        derivative in full (left uninitialised here); the others stay zero."""
         n, m = self.n_atoms, self.n_hkl
-        r = dict(f=np.zeros(2 * m), d_xyz=np.zeros(3 * n), d_adp=np.zeros(6 * n), d_occ=np.zeros(n))
+        new = lambda k, bit: np.empty(k) if flags & bit else np.zeros(k)
+        r = dict(f=np.empty(2 * m), d_xyz=new(3 * n, DSF_D_XYZ), d_adp=new(6 * n, DSF_D_ADP),
+                 d_occ=new(n, DSF_D_OCC))
         if multipoles:
-            r.update(d_pval=np.zeros(n), d_plm=np.zeros(25 * n), d_kappa=np.zeros(n), d_kappa_prime=np.zeros(n))
+            mp = DSF_D_MULTIPOLE if isinstance(self, HcCalculator) else 0
+            r.update(d_pval=new(n, mp), d_plm=new(25 * n, mp), d_kappa=new(n, mp), d_kappa_prime=new(n, mp))
         return r
 
     @staticmethod
@@ -466,7 +471,7 @@ class _Calculator:
         each atom's component count."""
         flags = _flags(derivatives, multipoles)
         g = np.ascontiguousarray(dtdf, dtype=np.complex128).view(np.float64)
-        r = self._out_arrays(multipoles)
+        r = self._out_arrays(multipoles, flags)
         o = _Out()
         self._fill_out(o, r, multipoles)
         inc = None
@@ -488,7 +493,7 @@ class _Calculator:
         (None while it is pending).  One pending call per calculator."""
         flags = _flags(derivatives, multipoles)
         g = np.ascontiguousarray(dtdf, dtype=np.complex128).view(np.float64)
-        r = self._out_arrays(multipoles)
+        r = self._out_arrays(multipoles, flags)
         o = _Out()
         self._fill_out(o, r, multipoles)
         inc, keep = None, [g]

@@ -1173,6 +1173,11 @@ cudaError_t launch_grad_epilogue(int n_atoms, int xyz_conv, const double *Minv, 
 // ==========================================================================
 // C ABI
 // ==========================================================================
+// host-buffer batches of at least kPipelineBytes of inputs and outputs run as up to
+// kPipelineGroups groups, so the host copies of one group overlap the GPU work of another
+constexpr size_t kPipelineBytes = 64u << 20;
+constexpr int kPipelineGroups = 4;
+
 // host-side work of many structures on several threads when the bytes are worth it (batches of large
 // reflection sets: the staging and copy-out memcpys dominate the host time); f(i) must only touch structure i.
 // At most half the host's cores, and only above 32 MB, so a serving loop's other threads (structure set-up)
@@ -2382,20 +2387,21 @@ static int host_status(dsf_structure *s, const HostCall &hc)
     return DSF_OK;
 }
 
-// copy-out of the pinned results (no CUDA calls, thread-safe per structure)
+// copy-out of the pinned results (no CUDA calls, thread-safe per structure);
+// derivative outputs that the flags do not ask for are left as the caller had them
 static void host_copy_out(const dsf_structure *s, int flags, const HostCall &hc, const dsf_outputs *out)
 {
     const int n = s->n_atoms;
-    const bool mp = (flags & DSF_D_MULTIPOLE) != 0;
+    const int mp = s->model == MODEL_HC ? DSF_D_MULTIPOLE : 0;
     if (hc.nf) std::memcpy(out->f, hc.po, sizeof(double) * hc.nf);
     const double *q = hc.po + hc.nf;
-    struct { double *dst; size_t off, n; } cp[] = {
-        {out->d_xyz, 0, 3 * (size_t)n}, {out->d_adp, 3 * (size_t)n, 6 * (size_t)n},
-        {out->d_occ, 9 * (size_t)n, (size_t)n}, {out->d_pval, 10 * (size_t)n, (size_t)n},
-        {out->d_plm, 11 * (size_t)n, 25 * (size_t)n}, {out->d_kappa, 36 * (size_t)n, (size_t)n},
-        {out->d_kappa_prime, 37 * (size_t)n, (size_t)n}};
+    struct { double *dst; size_t off, n; int flag; } cp[] = {
+        {out->d_xyz, 0, 3 * (size_t)n, DSF_D_XYZ}, {out->d_adp, 3 * (size_t)n, 6 * (size_t)n, DSF_D_ADP},
+        {out->d_occ, 9 * (size_t)n, (size_t)n, DSF_D_OCC}, {out->d_pval, 10 * (size_t)n, (size_t)n, mp},
+        {out->d_plm, 11 * (size_t)n, 25 * (size_t)n, mp}, {out->d_kappa, 36 * (size_t)n, (size_t)n, mp},
+        {out->d_kappa_prime, 37 * (size_t)n, (size_t)n, mp}};
     for (auto &c : cp)
-        if (c.dst && (c.off < 10 * (size_t)n || mp)) std::memcpy(c.dst, q + c.off, sizeof(double) * c.n);
+        if (c.dst && (flags & c.flag)) std::memcpy(c.dst, q + c.off, sizeof(double) * c.n);
 }
 
 static int calculate_host(dsf_structure *s, int precision, int flags, const double *xyz, const double *adp,
@@ -2575,39 +2581,96 @@ int dsf_calculate_batch_atoms(dsf_structure *const *structures, int n, int preci
     std::vector<HostCall> hc(n);
     std::vector<dsf_outputs> d(n);
     std::vector<const double *> g(n);
-    size_t bytes_in = 0, bytes_out = 0;
+    std::vector<size_t> io(n);
+    std::vector<double> work(n);
+    size_t bytes_io = 0;
+    double total = 0;
     for (int i = 0; i < n; i++) {
         if (!structures[i] || structures[i]->eng != e)
             return fail(e, DSF_ERR_ARGUMENT, "batch structures must belong to one engine");
         int rc = host_begin(structures[i], xyz ? xyz[i] : nullptr, occupancy ? occupancy[i] : nullptr, dtdf[i],
                             include ? include[i] : nullptr, &out[i], hc[i]);
         if (rc) return rc;
-        bytes_in += 16 * (size_t)structures[i]->n_hkl + (xyz ? 80 * (size_t)structures[i]->n_atoms : 0);
-        bytes_out += 8 * hc[i].nout;
+        io[i] = 16 * (size_t)structures[i]->n_hkl + (xyz ? 80 * (size_t)structures[i]->n_atoms : 0) + 8 * hc[i].nout;
+        bytes_io += io[i];
+        work[i] = (double)structures[i]->n_atoms * structures[i]->n_hkl * structures[i]->n_sym + 1.0;
+        total += work[i];
         d[i] = hc[i].d;
         g[i] = structures[i]->d_dtdf.as<double>();
     }
-    // the CPU copies into the structures' pinned staging, in parallel for large batches
-    std::vector<int> bad(n, 0);
-    host_parallel(n, bytes_in, [&](int i) {
-        bad[i] = host_fill(structures[i], xyz ? xyz[i] : nullptr, adp ? adp[i] : nullptr,
-                           occupancy ? occupancy[i] : nullptr, dtdf[i], hc[i]);
-    });
-    for (int i = 0; i < n; i++)
-        if (bad[i]) return fail(e, DSF_ERR_ARGUMENT, "non-finite coordinate");
-    for (int i = 0; i < n; i++) {
-        int rc = host_send(structures[i], xyz != nullptr && xyz[i] != nullptr, hc[i]);
-        if (rc) return rc;
+    // Large batches run as groups of consecutive structures of about equal work:
+    // while the GPU computes one group, the CPU copies the next group's inputs into
+    // pinned staging and the previous group's results out of it.
+    const int n_groups = (bytes_io >= kPipelineBytes && n >= 8) ? std::min(kPipelineGroups, n / 4) : 1;
+    std::vector<int> gb(n_groups + 1, n);
+    gb[0] = 0;
+    {
+        double acc = 0;
+        int k = 1;
+        for (int i = 0; i < n && k < n_groups; i++) {
+            acc += work[i];
+            if (acc >= total * k / n_groups) gb[k++] = i + 1;
+        }
     }
-    int rc = dsf_calculate_batch_device(structures, n, precision, flags, g.data(), d.data(), e->stream);
-    if (rc) return rc;
-    for (int i = 0; i < n; i++)
-        if ((rc = host_readback(structures[i], flags, hc[i]))) return rc;
-    DSF_CUDA(cudaStreamSynchronize(e->stream));
-    for (int i = 0; i < n; i++)
-        if ((rc = host_status(structures[i], hc[i]))) return rc;
-    host_parallel(n, bytes_out, [&](int i) { host_copy_out(structures[i], flags, hc[i], &out[i]); });
-    return DSF_OK;
+    struct Events {  // one completion event per group, destroyed on every return path
+        std::vector<cudaEvent_t> ev;
+        ~Events()
+        {
+            for (cudaEvent_t x : ev)
+                if (x) cudaEventDestroy(x);
+        }
+    } evs;
+    evs.ev.assign(n_groups, nullptr);
+    cudaSetDevice(e->device);
+    auto group_bytes = [&](int k) {
+        size_t b = 0;
+        for (int i = gb[k]; i < gb[k + 1]; i++) b += io[i];
+        return b;
+    };
+    // inputs in, the group's calculation and its read-back enqueued, the event recorded
+    auto stage = [&](int k) -> int {
+        const int i0 = gb[k], m = gb[k + 1] - gb[k];
+        std::vector<int> bad(m, 0);
+        host_parallel(m, group_bytes(k), [&](int j) {
+            const int i = i0 + j;
+            bad[j] = host_fill(structures[i], xyz ? xyz[i] : nullptr, adp ? adp[i] : nullptr,
+                               occupancy ? occupancy[i] : nullptr, dtdf[i], hc[i]);
+        });
+        for (int j = 0; j < m; j++)
+            if (bad[j]) return fail(e, DSF_ERR_ARGUMENT, "non-finite coordinate");
+        int rc;
+        for (int i = i0; i < i0 + m; i++)
+            if ((rc = host_send(structures[i], xyz != nullptr && xyz[i] != nullptr, hc[i]))) return rc;
+        if ((rc = dsf_calculate_batch_device(structures + i0, m, precision, flags, g.data() + i0, d.data() + i0,
+                                             e->stream)))
+            return rc;
+        for (int i = i0; i < i0 + m; i++)
+            if ((rc = host_readback(structures[i], flags, hc[i]))) return rc;
+        DSF_CUDA(cudaEventCreateWithFlags(&evs.ev[k], cudaEventDisableTiming));
+        DSF_CUDA(cudaEventRecord(evs.ev[k], e->stream));
+        return DSF_OK;
+    };
+    // the group's results out of pinned staging, after its event
+    auto finish = [&](int k) -> int {
+        DSF_CUDA(cudaEventSynchronize(evs.ev[k]));
+        int rc;
+        for (int i = gb[k]; i < gb[k + 1]; i++)
+            if ((rc = host_status(structures[i], hc[i]))) return rc;
+        const int i0 = gb[k];
+        host_parallel(gb[k + 1] - i0, group_bytes(k),
+                      [&](int j) { host_copy_out(structures[i0 + j], flags, hc[i0 + j], &out[i0 + j]); });
+        return DSF_OK;
+    };
+    int rc = DSF_OK, prev = -1;
+    for (int k = 0; k < n_groups && !rc; k++) {
+        if (gb[k] == gb[k + 1]) continue;
+        rc = stage(k);
+        if (!rc && prev >= 0) rc = finish(prev);
+        prev = k;
+    }
+    if (!rc && prev >= 0) rc = finish(prev);
+    if (rc) cudaStreamSynchronize(e->stream);  // no copy of a failed call still in flight
+    return rc;
 }
 
 int dsf_calculate(dsf_structure *s, int precision, int flags, const double *dtdf, const int *include,

@@ -154,6 +154,8 @@ typedef struct {
     int adp_convention;
 } dsf_atoms;
 
+/* outputs of one call: f always written; each derivative output written only when derivative_flags asks for it
+ * (the others keep what the caller had there) */
 typedef struct {
     double *f;            /* [n_hkl][2] */
     double *d_xyz;        /* [n_atoms][3] or NULL */
@@ -259,8 +261,10 @@ int dsf_submit(dsf_structure *s, int precision, int derivative_flags, const doub
 /* waits up to timeout_ms (0: test only) for a submitted call: DSF_OK with the outputs written (the ticket is
  * released), DSF_PENDING (the ticket stays valid: poll again), or the call's error (the ticket is released) */
 int dsf_poll(dsf_ticket *ticket, int timeout_ms);
-/* the same with host buffers (dtdf[i] [n_hkl_i][2], include[i] NULL = all atoms, outputs on the host); one
- * stream synchronisation for the whole batch */
+/* the same with host buffers (dtdf[i] [n_hkl_i][2], include[i] NULL = all atoms, outputs on the host).  A batch
+ * of 8 or more structures with at least 64 MB of inputs and outputs runs as up to four groups of consecutive
+ * structures, so that the host copies of one group overlap the GPU work of another; smaller ones take one stream
+ * synchronisation */
 int dsf_calculate_batch(dsf_structure *const *structures, int n, int precision, int derivative_flags,
                         const double *const *dtdf, const int *const *include, const dsf_outputs *out);
 /* the same with every structure's atomic parameters of this call (xyz[i] NULL: the resident ones), as

@@ -114,6 +114,29 @@ def test_batch_larger_than_one_launch(engine):
         c.close()
 
 
+def test_large_host_batch_in_overlapped_groups(engine):
+    # 20 structures of about 130k reflections: more than 64 MB of host inputs and outputs, so the call runs in
+    # groups whose host copies overlap the GPU work of the others; the results equal one call each (FP32: at
+    # the FP32 bar, since batch and single call re-anchor the line recurrence at different reflections)
+    sts = [W.small_case("P21/c", n_atoms=4, stol_max=2.2, seed=500 + i, aniso=bool(i % 2)) for i in range(20)]
+    assert sum(32 * st.n_hkl + 8 * 38 * st.n_atoms for st in sts) >= 64 << 20
+    calcs = [api.HcCalculator(engine, st) for st in sts]
+    for prec, tol_f, tol_d in ((FP64, 1e-12, 1e-12), (FP32, 1e-6, 1e-5)):
+        batch = engine.calculate_batch(calcs, [st.dtdf for st in sts], precision=prec)
+        for c, st, b in zip(calcs, sts, batch):
+            a = c.calculate(st.dtdf, precision=prec, adp_layout="padded")
+            assert rel_f(b["f"], a["f"]) < tol_f
+            for k in ("d_xyz", "d_adp", "d_occ"):
+                assert rel_norm(b[k], a[k]) < tol_d, k
+    # derivative outputs the flags leave out are not written
+    batch = engine.calculate_batch(calcs, [st.dtdf for st in sts], precision=FP32, derivatives=("xyz",))
+    for b in batch:
+        assert np.all(b["d_adp"] == 0) and np.all(b["d_occ"] == 0)
+        assert np.abs(b["d_xyz"]).max() > 0
+    for c in calcs:
+        c.close()
+
+
 def test_batch_rejects_foreign_structures(engine):
     st = W.small_case("P21", n_atoms=3, stol_max=0.3, seed=450)
     other = api.Engine(0)
