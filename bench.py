@@ -635,17 +635,32 @@ def run_gpu(args):
     with ClockSampler(device) as clk:
         ms32, kern32, launches32, wall32 = timed_device(api.DSF_FP32_BULK, args.steps, args.warmup)
     clocks = clk.summary()
-    # the plain FP64 form, on the whole reflection set or on a leading fraction of it
+
+    def snapshot(m):
+        return f[:m].clone(), {k: v.clone() for k, v in g.items()}
+
+    # the plain FP64 form, on the whole reflection set or on a leading fraction of it; the FP32 results of the
+    # same reflections against it (sum|dF|/sum|F|, per-class derivative norm error)
     frac64 = wl["fp64_frac"]
     if frac64 < 1.0:
         m64 = max(16, int(n_hkl * frac64))
         calc.set_hkl(st.hkl[:m64])
-        ms64, kern64, _, _ = timed_device(api.DSF_FP64, 2, 1, dtdf_=dtdf[:m64].contiguous())
+        d64 = dtdf[:m64].contiguous()
+        timed_device(api.DSF_FP32_BULK, 1, 1, dtdf_=d64)
+        r32 = snapshot(m64)
+        ms64, kern64, _, _ = timed_device(api.DSF_FP64, 2, 1, dtdf_=d64)
+        r64 = snapshot(m64)
         calc.set_hkl(st.hkl)
         terms64 = terms * m64 / n_hkl
     else:
+        m64 = n_hkl
+        r32 = snapshot(m64)
         ms64, kern64, _, _ = timed_device(api.DSF_FP64, max(2, min(args.steps, 3)), 1)
+        r64 = snapshot(m64)
         terms64 = terms
+    err32 = {"f": float((r32[0] - r64[0]).norm(dim=1).sum() / r64[0].norm(dim=1).sum())}
+    for k in r64[1]:
+        err32[k] = float((r32[1][k] - r64[1][k]).norm() / r64[1][k].norm())
 
     # end to end through the reference-shaped host call (atoms + dT/dF in, F and
     # derivatives out); the library stages through its own pinned buffer
@@ -691,7 +706,9 @@ def run_gpu(args):
         "fp64": {"value": world * terms64 / (step64 * 1e-3), "ms_per_step": step64,
                  "kernel_ms": statistics.mean(kern64),
                  "fp32_over_fp64": (terms / step32) / (terms64 / step64),
-                 "sample": "all reflections" if frac64 >= 1.0 else f"first {frac64:.0%} of the reflections"},
+                 "sample": "all reflections" if frac64 >= 1.0 else f"first {frac64:.0%} of the reflections",
+                 "fp32_error": {**err32, "measure": "sum|dF|/sum|F|; derivatives per class |dg|/|g|, FP32-bulk "
+                                                   "against this FP64 run on the same reflections"}},
         "e2e": {"value": job_terms / (e2e_ms * 1e-3), "unit": "terms/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
