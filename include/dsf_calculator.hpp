@@ -4,6 +4,7 @@
  *
  *   calculateStructureFactorsAndDerivatives(atoms, hkl, f, dTarget_dparam,
  *       dTarget_df, countAtomContribution)          SfCalculator.h:45-67
+ *   the same without countAtomContribution, and with a DerivativesSelector
  *   calculateStructureFactors(atoms, hkl, f, countAtomContribution)
  *   calculateStructureFactorsAndDerivatives(hkl, f, SfDerivativesAtHkl,
  *       countAtomContribution)    (single h)        SfCalculator.h:82-86
@@ -56,6 +57,14 @@ struct SfDerivativesAtHkl {
     std::vector<cplx> occupancyDerivatives;
 };
 
+// SF_CalcDataTypes.h:22-27; d_anom has no counterpart (the engine takes f', f'' as inputs)
+struct DerivativesSelector {
+    bool d_xyz = true;
+    bool d_adp = true;
+    bool d_occ = true;
+    bool d_anom = true;
+};
+
 class Error : public std::runtime_error {
 public:
     using std::runtime_error::runtime_error;
@@ -100,6 +109,30 @@ public:
     {
         if (dTarget_df.size() != hkl.size()) throw Error("dTarget_df and hkl sizes differ");
         run(atoms, hkl, dTarget_df, countAtomContribution, DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC, f, &dTarget_dparam);
+    }
+
+    // every atom counted (SfCalculator.h:52-57)
+    void calculateStructureFactorsAndDerivatives(const std::vector<AtomInCrystal> &atoms,
+                                                 const std::vector<Vector3i> &hkl, std::vector<cplx> &f,
+                                                 std::vector<TargetFunctionAtomicParamDerivatives> &dTarget_dparam,
+                                                 const std::vector<cplx> &dTarget_df)
+    {
+        calculateStructureFactorsAndDerivatives(atoms, hkl, f, dTarget_dparam, dTarget_df, std::vector<bool>());
+    }
+
+    // only the selected derivative classes are computed; the others come back zero (SfCalculator.h:59-66, whose
+    // default computes them all)
+    void calculateStructureFactorsAndDerivatives(const std::vector<AtomInCrystal> &atoms,
+                                                 const std::vector<Vector3i> &hkl, std::vector<cplx> &f,
+                                                 std::vector<TargetFunctionAtomicParamDerivatives> &dTarget_dparam,
+                                                 const std::vector<cplx> &dTarget_df,
+                                                 const std::vector<bool> &countAtomContribution,
+                                                 const DerivativesSelector &selector)
+    {
+        if (dTarget_df.size() != hkl.size()) throw Error("dTarget_df and hkl sizes differ");
+        const int flags = (selector.d_xyz ? DSF_D_XYZ : 0) | (selector.d_adp ? DSF_D_ADP : 0) |
+                          (selector.d_occ ? DSF_D_OCC : 0);
+        run(atoms, hkl, dTarget_df, countAtomContribution, flags, f, &dTarget_dparam);
     }
 
     void calculateStructureFactors(const std::vector<AtomInCrystal> &atoms, const std::vector<Vector3i> &hkl,

@@ -21,7 +21,7 @@ const char *drv_error() { return g_err.c_str(); }
 // atoms: xyz [n][3], adp [n][6] (first nadp used), occ [n]; hkl [m][3], dtdf [m][2]; include [n] (0/1)
 // outputs: f [m][2] and the derivatives [n][3], [n][6], [n] of the whole-set call; f_only [m][2] of
 // calculateStructureFactors; f1 [2], d1_xyz [n][3][2], d1_adp [n][6][2], d1_occ [n][2] of the single-h call at
-// hkl[0]; ff [n][2] of calculateFormFactors at hkl[1]; checks setAnomalous and getModelInformation itself
+// hkl[0]; ff [n][2] of calculateFormFactors at hkl[1]; checks setAnomalous, the DerivativesSelector overload and getModelInformation itself
 int drv_hc(int device, const dsf_symmetry *sym, const dsf_hc_model *model, const dsf_atoms *atoms, int precision,
            const double *xyz, const double *adp, const double *occ, int m, const int *hkl, const double *dtdf,
            const int *include, double *f, double *d_xyz, double *d_adp, double *d_occ, double *f_only, double *f1,
@@ -98,6 +98,25 @@ int drv_hc(int device, const dsf_symmetry *sym, const dsf_hc_model *model, const
             calc.calculateStructureFactors(at, h, f3, count);
             for (int i = 0; i < m; i++)
                 if (std::abs(f3[i] - f2[i]) > 1e-9 * (1.0 + std::abs(f2[i]))) throw dsf::Error("setAnomalous not restored");
+        }
+        // DerivativesSelector: positions only; F and dF/dxyz as the full call, the other classes zero
+        {
+            dsf::DerivativesSelector sel;
+            sel.d_adp = sel.d_occ = false;
+            std::vector<dsf::cplx> fsel;
+            std::vector<dsf::TargetFunctionAtomicParamDerivatives> dsel;
+            calc.calculateStructureFactorsAndDerivatives(at, h, fsel, dsel, g, count, sel);
+            for (int i = 0; i < m; i++)
+                if (std::abs(fsel[i] - fv[i]) > 1e-9 * (1.0 + std::abs(fv[i]))) throw dsf::Error("selector: F differs");
+            for (int a = 0; a < n; a++) {
+                for (int k = 0; k < 3; k++)
+                    if (std::abs(dsel[a].atomic_position_derivatives[k] - d[a].atomic_position_derivatives[k]) >
+                        1e-9 * (1.0 + std::abs(d[a].atomic_position_derivatives[k])))
+                        throw dsf::Error("selector: dF/dxyz differs");
+                for (double v : dsel[a].adp_derivatives)
+                    if (v != 0.0) throw dsf::Error("selector: unselected ADP derivative not zero");
+                if (dsel[a].occupancy_derivatives != 0.0) throw dsf::Error("selector: unselected occupancy derivative");
+            }
         }
         std::vector<std::pair<std::string, std::string> > info;
         calc.getModelInformation(info);
