@@ -614,11 +614,13 @@ class HcCalculator(_Calculator):
 
 class IamCalculator(_Calculator):
     """IAM with per-type n-Gaussian form factors; all operations modulo
-    centering (the AnyScatterer engine's representation)."""
+    centering (the AnyScatterer engine's representation) by default, or
+    representation="engine": the subset with the inversion and centering
+    taken by the engine (the same F and derivatives)."""
 
-    def __init__(self, engine, st, iam):
+    def __init__(self, engine, st, iam, representation="all"):
         super().__init__(engine, st)
-        sym, k1 = symmetry_desc(st, "all")
+        sym, k1 = symmetry_desc(st, representation)
         m = _Iam()
         m.n_types = len(iam["c"])
         keep = []

@@ -230,6 +230,31 @@ SPACE_GROUPS = {
 }
 
 
+def _with_centering(ops, vectors):
+    """Every operation of ``ops`` combined with every centering translation
+    (fractions as text, e.g. ("2/3", "1/3", "1/3"))."""
+    out = []
+    for v in [("0", "0", "0")] + list(vectors):
+        for op in ops:
+            rows = op.split(",")
+            out.append(",".join(r if t == "0" else f"{r}+{t}" for r, t in zip(rows, v)))
+    return out
+
+
+_R_OBVERSE = [("2/3", "1/3", "1/3"), ("1/3", "2/3", "2/3")]
+_R_REVERSE = [("1/3", "2/3", "1/3"), ("2/3", "1/3", "2/3")]
+_F_VECTORS = [("0", "1/2", "1/2"), ("1/2", "0", "1/2"), ("1/2", "1/2", "0")]
+_P3 = ["x,y,z", "-y,x-y,z", "-x+y,-x,z"]
+_P3_INV = ["-x,-y,-z", "y,-x+y,-z", "x-y,x,-z"]
+SPACE_GROUPS.update({
+    # rhombohedral centering on hexagonal axes, obverse and reverse settings
+    "R-3": _with_centering(_P3 + _P3_INV, _R_OBVERSE),
+    "R3(reverse)": _with_centering(_P3, _R_REVERSE),
+    # face centering with quarter-cell glide translations
+    "Fdd2": _with_centering(["x,y,z", "-x,-y,z", "x+1/4,-y+1/4,z+1/4", "-x+1/4,y+1/4,z+1/4"], _F_VECTORS),
+})
+
+
 def space_group(symbol):
     return SpaceGroup(symbol, SPACE_GROUPS[symbol])
 
@@ -242,8 +267,11 @@ def centering_multipliers(centering, obverse, hkl):
     if c == "P":
         return np.ones(len(hkl))
     if c == "R":
-        s = (-h + k + l) if obverse else (h - k + l)
-        return np.where(np.abs(s) % 3 == 0, 3.0, 0.0)
+        # obverse: -h + k + l = 3n.  Reverse: the reference tests (h - k + l) mod 2
+        # (scattering_utilities.cpp:130), and so does this restatement
+        if obverse:
+            return np.where(np.abs(-h + k + l) % 3 == 0, 3.0, 0.0)
+        return np.where(np.abs(h - k + l) % 2 == 0, 3.0, 0.0)
     if c == "F":
         hm, km, lm = np.abs(h % 2), np.abs(k % 2), np.abs(l % 2)
         return np.where((hm == km) & (hm == lm), 4.0, 0.0)

@@ -689,7 +689,11 @@ double centering_multiplier(char c, int obverse, int h, int k, int l)
 {
     switch (c) {
     case 'P': return 1.0;
-    case 'R': return (std::abs(obverse ? (-h + k + l) : (h - k + l)) % 3 == 0) ? 3.0 : 0.0;
+    // obverse: -h + k + l = 3n; the reverse setting tests (h - k + l) mod 2, as the reference does
+    // (scattering_utilities.cpp:117-134), so that results match it on the same input
+    case 'R':
+        if (obverse) return (std::abs(-h + k + l) % 3 == 0) ? 3.0 : 0.0;
+        return (std::abs(h - k + l) % 2 == 0) ? 3.0 : 0.0;
     case 'F': {
         const int a = std::abs(h % 2), b = std::abs(k % 2), d = std::abs(l % 2);
         return (a == b && a == d) ? 4.0 : 0.0;

@@ -13,10 +13,21 @@
 // dsf_calculate_device on that scratch and allocates nothing.
 //
 // The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress, once per device, with that device current); make
-// that first call before any stream capture.  All calls share the array:
-// calls that overlap on the GPU (different streams, or different host
-// threads) race on it and must be serialised by the caller.
+// (cudaGetSymbolAddress, once per device, with that device current).  Under
+// CUDA's lazy module loading that lookup is also what loads this file's
+// module and places the array on the GPU, so the first call can fail with
+// DSF_ERR_CUDA (out of memory); make it during set-up, before any stream
+// capture.  The address is kept per device ordinal for the life of the
+// process: after cudaDeviceReset of a device this call must not be used on
+// that device again.  All calls share the array: calls that overlap on the
+// GPU (different streams, or different host threads) race on it and must be
+// serialised by the caller.
+//
+// It runs the first-generation kernel of the engine (sf_grad_kernel: the
+// per-block reflection tables in shared memory, no line recurrences, no
+// sign-diagonal cosets), several times slower than dsf_calculate_device.
+// Atoms whose type index lies outside 0..n_types-1 contribute nothing;
+// adp_components other than 1 or 6 mean no temperature factor.
 #include "../../include/dsf_gb300.h"
 #include "dsf_device.cuh"
 #include "dsf_math.cuh"
@@ -234,7 +245,10 @@ struct HklIn {
 __device__ double centering_mult(char c, int obverse, int h, int k, int l)
 {
     switch (c) {
-    case 'R': return (abs(obverse ? (-h + k + l) : (h - k + l)) % 3 == 0) ? 3.0 : 0.0;
+    // reverse setting: (h - k + l) mod 2, as the reference and the allocating path test it
+    case 'R':
+        if (obverse) return (abs(-h + k + l) % 3 == 0) ? 3.0 : 0.0;
+        return (abs(h - k + l) % 2 == 0) ? 3.0 : 0.0;
     case 'F': {
         const int a = abs(h % 2), b = abs(k % 2), d = abs(l % 2);
         return (a == b && a == d) ? 4.0 : 0.0;
@@ -306,6 +320,18 @@ extern "C" int dsf_iam_calculate_noalloc(const dsf_symmetry *sym, const dsf_iam_
     if (n_atoms < 1 || n_hkl < 1) return report(err, err_len, DSF_ERR_ARGUMENT, "need atoms and reflections");
     if (sym->n_symops < 1 || sym->n_symops > kMaxSym)
         return report(err, err_len, DSF_ERR_ARGUMENT, "n_symops must be in 1..48");
+    // the symmetry checks of the allocating path, before anything is launched
+    for (int i = 0; i < 3; i++)
+        if (!(sym->cell[i] > 0)) return report(err, err_len, DSF_ERR_ARGUMENT, "cell lengths must be positive");
+    const char centering = sym->centering ? (char)toupper(sym->centering) : 'P';
+    if (!std::strchr("PABCIFR", centering))
+        return report(err, err_len, DSF_ERR_ARGUMENT, "unsupported lattice centering");
+    if (sym->centrosymmetric)
+        for (int i = 0; i < 3; i++) {
+            const double t = sym->inversion_translation[i] * 24.0;
+            if (std::fabs(t - std::rint(t)) > 1e-6)
+                return report(err, err_len, DSF_ERR_ARGUMENT, "inversion translation must be a multiple of 1/24");
+        }
     if (model->n_types < 1 || model->n_types > DSF_NOALLOC_MAX_TYPES)
         return report(err, err_len, DSF_ERR_ARGUMENT, "IAM types must number 1..32 for the allocation-free call");
     if (precision != DSF_FP64 && precision != DSF_FP32_BULK)
@@ -383,7 +409,7 @@ extern "C" int dsf_iam_calculate_noalloc(const dsf_symmetry *sym, const dsf_iam_
     HklIn hi;
     hi.n_hkl = n_hkl;
     std::copy(B, B + 9, hi.B);
-    hi.centering = sym->centering ? (char)toupper(sym->centering) : 'P';
+    hi.centering = centering;
     hi.obverse = sym->obverse;
     int centro = 0;
     for (int i = 0; i < 3; i++) {

@@ -96,6 +96,9 @@ def random_cell(rng, kind):
     if kind == "triclinic":
         a, b, c = rng.uniform(6, 12, 3)
         return (a, b, c, rng.uniform(80, 100), rng.uniform(95, 110), rng.uniform(80, 100))
+    if kind == "hexagonal":
+        a, c = rng.uniform(8, 15, 2)
+        return (a, a, c, 90.0, 90.0, 120.0)
     a, b, c = rng.uniform(8, 15, 3)
     return (a, b, c, 90.0, 90.0, 90.0)
 
@@ -229,7 +232,8 @@ def small_case(sg_symbol="P21/c", n_atoms=6, stol_max=0.5, seed=7, cell_kind=Non
     if cell_kind is None:
         cell_kind = {"P1": "triclinic", "P-1": "triclinic", "P-1(shift)": "triclinic",
                      "P21": "monoclinic", "P21/c": "monoclinic", "C2/c": "monoclinic",
-                     "I2/m-like": "monoclinic"}.get(sg_symbol, "orthorhombic")
+                     "I2/m-like": "monoclinic", "R-3": "hexagonal",
+                     "R3(reverse)": "hexagonal"}.get(sg_symbol, "orthorhombic")
     cell = random_cell(rng, cell_kind)
     if sg_symbol in ("P43212", "P41"):
         a = cell[0]

@@ -104,7 +104,8 @@ typedef struct {
     int centrosymmetric;
     double inversion_translation[3];
     char centering;                   /* P A B C I F R */
-    int obverse;
+    int obverse;                      /* R only: 1 obverse (-h+k+l = 3n); 0 reverse, tested as the reference
+                                       * tests it, (h-k+l) even (scattering_utilities.cpp:117-134) */
     int n_symops_total;               /* full operation count; weight = multiplicity / n_symops_total */
 } dsf_symmetry;
 
@@ -291,11 +292,22 @@ double dsf_last_kernel_ms(dsf_structure *s);
  * bytes per reflection (e.g. 20,000 atoms with 200,000 reflections).  Larger
  * problems are rejected with DSF_ERR_ARGUMENT and a message in err.  No
  * cudaMalloc, cudaFree or other allocating call is made.
- * The first call on a device does a one-time set-up (it looks up the device
- * address of the array); make that first call before any stream capture.
+ * The first call on a device does a one-time set-up: it looks up the device
+ * address of the array.  Under CUDA's lazy module loading (the default) that
+ * lookup is also what loads the module and places the 32 MiB array on the
+ * GPU, so the first call can fail with DSF_ERR_CUDA (out of memory); make it
+ * during set-up, before any stream capture.  The address is kept per device
+ * for the life of the process: after cudaDeviceReset of a device, do not call
+ * this entry point on that device again.
  * All calls share the array, which keeps the last call's contents: calls
  * that overlap on the GPU (other streams, other host threads) race on it and
  * must be serialised by the caller.
+ * The symmetry is checked as dsf_structure_create_* checks it (positive cell
+ * lengths, centering one of P A B C I F R, translations in multiples of
+ * 1/24).  Atoms whose atom_type is outside 0..n_types-1 contribute nothing;
+ * adp_components other than 1 or 6 mean no temperature factor.  It runs the
+ * engine's first-generation kernel, several times slower than
+ * dsf_calculate_device.
  * Device inputs: atom_type [n], adp_components [n] (0/1/6), xyz [n][3]
  * fractional, adp [n][6] U_cif (Uiso in [0]), occupancy [n], multiplicity
  * [n], anomalous [n][2] or NULL, hkl [n_hkl][3], dtdf [n_hkl][2]; device

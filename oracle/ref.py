@@ -16,7 +16,22 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _REPO = os.path.dirname(_HERE)
 LIB_PATH = os.path.join(_HERE, "_ref", "libref_driver.so")
-REF_TREE = os.environ.get("DSF_REFERENCE_TREE", "/root/reference")
+
+
+def _recipe_tree():
+    """The reference tree the build recipe names (its ``REF ?=`` line); the
+    environment variable DSF_REFERENCE_TREE overrides it."""
+    try:
+        with open(os.path.join(_HERE, "Makefile.ref")) as fh:
+            for line in fh:
+                if line.startswith("REF ?="):
+                    return line.split("=", 1)[1].strip()
+    except OSError:
+        pass
+    return ""
+
+
+REF_TREE = os.environ.get("DSF_REFERENCE_TREE") or _recipe_tree()
 
 _lib = None
 
@@ -26,8 +41,8 @@ def available():
 
 
 def build(jobs=8):
-    if not os.path.isdir(os.path.join(REF_TREE, "src", "Scattering")):
-        raise RuntimeError("reference tree not present")
+    if not REF_TREE or not os.path.isdir(os.path.join(REF_TREE, "src", "Scattering")):
+        raise RuntimeError("reference tree not present (set DSF_REFERENCE_TREE to the reference sources)")
     subprocess.check_call(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={REF_TREE}", f"-j{jobs}"],
                           cwd=_REPO)
     return LIB_PATH
@@ -52,6 +67,24 @@ def _d(a):
 def _i(a):
     a = np.ascontiguousarray(a, dtype=np.int32)
     return a, a.ctypes.data_as(C.c_void_p)
+
+
+_ADP_CONV = {"U_cif": 0, "U_cart": 1, "U_star": 2}
+
+
+class _Conventions:
+    """The structure's xyz and ADP conventions for the reference calls made
+    inside the block (the crystal the driver builds takes them)."""
+
+    def __init__(self, st):
+        self.xyz = 1 if st.xyz_convention == "cartesian" else 0
+        self.adp = _ADP_CONV[st.adp_convention]
+
+    def __enter__(self):
+        lib().ref_set_conventions(self.xyz, self.adp)
+
+    def __exit__(self, *a):
+        lib().ref_set_conventions(0, 0)
 
 
 def _common(st):
@@ -105,16 +138,17 @@ def hc(st, n_threads=1):
     atom_anom = None
     if st.anomalous is not None:
         atom_anom = D(np.stack([np.real(st.anomalous), np.imag(st.anomalous)], axis=1).reshape(-1))
-    rc = lib().ref_hc_sf(
-        D(cell), C.c_char_p(ops), C.c_int(n), D(st.xyz.reshape(-1)), I(st.n_adp()), D(adp.reshape(-1)),
-        D(st.occupancy), I(st.multiplicity), I(st.atom_wfn), I(st.atom_type), D(np.asarray(st.lcs).reshape(-1)),
-        C.c_int(len(st.wfns)), I(orb_off), I(orb_occ), I(orb_core), I(sto_off), I(sto_pow), D(sto_exp),
-        D(sto_coeff), D(def_exp), I(def_npow), I(def_pow), D(anom), I(zs),
-        C.c_int(len(types)), I([t.n_l for t in types]), D(np.array([t.plm for t in types]).reshape(-1)),
-        D([t.p_val for t in types]), D([t.kappa for t in types]), D([t.kappa_prime for t in types]),
-        C.c_int(st.n_hkl), I(st.hkl.reshape(-1)), D(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1)),
-        atom_anom, I(st.include_mask().astype(np.int32)), C.c_int(n_threads),
-        D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]), C.byref(ms))
+    with _Conventions(st):
+        rc = lib().ref_hc_sf(
+            D(cell), C.c_char_p(ops), C.c_int(n), D(st.xyz.reshape(-1)), I(st.n_adp()), D(adp.reshape(-1)),
+            D(st.occupancy), I(st.multiplicity), I(st.atom_wfn), I(st.atom_type), D(np.asarray(st.lcs).reshape(-1)),
+            C.c_int(len(st.wfns)), I(orb_off), I(orb_occ), I(orb_core), I(sto_off), I(sto_pow), D(sto_exp),
+            D(sto_coeff), D(def_exp), I(def_npow), I(def_pow), D(anom), I(zs),
+            C.c_int(len(types)), I([t.n_l for t in types]), D(np.array([t.plm for t in types]).reshape(-1)),
+            D([t.p_val for t in types]), D([t.kappa for t in types]), D([t.kappa_prime for t in types]),
+            C.c_int(st.n_hkl), I(st.hkl.reshape(-1)), D(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1)),
+            atom_anom, I(st.include_mask().astype(np.int32)), C.c_int(n_threads),
+            D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]), C.byref(ms))
     if rc != 0:
         raise RuntimeError("reference HC path raised an exception: " + _err())
     return _pack(out, st, ms.value)
@@ -148,11 +182,12 @@ def iam(st, labels, table="IT92", n_threads=1):
     nadp = st.n_adp(); mult = np.asarray(st.multiplicity, dtype=np.int32); occ = np.ascontiguousarray(st.occupancy)
     hkl = np.ascontiguousarray(st.hkl.reshape(-1), dtype=np.int32)
     g = np.ascontiguousarray(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1))
-    rc = lib().ref_iam_sf(D_out(cell), C.c_char_p(ops), C.c_char_p(";".join(labels).encode()),
-                          C.c_char_p(table.encode()), C.c_int(n), D_out(xyz), D_out(nadp), D_out(adpf),
-                          D_out(occ), D_out(mult), C.c_int(st.n_hkl), D_out(hkl), D_out(g), C.c_int(n_threads),
-                          D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]),
-                          C.byref(ms))
+    with _Conventions(st):
+        rc = lib().ref_iam_sf(D_out(cell), C.c_char_p(ops), C.c_char_p(";".join(labels).encode()),
+                              C.c_char_p(table.encode()), C.c_int(n), D_out(xyz), D_out(nadp), D_out(adpf),
+                              D_out(occ), D_out(mult), C.c_int(st.n_hkl), D_out(hkl), D_out(g), C.c_int(n_threads),
+                              D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]),
+                              C.byref(ms))
     if rc != 0:
         raise RuntimeError("reference IAM path raised an exception: " + _err())
     return _pack(out, st, ms.value)
@@ -190,10 +225,11 @@ def table(st, keys, values):
     g = np.ascontiguousarray(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1))
     k = np.ascontiguousarray(np.asarray(keys, dtype=np.int32).reshape(-1))
     v = np.ascontiguousarray(np.stack([np.real(values), np.imag(values)], -1).reshape(-1))
-    rc = lib().ref_table_sf(D_out(cell), C.c_char_p(ops), C.c_char_p(labels), C.c_int(n), D_out(xyz), D_out(nadp), D_out(adpf),
-                            D_out(occ), D_out(mult), C.c_int(len(keys)), D_out(k), D_out(v), C.c_int(st.n_hkl),
-                            D_out(hkl), D_out(g), D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]),
-                            D_out(out["d_occ"]), C.byref(ms))
+    with _Conventions(st):
+        rc = lib().ref_table_sf(D_out(cell), C.c_char_p(ops), C.c_char_p(labels), C.c_int(n), D_out(xyz), D_out(nadp), D_out(adpf),
+                                D_out(occ), D_out(mult), C.c_int(len(keys)), D_out(k), D_out(v), C.c_int(st.n_hkl),
+                                D_out(hkl), D_out(g), D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]),
+                                D_out(out["d_occ"]), C.byref(ms))
     if rc != 0:
         raise RuntimeError("reference tabulated path raised an exception: " + _err())
     return _pack(out, st, ms.value)
@@ -210,9 +246,10 @@ def tsc(st, path):
     nadp = st.n_adp(); mult = np.asarray(st.multiplicity, dtype=np.int32); occ = np.ascontiguousarray(st.occupancy)
     hkl = np.ascontiguousarray(st.hkl.reshape(-1), dtype=np.int32)
     g = np.ascontiguousarray(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1))
-    rc = lib().ref_tsc_sf(C.c_char_p(os.fsencode(path)), D_out(cell), C.c_char_p(ops), C.c_char_p(labels), C.c_int(n),
-                          D_out(xyz), D_out(nadp), D_out(adpf), D_out(occ), D_out(mult), C.c_int(st.n_hkl), D_out(hkl),
-                          D_out(g), D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]))
+    with _Conventions(st):
+        rc = lib().ref_tsc_sf(C.c_char_p(os.fsencode(path)), D_out(cell), C.c_char_p(ops), C.c_char_p(labels), C.c_int(n),
+                              D_out(xyz), D_out(nadp), D_out(adpf), D_out(occ), D_out(mult), C.c_int(st.n_hkl), D_out(hkl),
+                              D_out(g), D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]))
     if rc != 0:
         raise RuntimeError("reference tsc path raised an exception: " + _err())
     return _pack(out, st, 0.0)

@@ -55,6 +55,13 @@ struct Input {
     const char *atom_types;   // ';' separated element labels (IAM / labels)
 };
 
+// conventions of the crystal the following calls build (the inputs are given in them and the reference returns
+// the derivatives in them, HansenCoppensStructureFactorCalculator.cpp:69-70, 634-664;
+// AnyScattererStructureFactorCalculator.cpp:89-90): xyz fractional (0) or Cartesian (1); ADPs U_cif (0), U_cart (1)
+// or U_star (2)
+int g_xyz_cartesian = 0;
+int g_adp_convention = 0;
+
 Crystal make_crystal(const Input &in)
 {
     Crystal c;
@@ -79,8 +86,11 @@ Crystal make_crystal(const Input &in)
         a.multiplicity = in.mult[i];
         if (i < (int)labels.size()) { a.type = labels[i]; a.label = labels[i] + std::to_string(i + 1); }
     }
-    c.adpConvention = structural_parameters_convention::AdpConvention::U_cif;
-    c.xyzCoordinateSystem = structural_parameters_convention::XyzCoordinateSystem::fractional;
+    c.adpConvention = g_adp_convention == 1 ? structural_parameters_convention::AdpConvention::U_cart
+                      : g_adp_convention == 2 ? structural_parameters_convention::AdpConvention::U_star
+                                              : structural_parameters_convention::AdpConvention::U_cif;
+    c.xyzCoordinateSystem = g_xyz_cartesian ? structural_parameters_convention::XyzCoordinateSystem::cartesian
+                                            : structural_parameters_convention::XyzCoordinateSystem::fractional;
     return c;
 }
 
@@ -100,6 +110,13 @@ void write_out(const vector<complex<double> > &f, const vector<TargetFunctionAto
 extern "C" {
 
 const char *ref_last_error(void) { return g_last_error.c_str(); }
+
+int ref_set_conventions(int xyz_cartesian, int adp_convention)
+{
+    g_xyz_cartesian = xyz_cartesian != 0;
+    g_adp_convention = adp_convention;
+    return 0;
+}
 
 // electron scattering (Mott-Bethe conversion inside the engine) for the following ref_hc_sf calls
 static bool g_electron = false;

@@ -2,7 +2,8 @@
 library's own CPU code (oracle/_ref/libref_driver.so, built from the
 reference sources by oracle/Makefile.ref) on seeded synthetic structures.
 
-    python tests/golden/make_golden.py [hc|def_val_symm|form_factors|rest ...]   (default: all)
+    python tests/golden/make_golden.py [hc|centering|conventions|def_val_symm|form_factors|rest ...]
+                                                                                  (default: all)
 
 Each fixture (.npz) holds every input of the case (structure_to_arrays) and
 the reference outputs: F, d_xyz, d_adp, d_occ in the crystal's conventions.
@@ -250,7 +251,76 @@ def write_form_factors():
     print("wrote ff_iam_c2c", st.n_atoms, st.n_hkl)
 
 
-GROUPS = {"hc": write_hc, "def_val_symm": write_def_val_symm, "form_factors": write_form_factors,
+def _with_absences(st, stol_max, seed):
+    """The structure's reflections replaced by every unique reflection up to
+    stol_max, lattice-centering absences included (the reference multiplies
+    those by 0), with a fresh seeded dT/dF."""
+    from discamb_gb300.crystal import unique_hkl
+    st.hkl = unique_hkl(st.cell, st.sg, stol_max=stol_max, drop_absent=False)
+    rng = np.random.default_rng(seed)
+    st.dtdf = rng.normal(size=st.n_hkl) + 1j * rng.normal(size=st.n_hkl)
+    return st
+
+
+def write_centering():
+    """Rhombohedral (obverse R-3, reverse R3) and face-centred (Fdd2) lattices
+    through the reference's HC engine, absences included: pins
+    centeringSfMultipliers (scattering_utilities.cpp:103-170), whose reverse
+    setting tests (h - k + l) mod 2."""
+    for i, sg in enumerate(["R-3", "R3(reverse)", "Fdd2"]):
+        st = W.small_case(sg, n_atoms=4, stol_max=0.5, seed=900 + i, improper_lcs=True)
+        st = _with_absences(st, 0.5, 950 + i)
+        name = "hc_" + sg.replace("(", "_").replace(")", "")
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **run_hc(name, st))
+        print("wrote", name, st.n_atoms, st.n_hkl)
+
+
+def to_conventions(st, xyz, adp):
+    """st with its positions and ADPs rewritten in the given conventions
+    (xyz "fractional" / "cartesian"; adp "U_cif" / "U_cart" / "U_star";
+    isotropic U unchanged)."""
+    from discamb_gb300.crystal import convert_adp, frac_to_cart_matrix
+    if xyz == "cartesian":
+        st.xyz = (frac_to_cart_matrix(st.cell) @ st.xyz.T).T.copy()
+    st.adp = [list(convert_adp(st.cell, a, "U_cif", adp)) if len(a) == 6 else list(a) for a in st.adp]
+    st.xyz_convention, st.adp_convention = xyz, adp
+    return st
+
+
+def write_conventions():
+    """The crystal's xyz and ADP conventions other than fractional / U_cif:
+    the reference reads the atoms in them and returns the derivatives in them
+    (HansenCoppensStructureFactorCalculator.cpp:69-70, 634-664;
+    StructuralParametersConverter.h:90-112).  HC: Cartesian + U_cart (P2_1/c),
+    fractional + U_star (P-1), Cartesian + U_cif (P2_1 2_1 2_1); IAM (generic
+    engine): Cartesian + U_star (C2/c)."""
+    for i, (sg, xyz, adp) in enumerate([("P21/c", "cartesian", "U_cart"), ("P-1", "fractional", "U_star"),
+                                         ("P212121", "cartesian", "U_cif")]):
+        st = W.small_case(sg, n_atoms=5, stol_max=0.5, seed=1000 + i, improper_lcs=True)
+        st = to_conventions(st, xyz, adp)
+        name = f"hc_conv_{sg.replace('/', '_')}_{xyz[:4]}_{adp}"
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **run_hc(name, st))
+        print("wrote", name, st.n_atoms, st.n_hkl)
+    st = W.small_case("C2/c", n_atoms=6, stol_max=0.55, seed=1010)
+    labels = [w.label for w in st.wfns]
+    ng, ga, gb, gc = [], np.zeros((len(labels), 5)), np.zeros((len(labels), 5)), []
+    for i, lab in enumerate(labels):
+        a, b, c = R.iam_coefficients(lab, "IT92")
+        ng.append(len(a)); ga[i, :len(a)] = a; gb[i, :len(b)] = b; gc.append(c)
+    st.atom_type = st.atom_wfn.copy()
+    st = to_conventions(st, "cartesian", "U_star")
+    r = R.iam(st, [st.wfns[w].label for w in st.atom_wfn], "IT92")
+    out = structure_to_arrays(st)
+    d_adp = np.zeros((st.n_atoms, 6))
+    for i, v in enumerate(r["d_adp"]):
+        d_adp[i, :len(v)] = v
+    out.update(iam_ngauss=np.array(ng), iam_a=ga, iam_b=gb, iam_c=np.array(gc), ref_f=r["f"], ref_d_xyz=r["d_xyz"],
+               ref_d_adp=d_adp, ref_d_occ=r["d_occ"])
+    np.savez_compressed(os.path.join(HERE, "iam_conv_c2c_cart_U_star.npz"), **out)
+    print("wrote iam_conv_c2c_cart_U_star", st.n_atoms, st.n_hkl)
+
+
+GROUPS = {"hc": write_hc, "centering": write_centering, "conventions": write_conventions, "def_val_symm": write_def_val_symm, "form_factors": write_form_factors,
           "rest": write_rest}
 
 

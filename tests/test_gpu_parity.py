@@ -87,8 +87,10 @@ def iam_dict(d):
 
 
 @pytest.mark.parametrize("prec", [FP64, FP32])
-def test_iam_matches_reference(engine, prec):
-    st, d = load_fixture("iam_it92")
+@pytest.mark.parametrize("name", fixture_names("iam_"))
+def test_iam_matches_reference(engine, name, prec):
+    # iam_it92: fractional + U_cif; iam_conv_*: Cartesian positions and U_star ADPs in and out
+    st, d = load_fixture(name)
     calc = api.IamCalculator(engine, st, iam_dict(d))
     r = calc.calculate(st.dtdf, precision=prec)
     check(r, d["ref_f"], d["ref_d_xyz"], ref_adp_list(st, d), d["ref_d_occ"], prec)

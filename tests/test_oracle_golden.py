@@ -33,8 +33,9 @@ def iam_dict(d):
     return dict(ngauss=d["iam_ngauss"], a=d["iam_a"], b=d["iam_b"], c=d["iam_c"])
 
 
-def test_iam_oracle_matches_reference():
-    st, d = load_fixture("iam_it92")
+@pytest.mark.parametrize("name", fixture_names("iam_"))
+def test_iam_oracle_matches_reference(name):
+    st, d = load_fixture(name)
     r = O.compute(st, model="iam", iam=iam_dict(d), n_threads=2)
     assert rel_f(r["f"], d["ref_f"]) < 1e-12
     assert rel_norm(r["d_xyz"], d["ref_d_xyz"]) < 1e-11

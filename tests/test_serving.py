@@ -129,13 +129,19 @@ def test_unknown_structure_is_rejected():
         srv.submit(req("zz", 0))
 
 
+# the same request answered alone and inside a mixed batch: FP64 to rounding (the cross-block sums are FP64
+# atomics in varying order), FP32-bulk within the stated tolerance (1e-6 for F, 1e-5 per derivative class; the
+# batch runs the batched kernel, the call alone the single-structure kernel)
 @pytest.mark.gpu
-def test_request_in_a_mixed_batch_equals_the_call_alone(engine):
+@pytest.mark.parametrize("precision,tf,tg", [(0, 1e-12, 1e-12), (1, 1e-6, 1e-5)])
+def test_request_in_a_mixed_batch_equals_the_call_alone(engine, precision, tf, tg):
     from discamb_gb300 import api, workloads as W
     from conftest import rel_f, rel_norm
-    sts = {sg: W.small_case(sg, n_atoms=6, stol_max=0.5, seed=600 + i)
-           for i, sg in enumerate(["P1", "P-1", "P21", "P21/c", "P212121", "C2/c"])}
-    srv = serve.SfServer(serve.batch_executor(engine, precision=api.DSF_FP64), 1 << 34)
+    # uneven sizes: 6 to 160 atoms, sin(theta)/lambda up to 0.4-0.6
+    sts = {sg: W.small_case(sg, n_atoms=n, stol_max=smax, seed=600 + i)
+           for i, (sg, n, smax) in enumerate([("P1", 6, 0.5), ("P-1", 40, 0.45), ("P21", 160, 0.4),
+                                              ("P21/c", 12, 0.6), ("P212121", 90, 0.45), ("C2/c", 25, 0.5)])}
+    srv = serve.SfServer(serve.batch_executor(engine, precision=precision), 1 << 34)
     for k, st in sts.items():
         srv.add_structure(k, lambda st=st: api.HcCalculator(engine, st),
                           serve.estimate_device_bytes(st.n_atoms, st.n_hkl, len(st.sg.subset_rot), st.n_atoms))
@@ -149,11 +155,11 @@ def test_request_in_a_mixed_batch_equals_the_call_alone(engine):
     assert srv.batch_sizes == [len(sts)]
     for k, st in sts.items():
         c = api.HcCalculator(engine, st)
-        a = c.calculate(st.dtdf, precision=api.DSF_FP64, atoms=cycles[k], adp_layout="padded")
+        a = c.calculate(st.dtdf, precision=precision, atoms=cycles[k], adp_layout="padded")
         c.close()
         r = rs[k].result
         assert rs[k].error is None
-        assert rel_f(r["f"], a["f"]) < 1e-12
+        assert rel_f(r["f"], a["f"]) < tf, (k, rel_f(r["f"], a["f"]))
         for q in ("d_xyz", "d_adp", "d_occ"):
-            assert rel_norm(r[q], a[q]) < 1e-12, q
+            assert rel_norm(r[q], a[q]) < tg, (k, q, rel_norm(r[q], a[q]))
     srv.close()
