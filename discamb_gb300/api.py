@@ -689,7 +689,10 @@ class CombinedCalculator:
     CombinedStructureFactorCalculator.h:14-60; TAAM: multipolar atoms on the
     HC model, the rest IAM, src/Scattering/HcAtomBankStructureFactorCalculator.cpp:482-499).
     Each part is a calculator over its own atoms (no masked-out work); the
-    parts run in one batched submission."""
+    parts run in one batched submission.  As the reference's set()
+    (src/Scattering/CombinedStructureFactorCalculator.cpp:19-52), building it
+    sets every atom's anomalous dispersion to zero; set_anomalous gives the
+    parts new per-atom values."""
 
     def __init__(self, engine, st, parts):
         """parts: [(make, atom_indices)], make(substructure) -> calculator."""
@@ -704,6 +707,16 @@ class CombinedCalculator:
             self.parts.append((make(sub), idx))
         if not np.all(seen == 1):
             raise DsfError("every atom must belong to exactly one part")
+        self.set_anomalous(np.zeros(st.n_atoms, dtype=np.complex128))
+
+    def set_anomalous(self, anomalous):
+        """Per-atom f' + i f'' in the whole structure's atom order, handed to
+        each part for its own atoms (CombinedStructureFactorCalculator::setAnomalous)."""
+        a = np.asarray(anomalous, dtype=np.complex128).reshape(-1)
+        if len(a) != self.st.n_atoms:
+            raise DsfError("anomalous dispersion size differs from the atom count")
+        for c, idx in self.parts:
+            c.set_anomalous(a[idx])
 
     def calculate(self, dtdf, precision=DSF_FP64, derivatives=("xyz", "adp", "occ"), atoms=None):
         calcs = [c for c, _ in self.parts]

@@ -253,3 +253,124 @@ def tsc(st, path):
     if rc != 0:
         raise RuntimeError("reference tsc path raised an exception: " + _err())
     return _pack(out, st, 0.0)
+
+
+def flatten_lcs(defs):
+    """XD-style LCS definitions (dicts: central, point1, point2_from, point2_to
+    (atom lists; empty = the dummy), dummy (3 fractional positions), axis1,
+    axis2 (+-1..3), right) -> (lcs_def [n][7], lcs_atoms, lcs_dummy [n][9])."""
+    d, at, du = [], [], []
+    for q in defs:
+        d.append([q["central"], q["axis1"], q["axis2"], int(q["right"]), len(q["point1"]), len(q["point2_from"]),
+                  len(q["point2_to"])])
+        at += list(q["point1"]) + list(q["point2_from"]) + list(q["point2_to"])
+        du.append(np.asarray(q.get("dummy", np.zeros((3, 3))), dtype=np.float64).reshape(9))
+    return (np.array(d, dtype=np.int32), np.array(at + [0], dtype=np.int32), np.array(du, dtype=np.float64))
+
+
+def anyhc_lcs(st, xyz_moved, defs, n_threads=1):
+    """AnyHcCalculator (large-molecule implementation, LCS not frozen) built on
+    st's atoms with XD-style local coordinate systems, called with the atoms
+    moved to xyz_moved: F and derivatives, and the reference's LCS matrices of
+    the moved geometry ([n][3][3], columns = local x, y, z)."""
+    keep = []
+
+    def D(a):
+        arr, p = _d(a); keep.append(arr); return p
+
+    def I(a):
+        arr, p = _i(a); keep.append(arr); return p
+
+    cell, ops, adp = _common(st)
+    n = st.n_atoms
+    orb_off, orb_occ, orb_core, sto_off, sto_pow, sto_exp, sto_coeff = [0], [], [], [0], [], [], []
+    def_exp, def_npow, def_pow, anom, zs = [], [], [], [], []
+    for w in st.wfns:
+        for k, o in enumerate(w.orbitals):
+            orb_occ.append(w.occupancy[k])
+            orb_core.append(1 if k in w.core else 0)
+            sto_pow += list(o.powers); sto_exp += list(o.exponents); sto_coeff += list(o.coefficients)
+            sto_off.append(len(sto_pow))
+        orb_off.append(len(orb_occ))
+        def_exp.append(w.def_val_exp)
+        def_npow.append(len(w.def_val_pow))
+        def_pow += list(w.def_val_pow)[:5] + [0] * (5 - min(5, len(w.def_val_pow)))
+        anom += [complex(w.anomalous).real, complex(w.anomalous).imag]
+        zs.append(w.atomic_number)
+    types = st.types
+    ld, la, ldu = flatten_lcs(defs)
+    out = _outputs(st.n_hkl, n)
+    lcs_out = np.zeros(9 * n)
+    with _Conventions(st):
+        rc = lib().ref_anyhc_lcs(
+            D(cell), C.c_char_p(ops), C.c_int(n), D(st.xyz.reshape(-1)), D(np.asarray(xyz_moved).reshape(-1)),
+            I(st.n_adp()), D(adp.reshape(-1)), D(st.occupancy), I(st.multiplicity), I(st.atom_wfn), I(st.atom_type),
+            I(ld.reshape(-1)), I(la), D(ldu.reshape(-1)),
+            C.c_int(len(st.wfns)), I(orb_off), I(orb_occ), I(orb_core), I(sto_off), I(sto_pow), D(sto_exp),
+            D(sto_coeff), D(def_exp), I(def_npow), I(def_pow), D(anom), I(zs),
+            C.c_int(len(types)), I([t.n_l for t in types]), D(np.array([t.plm for t in types]).reshape(-1)),
+            D([t.p_val for t in types]), D([t.kappa for t in types]), D([t.kappa_prime for t in types]),
+            C.c_int(st.n_hkl), I(st.hkl.reshape(-1)), D(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1)),
+            C.c_int(n_threads), D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]),
+            D_out(lcs_out))
+    if rc != 0:
+        raise RuntimeError("reference AnyHcCalculator path raised an exception: " + _err())
+    r = _pack(out, st, 0.0)
+    r["lcs"] = lcs_out.reshape(n, 3, 3)
+    return r
+
+
+def _hc_arrays(st):
+    """The flat HC-model arrays the driver's HC entries take."""
+    orb_off, orb_occ, orb_core, sto_off, sto_pow, sto_exp, sto_coeff = [0], [], [], [0], [], [], []
+    def_exp, def_npow, def_pow, anom, zs = [], [], [], [], []
+    for w in st.wfns:
+        for k, o in enumerate(w.orbitals):
+            orb_occ.append(w.occupancy[k])
+            orb_core.append(1 if k in w.core else 0)
+            sto_pow += list(o.powers); sto_exp += list(o.exponents); sto_coeff += list(o.coefficients)
+            sto_off.append(len(sto_pow))
+        orb_off.append(len(orb_occ))
+        def_exp.append(w.def_val_exp)
+        def_npow.append(len(w.def_val_pow))
+        def_pow += list(w.def_val_pow)[:5] + [0] * (5 - min(5, len(w.def_val_pow)))
+        anom += [complex(w.anomalous).real, complex(w.anomalous).imag]
+        zs.append(w.atomic_number)
+    types = st.types
+    return [("i", orb_off), ("i", orb_occ), ("i", orb_core), ("i", sto_off), ("i", sto_pow), ("d", sto_exp),
+            ("d", sto_coeff), ("d", def_exp), ("i", def_npow), ("i", def_pow), ("d", anom), ("i", zs),
+            ("n", len(types)), ("i", [t.n_l for t in types]), ("d", np.array([t.plm for t in types]).reshape(-1)),
+            ("d", [t.p_val for t in types]), ("d", [t.kappa for t in types]), ("d", [t.kappa_prime for t in types])]
+
+
+def combined(st, hc_atoms, iam_atoms, defs, table="IT92"):
+    """CombinedStructureFactorCalculator over an AnyHcCalculator (XD local
+    coordinate systems, large-molecule implementation) for hc_atoms and an
+    AnyIamCalculator with the named Gaussian table for iam_atoms, both on the
+    whole crystal; F and derivatives of the crystal's atoms."""
+    keep = []
+
+    def D(a):
+        arr, p = _d(a); keep.append(arr); return p
+
+    def I(a):
+        arr, p = _i(a); keep.append(arr); return p
+
+    cell, ops, adp = _common(st)
+    n = st.n_atoms
+    ld, la, ldu = flatten_lcs(defs)
+    model = []
+    for kind, v in _hc_arrays(st):
+        model.append(C.c_int(v) if kind == "n" else (I(v) if kind == "i" else D(v)))
+    out = _outputs(st.n_hkl, n)
+    with _Conventions(st):
+        rc = lib().ref_combined_sf(
+            D(cell), C.c_char_p(ops), C.c_int(n), D(st.xyz.reshape(-1)), I(st.n_adp()), D(adp.reshape(-1)),
+            D(st.occupancy), I(st.multiplicity), I(st.atom_wfn), I(st.atom_type), I(ld.reshape(-1)), I(la),
+            D(ldu.reshape(-1)), C.c_int(len(hc_atoms)), I(hc_atoms), C.c_int(len(iam_atoms)), I(iam_atoms),
+            C.c_char_p(table.encode()), C.c_int(len(st.wfns)), *model,
+            C.c_int(st.n_hkl), I(st.hkl.reshape(-1)), D(np.stack([st.dtdf.real, st.dtdf.imag], 1).reshape(-1)),
+            D_out(out["f"]), D_out(out["d_xyz"]), D_out(out["d_adp"]), D_out(out["d_occ"]))
+    if rc != 0:
+        raise RuntimeError("reference combined calculator raised an exception: " + _err())
+    return _pack(out, st, 0.0)

@@ -19,6 +19,10 @@
 #include "discamb/CrystalStructure/SpaceGroupOperation.h"
 #include "discamb/CrystalStructure/UnitCell.h"
 #include "discamb/HC_Model/HC_ModelParameters.h"
+#include "discamb/HC_Model/XdLocalCoordinateSystem.h"
+#include "discamb/Scattering/AnyHcCalculator.h"
+#include "discamb/Scattering/AnyIamCalculator.h"
+#include "discamb/Scattering/CombinedStructureFactorCalculator.h"
 #include "discamb/IO/tsc_io.h"
 #include "discamb/Scattering/AnyScattererStructureFactorCalculator.h"
 #include "discamb/Scattering/ConstFormFactorCalculationsManager.h"
@@ -105,6 +109,86 @@ void write_out(const vector<complex<double> > &f, const vector<TargetFunctionAto
     }
 }
 
+// the reference's HC model parameters from flat arrays (wavefunctions as Slater orbitals: per wfn
+// [orb_off[w], orb_off[w+1]) orbitals, per orbital [sto_off[o], sto_off[o+1]) Slater functions)
+HC_ModelParameters make_hc_params(int n_atoms, const int *atom_wfn, const int *atom_type, int n_wfn, const int *orb_off,
+                                  const int *orb_occ, const int *orb_core, const int *sto_off, const int *sto_pow,
+                                  const double *sto_exp, const double *sto_coeff, const double *def_exp,
+                                  const int *def_npow, const int *def_pow, const double *wfn_anom, const int *wfn_z,
+                                  int n_types, const int *type_nl, const double *type_plm, const double *type_pval,
+                                  const double *type_kappa, const double *type_kappa_p)
+{
+    HC_ModelParameters p;
+    p.wfn_parameters.resize(n_wfn);
+    for (int w = 0; w < n_wfn; w++) {
+        HC_WfnType &wt = p.wfn_parameters[w];
+        wt.wfnAtomTypeName = "W" + std::to_string(w);
+        wt.atomic_number = wfn_z[w];
+        for (int o = orb_off[w]; o < orb_off[w + 1]; o++) {
+            SlaterTypeAtomicOrbitalRdf orb;
+            for (int s = sto_off[o]; s < sto_off[o + 1]; s++) {
+                orb.power_r.push_back(sto_pow[s]);
+                orb.exponents.push_back(sto_exp[s]);
+                orb.coefficients.push_back(sto_coeff[s]);
+            }
+            int idx = (int)wt.orbitals.size();
+            wt.orbitals.push_back(orb);
+            wt.orbital_occupancy.push_back(orb_occ[o]);
+            if (orb_core[o]) wt.core_orbitals_indices.push_back(idx);
+            else wt.valence_orbitals_indices.push_back(idx);
+        }
+        wt.deformation_valence_exponent = def_exp[w];
+        wt.deformation_valence_power.assign(def_pow + 5 * w, def_pow + 5 * w + def_npow[w]);
+        wt.anomalous_scattering = complex<double>(wfn_anom[2 * w], wfn_anom[2 * w + 1]);
+    }
+    p.type_parameters.resize(n_types);
+    for (int t = 0; t < n_types; t++) {
+        HC_AtomTypeParameters &tp = p.type_parameters[t];
+        tp.p_lm.resize(type_nl[t]);
+        for (int l = 0; l < type_nl[t]; l++)
+            tp.p_lm[l].assign(type_plm + 25 * t + l * l, type_plm + 25 * t + l * l + 2 * l + 1);
+        tp.p_val = type_pval[t];
+        tp.kappa_spherical_valence = type_kappa[t];
+        tp.kappa_deformation_valence = type_kappa_p[t];
+    }
+    p.atom_to_wfn_map.assign(atom_wfn, atom_wfn + n_atoms);
+    p.atom_to_type_map.assign(atom_type, atom_type + n_atoms);
+    return p;
+}
+
+// XD-style local coordinate systems from flat arrays (lcs_def [n][7] = central, axis 1, axis 2 (+-1..3 for
+// +-X..Z), right-handed, n1, n2a, n2b; the points are sums of the atoms listed in lcs_atoms (consumed in order)
+// or, with n = 0, the fractional dummy position lcs_dummy[a][point][3])
+vector<std::shared_ptr<LocalCoordinateSystemInCrystal> > make_xd_lcs(const Crystal &crystal,
+                                                                      const vector<string> &labels, int n_atoms,
+                                                                      const int *lcs_def, const int *lcs_atoms,
+                                                                      const double *lcs_dummy)
+{
+    const char *axes[] = {"-Z", "-Y", "-X", "", "X", "Y", "Z"};
+    vector<std::shared_ptr<LocalCoordinateSystemInCrystal> > lcs;
+    int cursor = 0;
+    for (int a = 0; a < n_atoms; a++) {
+        const int *d = lcs_def + 7 * a;
+        vector<Vector3d> dummies;
+        string pts[3];
+        for (int q = 0; q < 3; q++) {
+            const int cnt = d[4 + q];
+            if (cnt == 0) {
+                pts[q] = "DUM" + std::to_string(dummies.size());
+                const double *v = lcs_dummy + 9 * a + 3 * q;
+                dummies.push_back(Vector3d(v[0], v[1], v[2]));
+            } else {
+                for (int k = 0; k < cnt; k++) pts[q] += (k ? ";" : "") + labels[lcs_atoms[cursor++]];
+            }
+        }
+        auto x = std::make_shared<XdLocalCoordinateSystem>();
+        x->set(labels[d[0]], pts[0], pts[1], pts[2], axes[d[1] + 3], axes[d[2] + 3], d[3] != 0, crystal, true,
+               dummies);
+        lcs.push_back(x);
+    }
+    return lcs;
+}
+
 } // namespace
 
 extern "C" {
@@ -166,41 +250,9 @@ int ref_hc_sf(const double *cell, const char *ops, int n_atoms, const double *xy
         for (int a = 0; a < n_atoms; a++) types += periodic_table::symbol(wfn_z[atom_wfn[a]]) + ";";
         Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, types.c_str()};
         Crystal crystal = make_crystal(in);
-        HC_ModelParameters p;
-        p.wfn_parameters.resize(n_wfn);
-        for (int w = 0; w < n_wfn; w++) {
-            HC_WfnType &wt = p.wfn_parameters[w];
-            wt.wfnAtomTypeName = "W" + std::to_string(w);
-            wt.atomic_number = wfn_z[w];
-            for (int o = orb_off[w]; o < orb_off[w + 1]; o++) {
-                SlaterTypeAtomicOrbitalRdf orb;
-                for (int s = sto_off[o]; s < sto_off[o + 1]; s++) {
-                    orb.power_r.push_back(sto_pow[s]);
-                    orb.exponents.push_back(sto_exp[s]);
-                    orb.coefficients.push_back(sto_coeff[s]);
-                }
-                int idx = (int)wt.orbitals.size();
-                wt.orbitals.push_back(orb);
-                wt.orbital_occupancy.push_back(orb_occ[o]);
-                if (orb_core[o]) wt.core_orbitals_indices.push_back(idx);
-                else wt.valence_orbitals_indices.push_back(idx);
-            }
-            wt.deformation_valence_exponent = def_exp[w];
-            wt.deformation_valence_power.assign(def_pow + 5 * w, def_pow + 5 * w + def_npow[w]);
-            wt.anomalous_scattering = complex<double>(wfn_anom[2 * w], wfn_anom[2 * w + 1]);
-        }
-        p.type_parameters.resize(n_types);
-        for (int t = 0; t < n_types; t++) {
-            HC_AtomTypeParameters &tp = p.type_parameters[t];
-            tp.p_lm.resize(type_nl[t]);
-            for (int l = 0; l < type_nl[t]; l++)
-                tp.p_lm[l].assign(type_plm + 25 * t + l * l, type_plm + 25 * t + l * l + 2 * l + 1);
-            tp.p_val = type_pval[t];
-            tp.kappa_spherical_valence = type_kappa[t];
-            tp.kappa_deformation_valence = type_kappa_p[t];
-        }
-        p.atom_to_wfn_map.assign(atom_wfn, atom_wfn + n_atoms);
-        p.atom_to_type_map.assign(atom_type, atom_type + n_atoms);
+        HC_ModelParameters p = make_hc_params(n_atoms, atom_wfn, atom_type, n_wfn, orb_off, orb_occ, orb_core, sto_off,
+                                              sto_pow, sto_exp, sto_coeff, def_exp, def_npow, def_pow, wfn_anom, wfn_z,
+                                              n_types, type_nl, type_plm, type_pval, type_kappa, type_kappa_p);
         vector<Matrix3d> lcsm(n_atoms);
         for (int a = 0; a < n_atoms; a++)
             for (int i = 0; i < 3; i++)
@@ -388,6 +440,123 @@ int ref_tsc_sf(const char *path, const double *cell, const char *ops, const char
         }
         return ref_table_sf(cell, ops, labels, n_atoms, xyz, n_adp, adp, occ, mult, (int)keys.size(), k.data(),
                             v.data(), n_hkl, hkl, dtdf, f_out, d_xyz, d_adp, d_occ, nullptr);
+    } catch (const std::exception &ex) {
+        g_last_error = ex.what();
+        return 1;
+    } catch (...) {
+        g_last_error = "unknown exception";
+        return 1;
+    }
+}
+
+// AnyHcCalculator with XD-style local coordinate systems (XdLocalCoordinateSystem, src/HC_Model/
+// XdLocalCoordinateSystem.cpp:86-264), the large-molecule implementation and the LCS not frozen
+// (src/Scattering/AnyHcCalculator.cpp:117-206): the calculator is built on the atoms at xyz, then
+// calculateStructureFactorsAndDerivatives is called with the atoms moved to xyz_moved, so the reference
+// recomputes every LCS from the moved geometry (AnyHcCalculator.cpp:236-244, 319-329).
+// lcs_def[a] = {central atom, axis 1, axis 2 (+-1..3 for +-X..Z), right-handed, n1, n2a, n2b}: the points
+// are sums of the n atoms listed in lcs_atoms (consumed in order) or, with n = 0, the fractional dummy
+// position lcs_dummy[a][point][3].  lcs_out: the LCS matrices of the moved geometry [n][3][3] (columns x y z).
+int ref_anyhc_lcs(const double *cell, const char *ops, int n_atoms, const double *xyz, const double *xyz_moved,
+                  const int *n_adp, const double *adp, const double *occ, const int *mult, const int *atom_wfn,
+                  const int *atom_type, const int *lcs_def, const int *lcs_atoms, const double *lcs_dummy,
+                  int n_wfn, const int *orb_off, const int *orb_occ, const int *orb_core,
+                  const int *sto_off, const int *sto_pow, const double *sto_exp, const double *sto_coeff,
+                  const double *def_exp, const int *def_npow, const int *def_pow, const double *wfn_anom,
+                  const int *wfn_z, int n_types, const int *type_nl, const double *type_plm, const double *type_pval,
+                  const double *type_kappa, const double *type_kappa_p, int n_hkl, const int *hkl,
+                  const double *dtdf, int n_threads, double *f_out, double *d_xyz, double *d_adp, double *d_occ,
+                  double *lcs_out)
+{
+    try {
+        std::string types;
+        vector<string> labels(n_atoms);
+        for (int a = 0; a < n_atoms; a++) {
+            types += periodic_table::symbol(wfn_z[atom_wfn[a]]) + ";";
+            labels[a] = periodic_table::symbol(wfn_z[atom_wfn[a]]) + std::to_string(a + 1);
+        }
+        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, types.c_str()};
+        Crystal crystal = make_crystal(in);
+        HC_ModelParameters p = make_hc_params(n_atoms, atom_wfn, atom_type, n_wfn, orb_off, orb_occ, orb_core, sto_off,
+                                              sto_pow, sto_exp, sto_coeff, def_exp, def_npow, def_pow, wfn_anom, wfn_z,
+                                              n_types, type_nl, type_plm, type_pval, type_kappa, type_kappa_p);
+        vector<std::shared_ptr<LocalCoordinateSystemInCrystal> > lcs = make_xd_lcs(crystal, labels, n_atoms, lcs_def, lcs_atoms, lcs_dummy);
+        AnyHcCalculator calc(crystal, p, lcs, false, false, true, n_threads, false, false, "CPU");
+        vector<AtomInCrystal> moved = crystal.atoms;
+        for (int a = 0; a < n_atoms; a++)
+            moved[a].coordinates = Vector3d(xyz_moved[3 * a], xyz_moved[3 * a + 1], xyz_moved[3 * a + 2]);
+        vector<Vector3i> h(n_hkl);
+        vector<complex<double> > g(n_hkl), f;
+        for (int i = 0; i < n_hkl; i++) {
+            h[i] = Vector3i(hkl[3 * i], hkl[3 * i + 1], hkl[3 * i + 2]);
+            g[i] = complex<double>(dtdf[2 * i], dtdf[2 * i + 1]);
+        }
+        vector<TargetFunctionAtomicParamDerivatives> dd;
+        calc.calculateStructureFactorsAndDerivatives(moved, h, f, dd, g, vector<bool>(n_atoms, true));
+        write_out(f, dd, f_out, d_xyz, d_adp, d_occ);
+        Crystal cm = crystal;
+        cm.atoms = moved;
+        for (int a = 0; a < n_atoms; a++) {
+            Matrix3d m;
+            lcs[a]->calculate(m, cm);
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) lcs_out[9 * a + 3 * i + j] = m(i, j);
+        }
+        return 0;
+    } catch (const std::exception &ex) {
+        g_last_error = ex.what();
+        return 1;
+    } catch (...) {
+        g_last_error = "unknown exception";
+        return 1;
+    }
+}
+
+// CombinedStructureFactorCalculator (src/Scattering/CombinedStructureFactorCalculator.cpp:9-52, 124-215) over an
+// AnyHcCalculator (XD local coordinate systems as ref_anyhc_lcs, large-molecule implementation) for the atoms in
+// hc_atoms and an AnyIamCalculator (the named Gaussian table, src/Scattering/AnyIamCalculator.cpp:13-19) for the
+// atoms in iam_atoms, both built on the whole crystal (TAAM's split, HcAtomBankStructureFactorCalculator.cpp:482-499).
+// The combined calculator sets every part's anomalous dispersion to zero when it is built (its set()).
+int ref_combined_sf(const double *cell, const char *ops, int n_atoms, const double *xyz, const int *n_adp,
+                    const double *adp, const double *occ, const int *mult, const int *atom_wfn, const int *atom_type,
+                    const int *lcs_def, const int *lcs_atoms, const double *lcs_dummy, int n_hc, const int *hc_atoms,
+                    int n_iam, const int *iam_atoms, const char *iam_table,
+                    int n_wfn, const int *orb_off, const int *orb_occ, const int *orb_core,
+                    const int *sto_off, const int *sto_pow, const double *sto_exp, const double *sto_coeff,
+                    const double *def_exp, const int *def_npow, const int *def_pow, const double *wfn_anom,
+                    const int *wfn_z, int n_types, const int *type_nl, const double *type_plm,
+                    const double *type_pval, const double *type_kappa, const double *type_kappa_p, int n_hkl,
+                    const int *hkl, const double *dtdf, double *f_out, double *d_xyz, double *d_adp, double *d_occ)
+{
+    try {
+        std::string types;
+        vector<string> labels(n_atoms);
+        for (int a = 0; a < n_atoms; a++) {
+            types += periodic_table::symbol(wfn_z[atom_wfn[a]]) + ";";
+            labels[a] = periodic_table::symbol(wfn_z[atom_wfn[a]]) + std::to_string(a + 1);
+        }
+        Input in{cell, ops, n_atoms, xyz, n_adp, adp, occ, mult, types.c_str()};
+        Crystal crystal = make_crystal(in);
+        HC_ModelParameters p = make_hc_params(n_atoms, atom_wfn, atom_type, n_wfn, orb_off, orb_occ, orb_core, sto_off,
+                                              sto_pow, sto_exp, sto_coeff, def_exp, def_npow, def_pow, wfn_anom, wfn_z,
+                                              n_types, type_nl, type_plm, type_pval, type_kappa, type_kappa_p);
+        vector<std::shared_ptr<LocalCoordinateSystemInCrystal> > lcs =
+            make_xd_lcs(crystal, labels, n_atoms, lcs_def, lcs_atoms, lcs_dummy);
+        vector<std::shared_ptr<SfCalculator> > calcs{
+            std::make_shared<AnyHcCalculator>(crystal, p, lcs, false, false, true, 1, false, false, "CPU"),
+            std::make_shared<AnyIamCalculator>(crystal, false, string(iam_table))};
+        vector<vector<int> > parts{vector<int>(hc_atoms, hc_atoms + n_hc), vector<int>(iam_atoms, iam_atoms + n_iam)};
+        CombinedStructureFactorCalculator calc(calcs, parts);
+        vector<Vector3i> h(n_hkl);
+        vector<complex<double> > g(n_hkl), f;
+        for (int i = 0; i < n_hkl; i++) {
+            h[i] = Vector3i(hkl[3 * i], hkl[3 * i + 1], hkl[3 * i + 2]);
+            g[i] = complex<double>(dtdf[2 * i], dtdf[2 * i + 1]);
+        }
+        vector<TargetFunctionAtomicParamDerivatives> dd;
+        calc.calculateStructureFactorsAndDerivatives(crystal.atoms, h, f, dd, g, vector<bool>(n_atoms, true));
+        write_out(f, dd, f_out, d_xyz, d_adp, d_occ);
+        return 0;
     } catch (const std::exception &ex) {
         g_last_error = ex.what();
         return 1;

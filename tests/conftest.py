@@ -52,3 +52,20 @@ def engine():
     eng = api.Engine(0)
     yield eng
     eng.close()
+
+
+def combined_parts(st, d):
+    """The two parts of the combined_taam fixture as the engine's split takes
+    them: the HC atoms' structure (anomalous dispersion zero, as the reference's
+    combined calculator sets it) and the IAM atoms' structure with its types
+    renumbered to its elements, plus that part's IT92 coefficients."""
+    hc, ia = np.asarray(d["hc_atoms"]), np.asarray(d["iam_atoms"])
+    s1 = st.subset(hc)
+    s1.anomalous = np.zeros(s1.n_atoms, dtype=complex)
+    used_w = sorted(set(int(w) for w in st.atom_wfn[ia]))
+    s2 = st.subset(ia)
+    s2.atom_type = s2.atom_wfn.copy()
+    s2.anomalous = np.zeros(s2.n_atoms, dtype=complex)
+    iam = dict(ngauss=d["wfn_iam_ngauss"][used_w], a=d["wfn_iam_a"][used_w], b=d["wfn_iam_b"][used_w],
+               c=d["wfn_iam_c"][used_w])
+    return hc, ia, s1, s2, iam

@@ -136,4 +136,136 @@ int drv_hc(int device, const dsf_symmetry *sym, const dsf_hc_model *model, const
     }
 }
 
+// XD-style definitions from the flat arrays of the golden fixtures (lcs_def [n][7] = central, axis1, axis2,
+// right-handed, n1, n2a, n2b; lcs_atoms consumed in order; lcs_dummy [n][3][3] fractional)
+static std::vector<dsf::XdLcs> lcs_definitions(int n, const int *def, const int *list, const double *dummy)
+{
+    std::vector<dsf::XdLcs> out(n);
+    int cursor = 0;
+    for (int a = 0; a < n; a++) {
+        const int *d = def + 7 * a;
+        dsf::XdLcs &q = out[a];
+        q.central = d[0];
+        q.axis1 = d[1];
+        q.axis2 = d[2];
+        q.right_handed = d[3] != 0;
+        std::vector<int> *pts[3] = {&q.point1, &q.point2_from, &q.point2_to};
+        dsf::Vector3d *dum[3] = {&q.dummy1, &q.dummy2_from, &q.dummy2_to};
+        for (int p = 0; p < 3; p++) {
+            for (int k = 0; k < d[4 + p]; k++) pts[p]->push_back(list[cursor++]);
+            for (int k = 0; k < 3; k++) (*dum[p])[k] = dummy[9 * a + 3 * p + k];
+        }
+    }
+    return out;
+}
+
+static std::vector<dsf::AtomInCrystal> atom_list(int n, const int *nadp, const double *xyz, const double *adp,
+                                                 const double *occ)
+{
+    std::vector<dsf::AtomInCrystal> at(n);
+    for (int a = 0; a < n; a++) {
+        at[a].coordinates = {xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]};
+        at[a].adp.assign(adp + 6 * a, adp + 6 * a + nadp[a]);
+        at[a].occupancy = occ[a];
+    }
+    return at;
+}
+
+// host only: the LCS matrices ([n][9]) of the definitions for the positions xyz (crystal convention)
+int drv_lcs_matrices(int n, const double *cell, int cartesian, const double *xyz, const int *def, const int *list,
+                     const double *dummy, double *out)
+{
+    try {
+        const auto defs = lcs_definitions(n, def, list, dummy);
+        std::vector<dsf::AtomInCrystal> at(n);
+        for (int a = 0; a < n; a++) at[a].coordinates = {xyz[3 * a], xyz[3 * a + 1], xyz[3 * a + 2]};
+        const auto M = dsf::fractionalToCartesian(cell);
+        for (int a = 0; a < n; a++) {
+            const auto m = dsf::lcsMatrix(defs[a], M, cartesian != 0, at);
+            std::copy(m.begin(), m.end(), out + 9 * a);
+        }
+        return 0;
+    } catch (const std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
+// AnyHcCalculator's flow with local coordinate systems: the calculator is created on the atoms of `atoms`
+// (xyz), the definitions are set (frozen or not), and the whole-set call is made with the atoms at xyz_moved;
+// outputs F and derivatives of that call and the matrices the engine holds afterwards (lcs_out [n][9])
+int drv_hc_lcs(int device, const dsf_symmetry *sym, const dsf_hc_model *model, const dsf_atoms *atoms,
+               int precision, int frozen, const double *xyz, const double *xyz_moved, const double *adp,
+               const double *occ, const int *def, const int *list, const double *dummy, int m, const int *hkl,
+               const double *dtdf, double *f, double *d_xyz, double *d_adp, double *d_occ, double *lcs_out)
+{
+    try {
+        auto engine = std::make_shared<dsf::Engine>(device);
+        dsf::HcCalculator calc(engine, *sym, *model, *atoms);
+        calc.setPrecision(precision);
+        const int n = atoms->n_atoms;
+        calc.setLocalCoordinateSystems(lcs_definitions(n, def, list, dummy), frozen != 0,
+                                       atom_list(n, atoms->adp_components, xyz, adp, occ));
+        const auto moved = atom_list(n, atoms->adp_components, xyz_moved, adp, occ);
+        std::vector<dsf::Vector3i> h(m);
+        std::vector<dsf::cplx> g(m);
+        for (int i = 0; i < m; i++) {
+            h[i] = {hkl[3 * i], hkl[3 * i + 1], hkl[3 * i + 2]};
+            g[i] = dsf::cplx(dtdf[2 * i], dtdf[2 * i + 1]);
+        }
+        std::vector<dsf::cplx> fv;
+        std::vector<dsf::TargetFunctionAtomicParamDerivatives> d;
+        calc.calculateStructureFactorsAndDerivatives(moved, h, fv, d, g);
+        std::memcpy(f, fv.data(), sizeof(double) * 2 * m);
+        for (int a = 0; a < n; a++) {
+            for (int k = 0; k < 3; k++) d_xyz[3 * a + k] = d[a].atomic_position_derivatives[k];
+            for (int k = 0; k < 6; k++) d_adp[6 * a + k] = k < (int)d[a].adp_derivatives.size() ? d[a].adp_derivatives[k] : 0.0;
+            d_occ[a] = d[a].occupancy_derivatives;
+        }
+        std::copy(calc.localCoordinateSystems().begin(), calc.localCoordinateSystems().end(), lcs_out);
+        return 0;
+    } catch (const std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
+// CombinedCalculator over an HC part (hc_* descriptors of the structure of the atoms hc_idx) and an IAM part
+// (iam_* descriptors of the atoms iam_idx); the whole structure's atoms: xyz [n][3], adp [n][6], occ [n], nadp [n]
+int drv_combined(int device, int precision, const dsf_symmetry *hc_sym, const dsf_hc_model *hc_model,
+                 const dsf_atoms *hc_atoms, const int *hc_idx, const dsf_symmetry *iam_sym,
+                 const dsf_iam_model *iam_model, const dsf_atoms *iam_atoms, const int *iam_idx, int n,
+                 const int *nadp, const double *xyz, const double *adp, const double *occ, int m, const int *hkl,
+                 const double *dtdf, double *f, double *d_xyz, double *d_adp, double *d_occ)
+{
+    try {
+        auto engine = std::make_shared<dsf::Engine>(device);
+        auto hc = std::make_shared<dsf::HcCalculator>(engine, *hc_sym, *hc_model, *hc_atoms);
+        auto iam = std::make_shared<dsf::IamCalculator>(engine, *iam_sym, *iam_model, *iam_atoms, "IT92");
+        dsf::CombinedCalculator comb({hc, iam}, {std::vector<int>(hc_idx, hc_idx + hc_atoms->n_atoms),
+                                                 std::vector<int>(iam_idx, iam_idx + iam_atoms->n_atoms)});
+        comb.setPrecision(precision);
+        const auto at = atom_list(n, nadp, xyz, adp, occ);
+        std::vector<dsf::Vector3i> h(m);
+        std::vector<dsf::cplx> g(m);
+        for (int i = 0; i < m; i++) {
+            h[i] = {hkl[3 * i], hkl[3 * i + 1], hkl[3 * i + 2]};
+            g[i] = dsf::cplx(dtdf[2 * i], dtdf[2 * i + 1]);
+        }
+        std::vector<dsf::cplx> fv;
+        std::vector<dsf::TargetFunctionAtomicParamDerivatives> d;
+        comb.calculateStructureFactorsAndDerivatives(at, h, fv, d, g, std::vector<bool>(n, true));
+        std::memcpy(f, fv.data(), sizeof(double) * 2 * m);
+        for (int a = 0; a < n; a++) {
+            for (int k = 0; k < 3; k++) d_xyz[3 * a + k] = d[a].atomic_position_derivatives[k];
+            for (int k = 0; k < 6; k++) d_adp[6 * a + k] = k < (int)d[a].adp_derivatives.size() ? d[a].adp_derivatives[k] : 0.0;
+            d_occ[a] = d[a].occupancy_derivatives;
+        }
+        return 0;
+    } catch (const std::exception &ex) {
+        g_err = ex.what();
+        return 1;
+    }
+}
+
 }  // extern "C"

@@ -2,7 +2,7 @@
 library's own CPU code (oracle/_ref/libref_driver.so, built from the
 reference sources by oracle/Makefile.ref) on seeded synthetic structures.
 
-    python tests/golden/make_golden.py [hc|centering|conventions|def_val_symm|form_factors|rest ...]
+    python tests/golden/make_golden.py [hc|centering|conventions|lcs|combined|def_val_symm|form_factors|rest ...]
                                                                                   (default: all)
 
 Each fixture (.npz) holds every input of the case (structure_to_arrays) and
@@ -320,7 +320,93 @@ def write_conventions():
     print("wrote iam_conv_c2c_cart_U_star", st.n_atoms, st.n_hkl)
 
 
-GROUPS = {"hc": write_hc, "centering": write_centering, "conventions": write_conventions, "def_val_symm": write_def_val_symm, "form_factors": write_form_factors,
+def lcs_definitions(n, rng):
+    """XD-style local coordinate systems for n >= 4 atoms, one per atom: Z (or
+    another axis) towards a neighbour, the second axis from a third pair; one
+    left-handed system, one point given by two atoms (the reference sums
+    their positions) and one by a dummy position."""
+    axes = [(3, 1), (1, 2), (-3, 1), (2, -3), (3, -2), (-1, 3)]
+    defs = []
+    for a in range(n):
+        a1, a2 = axes[a % len(axes)]
+        q = dict(central=a, point1=[(a + 1) % n], point2_from=[a], point2_to=[(a + 2) % n], axis1=a1, axis2=a2,
+                 right=True, dummy=np.zeros((3, 3)))
+        defs.append(q)
+    defs[1]["right"] = False
+    defs[2]["point2_to"] = [(2 + 2) % n, (2 + 3) % n]
+    defs[3]["point1"] = []
+    defs[3]["dummy"] = np.array([[0.31, 0.62, 0.12], [0.0, 0.0, 0.0], [0.0, 0.0, 0.0]]) + rng.uniform(0, 0.05, (3, 3))
+    return defs
+
+
+def write_lcs():
+    """AnyHcCalculator with XD local coordinate systems that are not frozen
+    (large-molecule implementation): the calculator is set up on one geometry
+    and called with the atoms moved (sigma 0.05 A), so the reference
+    recomputes every LCS from the moved atoms before its engine runs
+    (AnyHcCalculator.cpp:236-244, 319-329).  The fixture holds both
+    geometries, the definitions, the reference's LCS matrices of each
+    geometry and the results of the call with the moved atoms."""
+    for name, sg, xyz_conv in (("lcs_update_p21c", "P21/c", "fractional"), ("lcs_update_p1_cart", "P1", "cartesian")):
+        st = W.small_case(sg, n_atoms=6, stol_max=0.5, seed=1100 + len(name))
+        rng = np.random.default_rng(1150 + len(name))
+        if xyz_conv == "cartesian":
+            st = to_conventions(st, "cartesian", "U_cif")
+            moved = st.xyz + rng.normal(scale=0.05, size=st.xyz.shape)
+        else:
+            from discamb_gb300.crystal import frac_to_cart_matrix
+            minv = np.linalg.inv(frac_to_cart_matrix(st.cell))
+            moved = st.xyz + (minv @ rng.normal(scale=0.05, size=st.xyz.shape).T).T
+        defs = lcs_definitions(st.n_atoms, rng)
+        r0 = R.anyhc_lcs(st, st.xyz, defs)  # the set-up geometry: its LCS become st.lcs
+        st.lcs = r0["lcs"]
+        r = R.anyhc_lcs(st, moved, defs)
+        out = structure_to_arrays(st)
+        nadp = st.n_adp()
+        d_adp = np.zeros((st.n_atoms, 6))
+        for i, v in enumerate(r["d_adp"]):
+            d_adp[i, :nadp[i]] = v
+        ld, la, ldu = R.flatten_lcs(defs)
+        out.update(xyz_moved=moved, lcs_def=ld, lcs_atoms=la, lcs_dummy=ldu, ref_lcs_moved=r["lcs"],
+                   ref_f=r["f"], ref_d_xyz=r["d_xyz"], ref_d_adp=d_adp, ref_d_occ=r["d_occ"])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print("wrote", name, st.n_atoms, st.n_hkl)
+
+
+def write_combined():
+    """The reference's CombinedStructureFactorCalculator with TAAM's split
+    (HcAtomBankStructureFactorCalculator.cpp:482-499): the non-H atoms on an
+    AnyHcCalculator (XD local coordinate systems), the H atoms on an
+    AnyIamCalculator with the IT92 table.  The combined calculator zeroes the
+    anomalous dispersion of its parts when it is built.  The fixture adds the
+    atom lists, the IT92 coefficients per wavefunction (element) and the
+    reference's LCS matrices."""
+    st = W.small_case("P21/c", n_atoms=9, stol_max=0.5, seed=1300, improper_lcs=True)
+    rng = np.random.default_rng(1301)
+    defs = lcs_definitions(st.n_atoms, rng)
+    st.lcs = R.anyhc_lcs(st, st.xyz, defs)["lcs"]
+    labels = [st.wfns[w].label for w in st.atom_wfn]
+    hc_atoms = np.array([i for i, e in enumerate(labels) if e != "H"], dtype=np.int32)
+    iam_atoms = np.array([i for i, e in enumerate(labels) if e == "H"], dtype=np.int32)
+    r = R.combined(st, hc_atoms, iam_atoms, defs, "IT92")
+    ng, ga, gb, gc = [], np.zeros((len(st.wfns), 5)), np.zeros((len(st.wfns), 5)), []
+    for i, w in enumerate(st.wfns):
+        a, b, c = R.iam_coefficients(w.label, "IT92")
+        ng.append(len(a)); ga[i, :len(a)] = a; gb[i, :len(b)] = b; gc.append(c)
+    out = structure_to_arrays(st)
+    nadp = st.n_adp()
+    d_adp = np.zeros((st.n_atoms, 6))
+    for i, v in enumerate(r["d_adp"]):
+        d_adp[i, :nadp[i]] = v
+    ld, la, ldu = R.flatten_lcs(defs)
+    out.update(hc_atoms=hc_atoms, iam_atoms=iam_atoms, wfn_iam_ngauss=np.array(ng), wfn_iam_a=ga, wfn_iam_b=gb,
+               wfn_iam_c=np.array(gc), lcs_def=ld, lcs_atoms=la, lcs_dummy=ldu,
+               ref_f=r["f"], ref_d_xyz=r["d_xyz"], ref_d_adp=d_adp, ref_d_occ=r["d_occ"])
+    np.savez_compressed(os.path.join(HERE, "combined_taam_p21c.npz"), **out)
+    print("wrote combined_taam_p21c", st.n_atoms, st.n_hkl, len(hc_atoms), len(iam_atoms))
+
+
+GROUPS = {"hc": write_hc, "lcs": write_lcs, "combined": write_combined, "centering": write_centering, "conventions": write_conventions, "def_val_symm": write_def_val_symm, "form_factors": write_form_factors,
           "rest": write_rest}
 
 

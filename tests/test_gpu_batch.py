@@ -225,6 +225,8 @@ def test_combined_hc_and_iam_atoms(engine):
         r = comb.calculate(st.dtdf, precision=prec, atoms=(xyz, st.adp, st.occupancy))
         s1, s2 = st.subset(hc_idx), st.subset(iam_idx)
         s1.xyz, s2.xyz = xyz[hc_idx], xyz[iam_idx]
+        # the combined calculator starts with zero anomalous dispersion, as the reference's does
+        s1.anomalous, s2.anomalous = np.zeros(s1.n_atoms, complex), np.zeros(s2.n_atoms, complex)
         o1, o2 = O.compute(s1), O.compute(s2, model="iam", iam=iam)
         assert rel_f(r["f"], o1["f"] + o2["f"]) < tf
         ref_xyz = np.zeros((st.n_atoms, 3))
@@ -288,3 +290,24 @@ def test_submit_and_poll(engine):
     assert rel_f(calcs[0].calculate(sts[0].dtdf, precision=FP32)["f"], want[0]["f"]) < 1e-12
     for c in calcs:
         c.close()
+
+
+@pytest.mark.parametrize("prec,tf,tg", [(FP64, 1e-10, 1e-10), (FP32, 1e-6, 1e-5)])
+def test_combined_calculator_matches_reference(engine, prec, tf, tg):
+    # the reference's CombinedStructureFactorCalculator with TAAM's split: non-H atoms on AnyHcCalculator, H atoms
+    # on AnyIamCalculator (IT92), anomalous dispersion zeroed by the combined calculator
+    from conftest import combined_parts, load_fixture, ref_adp_list
+    st, d = load_fixture("combined_taam_p21c")
+    hc, ia, s1, s2, iam = combined_parts(st, d)
+
+    def make_iam(sub):
+        sub.atom_type = sub.atom_wfn.copy()
+        return api.IamCalculator(engine, sub, iam)
+
+    comb = api.CombinedCalculator(engine, st, [(lambda s: api.HcCalculator(engine, s), hc), (make_iam, ia)])
+    r = comb.calculate(st.dtdf, precision=prec)
+    assert rel_f(r["f"], d["ref_f"]) < tf, rel_f(r["f"], d["ref_f"])
+    assert rel_norm(r["d_xyz"], d["ref_d_xyz"]) < tg
+    assert rel_norm(r["d_adp"], ref_adp_list(st, d)) < tg
+    assert rel_norm(r["d_occ"], d["ref_d_occ"]) < tg
+    comb.close()

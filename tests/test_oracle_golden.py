@@ -138,3 +138,34 @@ def test_single_h_form_factors_match_reference():
     st, d = load_fixture("ff_iam_c2c")
     o = O.compute(st, model="iam", iam=iam_dict(d), form_factors=True)
     assert np.abs(o - d["ref_ff"]).max() <= 1e-13 * np.abs(d["ref_ff"]).max()
+
+
+@pytest.mark.parametrize("name", ["lcs_update_p21c", "lcs_update_p1_cart"])
+def test_reference_recomputed_the_lcs_from_the_moved_atoms(name):
+    # the fixture's reference result is that of the moved atoms with the LCS of the moved geometry; with the
+    # LCS of the set-up geometry instead it differs (so the fixture pins the recomputation)
+    st, d = load_fixture(name)
+    st.xyz = d["xyz_moved"]
+    kept = st.lcs.copy()
+    st.lcs = d["ref_lcs_moved"]
+    r = O.compute(st, n_threads=2)
+    assert rel_f(r["f"], d["ref_f"]) < 1e-12
+    assert rel_norm(r["d_xyz"], d["ref_d_xyz"]) < 1e-11
+    st.lcs = kept
+    assert rel_f(O.compute(st, n_threads=2)["f"], d["ref_f"]) > 1e-6
+
+
+def test_combined_calculator_fixture_is_the_sum_of_its_parts():
+    # the reference's CombinedStructureFactorCalculator (HC atoms + IAM atoms, anomalous dispersion zeroed by the
+    # combined calculator): F is the sum of the parts' F, each atom's derivatives come from its own part
+    from conftest import combined_parts
+    st, d = load_fixture("combined_taam_p21c")
+    hc, ia, s1, s2, iam = combined_parts(st, d)
+    o1, o2 = O.compute(s1, n_threads=2), O.compute(s2, model="iam", iam=iam, n_threads=2)
+    assert rel_f(o1["f"] + o2["f"], d["ref_f"]) < 1e-12
+    ref_xyz = d["ref_d_xyz"]
+    assert rel_norm(o1["d_xyz"], ref_xyz[hc]) < 1e-11 and rel_norm(o2["d_xyz"], ref_xyz[ia]) < 1e-11
+    ref_adp = ref_adp_list(st, d)
+    assert rel_norm(o1["d_adp"], [ref_adp[i] for i in hc]) < 1e-11
+    assert rel_norm(o2["d_adp"], [ref_adp[i] for i in ia]) < 1e-11
+    assert rel_norm(np.concatenate([o1["d_occ"], o2["d_occ"]]), np.concatenate([d["ref_d_occ"][hc], d["ref_d_occ"][ia]])) < 1e-11
