@@ -537,6 +537,65 @@ __global__ void atom_convert_kernel(AtomParams P, const double *raw, const int *
 // cosets have one size >= 2.
 bool fractional_signs(dsf_structure *s, int cs);
 
+// Cosets of four whose relative sign maps form a known group (222 or 2/m with b unique): each coset reordered
+// to [e, a, b, ab] of that group's generators (kPatD2, kPatC2hB), the same pattern for every coset, so the
+// Walsh-Hadamard coset kernels apply.  Only the order within a coset changes (the first operation stays, so
+// the relative signs stay); cosets that fit no pattern keep their order.
+void order_cosets_as_sign_group(dsf_structure *s)
+{
+    const int n = s->n_sym;
+    auto mask = [&](int op) {
+        int m = 0;
+        for (int i = 0; i < 3; i++)
+            if (s->sym_sign[3 * op + i] < 0) m |= 1 << i;
+        return m;
+    };
+    for (const int pat : {kPatD2, kPatC2hB}) {
+        const int want[4] = {0, pat & 7, (pat >> 3) & 7, (pat & 7) ^ ((pat >> 3) & 7)};
+        std::vector<int> perm(n);
+        bool fits = true;
+        for (int c0 = 0; c0 < n && fits; c0 += 4)
+            for (int j = 0; j < 4 && fits; j++) {
+                int found = -1;
+                for (int t = 0; t < 4; t++)
+                    if (mask(c0 + t) == want[j]) found = c0 + t;
+                if (found < 0) fits = false;
+                else perm[c0 + j] = found;
+            }
+        if (!fits) continue;
+        std::vector<int> rot(9 * (size_t)n), t24(3 * (size_t)n), sign(3 * (size_t)n);
+        for (int k = 0; k < n; k++) {
+            std::copy(&s->sym_rot[9 * perm[k]], &s->sym_rot[9 * perm[k]] + 9, &rot[9 * k]);
+            std::copy(&s->sym_t24[3 * perm[k]], &s->sym_t24[3 * perm[k]] + 3, &t24[3 * k]);
+            std::copy(&s->sym_sign[3 * perm[k]], &s->sym_sign[3 * perm[k]] + 3, &sign[3 * k]);
+        }
+        s->sym_rot.swap(rot);
+        s->sym_t24.swap(t24);
+        s->sym_sign.swap(sign);
+        return;
+    }
+}
+
+// the sign-group pattern of a launch's sign table: cosets of four whose every operation gives every parity
+// class (harmonic and fractional) the sign of the pattern's character at its position, else 0
+int wht_pattern_of(const SignTable &G, int n_sym, int coset)
+{
+    if (coset != 4 || n_sym % 4 != 0) return 0;
+    for (const int pat : {kPatD2, kPatC2hB}) {
+        bool ok = true;
+        for (int op = 0; op < n_sym && ok; op++) {
+            const int j = op & 3;
+            for (int c = 0; c < 8 && ok; c++) {
+                const int k = wht_char(pat, c);
+                const float want = (((k & 1) & (j & 1)) ^ (((k >> 1) & 1) & (j >> 1))) ? -1.0f : 1.0f;
+                ok = G.f[op][c] == want && G.xf[op][c] == want;
+            }
+        }
+        if (ok) return pat;
+    }
+    return 0;
+}
+
 void order_sign_cosets(dsf_structure *s)
 {
     const int n = s->n_sym;
@@ -597,6 +656,7 @@ void order_sign_cosets(dsf_structure *s)
     s->sym_t24.swap(t24);
     s->sym_sign = sign;
     s->coset_size = cs;
+    if (cs == 4) order_cosets_as_sign_group(s);
     // the same cosets must be sign-diagonal on the fractional h' as well (standard settings are)
     if (!fractional_signs(s, cs)) s->coset_size = 0;
 }
@@ -2016,6 +2076,7 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         A.G = &G;
         A.n_sym = s->n_sym;
         A.coset = L.coset;
+        A.pattern = wht_pattern_of(G, s->n_sym, L.coset);
         A.n_tiles = nt;
         A.n_chunks = n_chunks;
         A.smem = smem;
@@ -2161,6 +2222,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
                 A.G = &G;
                 A.n_sym = s->n_sym;
                 A.coset = L.coset;
+                A.pattern = wht_pattern_of(G, s->n_sym, L.coset);
                 A.n_tiles = nt;
                 A.n_chunks = n_chunks;
                 A.smem = smem;
@@ -2238,6 +2300,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
             A.G = &g.G;
             A.n_sym = g.n_sym;
             A.coset = g.coset;
+            A.pattern = wht_pattern_of(g.G, g.n_sym, g.coset);
             A.inv = g.inv;
             A.blocks = blocks;
             A.smem = g.smem;

@@ -7,6 +7,10 @@ namespace dsf {
 cudaError_t launch_k3_f32_hc(const K3Args &A, bool mp, bool aniso)
 {
     if (mp) return launch_k3_f32_hc_mp(A, aniso);
+    cudaError_t rc;
+    if (aniso ? dispatch_pattern<false, float, MODEL_HC, false, true, true, false, kPatD2>(A, rc)
+              : dispatch_pattern<false, float, MODEL_HC, false, false, true, false, kPatD2>(A, rc))
+        return rc;
     if (A.coset)
         return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, true, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
                      : dispatch_coset<false, float, MODEL_HC, false, false, true, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);

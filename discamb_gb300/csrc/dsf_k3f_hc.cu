@@ -9,6 +9,10 @@ namespace dsf {
 
 cudaError_t launch_k3f_hc(const K3Args &A, bool aniso)
 {
+    cudaError_t rc;
+    if (aniso ? dispatch_pattern<false, float, MODEL_HC, false, true, false, false, kPatD2>(A, rc)
+              : dispatch_pattern<false, float, MODEL_HC, false, false, false, false, kPatD2>(A, rc))
+        return rc;
     if (A.coset)
         return aniso ? dispatch_coset<false, float, MODEL_HC, false, true, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A)
                      : dispatch_coset<false, float, MODEL_HC, false, false, false, false, 2, 2, 4, 4, 4, 2, 8, 8, 8, 4>(A);

@@ -20,6 +20,7 @@ struct K3Args {
     int n_sym = 0, coset = 0;
     bool grad = true;  // false: structure factors only (single-structure FP32 kernels without the adjoint)
     bool inv = false;  // operations as n/2 plus their images under an inversion at the origin (generic models)
+    int pattern = 0;   // cosets of four in the order of a known sign group (kPatD2, kPatC2hB), else 0
     int n_tiles = 0, n_chunks = 0, blocks = 0;
     size_t smem = 0;
     cudaStream_t st = nullptr;
@@ -34,28 +35,42 @@ cudaError_t launch_with(K k, dim3 grid, size_t smem, cudaStream_t st, const Args
     return cudaGetLastError();
 }
 
-template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV, int NSC, int CS = 0>
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV, int NSC, int CS = 0,
+          int PAT = 0>
 cudaError_t launch_k3(const K3Args &A)
 {
     constexpr bool OCC4 = occ4_kernel<R, MODEL, NSC>();
     const dim3 grid = BATCH ? dim3(A.blocks) : dim3(A.n_tiles, A.n_chunks);
     static_assert(GRAD || !BATCH, "structure-factor-only kernels: single structures");
     if constexpr (!GRAD && OCC4)
-        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS, false, INV>, grid, A.smem, A.st, *A.S,
-                           *A.C, *A.L, *A.G);
+        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS, false, INV, PAT>, grid, A.smem, A.st,
+                           *A.S, *A.C, *A.L, *A.G);
     else if constexpr (!GRAD)
-        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS, false, INV>, grid, A.smem, A.st, *A.S, *A.C,
-                           *A.L, *A.G);
-    else if constexpr (BATCH && OCC4)
-        return launch_with(sf_grad_batch3_occ4<R, MODEL, MP, ANISO, NSC, CS, INV>, grid, A.smem, A.st, *A.B, *A.G);
-    else if constexpr (BATCH)
-        return launch_with(sf_grad_batch3<R, MODEL, MP, ANISO, NSC, CS, INV>, grid, A.smem, A.st, *A.B, *A.G);
-    else if constexpr (OCC4)
-        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS, true, INV>, grid, A.smem, A.st, *A.S,
+        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS, false, INV, PAT>, grid, A.smem, A.st, *A.S,
                            *A.C, *A.L, *A.G);
+    else if constexpr (BATCH && OCC4)
+        return launch_with(sf_grad_batch3_occ4<R, MODEL, MP, ANISO, NSC, CS, INV, PAT>, grid, A.smem, A.st, *A.B,
+                           *A.G);
+    else if constexpr (BATCH)
+        return launch_with(sf_grad_batch3<R, MODEL, MP, ANISO, NSC, CS, INV, PAT>, grid, A.smem, A.st, *A.B, *A.G);
+    else if constexpr (OCC4)
+        return launch_with(sf_grad_kernel3_occ4<R, MODEL, MP, ANISO, NSC, CS, true, INV, PAT>, grid, A.smem, A.st,
+                           *A.S, *A.C, *A.L, *A.G);
     else
-        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS, true, INV>, grid, A.smem, A.st, *A.S, *A.C,
-                           *A.L, *A.G);
+        return launch_with(sf_grad_kernel3<R, MODEL, MP, ANISO, NSC, CS, true, INV, PAT>, grid, A.smem, A.st, *A.S,
+                           *A.C, *A.L, *A.G);
+}
+
+// cosets of four in a known sign group's order (A.pattern == PAT): the Walsh-Hadamard kernels of the compiled
+// operation counts (4, 8); false when none applies (the caller then takes the general coset kernels)
+template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV, int PAT>
+bool dispatch_pattern(const K3Args &A, cudaError_t &rc)
+{
+    if (A.pattern != PAT || A.coset != 4) return false;
+    if (A.n_sym == 4) rc = launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, INV, 4, 4, PAT>(A);
+    else if (A.n_sym == 8 && !INV) rc = launch_k3<BATCH, R, MODEL, MP, ANISO, GRAD, INV, 8, 4, PAT>(A);
+    else return false;
+    return true;
 }
 
 // compiled operation counts first, runtime count last (INV kernels exist only for compiled counts: the

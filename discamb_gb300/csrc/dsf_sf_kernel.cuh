@@ -220,6 +220,38 @@ __host__ __device__ constexpr int harmonic_slot(int q)
     return sl[q];
 }
 
+// Cosets of four forming a known sign group (PAT != 0).  Within a coset ordered
+// [e, a, b, ab] (signs relative to its first operation; a, b the group's
+// generators as 3-bit masks of the axes they flip, PAT = a | b << 3), the sign
+// operation s gives parity class c is the character chi_k(s) = (-1)^(k0 s0 +
+// k1 s1) of index k = k0 + 2 k1, k0 = parity(c & a), k1 = parity(c & b), s0,
+// s1 the bits of the position s.  Every signed sum over a coset's operations
+// is then one of the four Walsh-Hadamard outputs of the operations' values
+// (8 additions for all four), and every operation's signed combination of
+// class sums one of the four outputs of the same transform of the class sums
+// gathered by character.  Patterns: kPatD2 (222: a = 2z, b = 2y) and kPatC2hB
+// (2/m, b unique: a = 2y, b = inversion).
+constexpr int kPatD2 = 3 | (5 << 3);
+constexpr int kPatC2hB = 5 | (7 << 3);
+
+__host__ __device__ constexpr int parity3(int v) { return (v ^ (v >> 1) ^ (v >> 2)) & 1; }
+__host__ __device__ constexpr int wht_char(int pat, int c)
+{
+    return parity3(c & pat & 7) + 2 * parity3(c & (pat >> 3) & 7);
+}
+
+// W[k] = sum_s chi_k(s) u[s] for the coset order [e, a, b, ab] (the transform is its own inverse up to 1/4,
+// and symmetric: the same butterfly gives each operation's combination of the character sums)
+template <typename R>
+__device__ __forceinline__ void wht4(const R (&u)[4], R (&W)[4])
+{
+    const R t0 = u[0] + u[1], t1 = u[0] - u[1], t2 = u[2] + u[3], t3 = u[2] - u[3];
+    W[0] = t0 + t2;
+    W[1] = t1 + t3;
+    W[2] = t0 - t2;
+    W[3] = t1 - t3;
+}
+
 template <typename R>
 struct StageLayout {
     size_t rs, tr, trm, gw, h2, cont, tab, bytes;
@@ -293,7 +325,10 @@ constexpr int kAnchorF32 = 8;
 // INV = true (FP32 tabulated and IAM models, the caller's operations as n/2 operations followed by their
 // images under an inversion at the origin, x -> -R x - t): the images' phase factors are the conjugates of their
 // partners' and their temperature factors equal, so only half the operations run the phase and exp work
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS, bool GRAD = true, bool INV = false>
+// PAT != 0 (CS = 4): the coset's operations in the order [e, a, b, ab] of that sign group, the signed sums by
+// Walsh-Hadamard transforms (wht4) instead of per-operation sign multiply-adds
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS, bool GRAD = true, bool INV = false,
+          int PAT = 0>
 __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBuffers &C, const SfLaunch &L,
                                              const SignTable &G, const int tile_rel, const int chunk)
 {
@@ -314,6 +349,8 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     constexpr bool ADIAG = CS > 0 && ANISO;
     constexpr bool XDIAG = CS > 0;
     constexpr int NSG = ADIAG ? 6 : (XDIAG ? 3 : 1);  // signed sums of u per coset
+    constexpr bool WHT = PAT != 0 && CS == 4;
+    static_assert(PAT == 0 || CS == 4, "sign-group patterns: cosets of four");
     static_assert(CS == 0 || (NSC > 0 && NSC <= 8 && NSC % CS == 0), "coset form: compiled count <= 8");
     static_assert(GRAD || !MP, "the multipole adjoint needs the derivative pass");
     static_assert(!INV || (MODEL != MODEL_HC && NSC > 0 && NSC % 2 == 0), "inversion pairs: generic models, even count");
@@ -576,7 +613,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     // XDIAG: the coset's first h' and the signed sums of u: x y z (classes 1 2 4);
                     // ADIAG adds its m6, the split quadratic form, the signed sums xy xz yz
                     // (classes 3 5 6) and plain U
-                    R hr[3] = {0, 0, 0}, m6r[ADIAG ? 6 : 1], qd = 0, qc[3] = {0, 0, 0};
+                    R hr[3] = {0, 0, 0}, m6r[ADIAG ? 6 : 1], qd = 0, qc[3] = {0, 0, 0}, qw[WHT && ADIAG ? 4 : 1];
                     R Sre[NSG], Sim[NSG], Ucre = 0, Ucim = 0;
 #pragma unroll
                     for (int q = 0; q < (ADIAG ? 6 : 1); q++) m6r[q] = R(0);
@@ -594,6 +631,14 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             qd = adp[0] * m6r[0] + adp[1] * m6r[1] + adp[2] * m6r[2];
                             qc[0] = adp[3] * m6r[3]; qc[1] = adp[4] * m6r[4]; qc[2] = adp[5] * m6r[5];
                             Ucre = R(0); Ucim = R(0);
+                            if constexpr (WHT) {
+                                // each operation's quadratic form: qd + the cross terms xy xz yz with its signs
+                                R Qp[4] = {qd, 0, 0, 0};
+                                Qp[wht_char(PAT, 3)] += qc[0];
+                                Qp[wht_char(PAT, 5)] += qc[1];
+                                Qp[wht_char(PAT, 6)] += qc[2];
+                                wht4(Qp, qw);
+                            }
                         }
                     };
                     auto adp_coset_end = [&]() {
@@ -610,6 +655,25 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     };
                     // coset form: radial-weighted class sums, even l (real part) and odd l (imaginary part)
                     R Ec[4] = {0, 0, 0, 0}, Oc[4] = {0, 0, 0, 0};  // classes 0 3 6 5 | 2 4 1 7
+                    // WHT: per position of the coset, the operations' f (HC), u and (multipole adjoint) g z
+                    R fwr[WHT ? 4 : 1], fwi[WHT ? 4 : 1], ur4[WHT ? 4 : 1], ui4[WHT ? 4 : 1];
+                    R wr4[WHT && MP ? 4 : 1], wi4[WHT && MP ? 4 : 1];
+                    // WHT (HC): each operation's f from the class sums gathered by character
+                    auto forward_wht = [&]() {
+                        if constexpr (WHT && DIAG) {
+                            constexpr int ec[4] = {0, 3, 6, 5}, oc[4] = {2, 4, 1, 7};
+                            R Ep[4] = {0, 0, 0, 0}, Op[4] = {0, 0, 0, 0}, t[4];
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                Ep[wht_char(PAT, ec[q])] += Ec[q];
+                                Op[wht_char(PAT, oc[q])] += Oc[q];
+                            }
+                            wht4(Ep, fwr);
+                            wht4(Op, t);
+#pragma unroll
+                            for (int q = 0; q < 4; q++) fwi[q] = fsim + t[q];
+                        }
+                    };
                     // with the multipole adjoint: the same class sums weighted by the kappa'
                     // derivatives of the radial terms (De, Do), and the operations' signed
                     // adjoint weights per class (We: Re(g z) of the even classes, Wo: Im(g z) of
@@ -618,6 +682,33 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     R De[DIAG && MP ? 4 : 1], Do[DIAG && MP ? 4 : 1], We[DIAG && MP ? 4 : 1], Wo[DIAG && MP ? 4 : 1];
 #pragma unroll
                     for (int k = 0; k < (DIAG && MP ? 4 : 1); k++) { De[k] = Do[k] = We[k] = Wo[k] = R(0); }
+                    // WHT: the coset's sums from its four operations' values: U (character 0), the signed sums
+                    // of u by the fractional classes x y z (xy xz yz), and the multipole adjoint's class weights
+                    auto wht_end = [&]() {
+                        if constexpr (WHT) {
+                            R Wr[4], Wi[4];
+                            wht4(ur4, Wr);
+                            wht4(ui4, Wi);
+                            Ure += Wr[0];
+                            Uim += Wi[0];
+                            constexpr int cls[6] = {1, 2, 4, 3, 5, 6};
+#pragma unroll
+                            for (int q = 0; q < NSG; q++) {
+                                Sre[q] = Wr[wht_char(PAT, cls[q])];
+                                Sim[q] = Wi[wht_char(PAT, cls[q])];
+                            }
+                            if constexpr (ADIAG) { Ucre = Wr[0]; Ucim = Wi[0]; }
+                            if constexpr (MP && DIAG) {
+                                R Vr[4], Vi[4];
+                                wht4(wr4, Vr);
+                                wht4(wi4, Vi);
+                                We[0] = Vr[0]; We[1] = Vr[wht_char(PAT, 3)]; We[2] = Vr[wht_char(PAT, 6)];
+                                We[3] = Vr[wht_char(PAT, 5)];
+                                Wo[0] = Vi[wht_char(PAT, 2)]; Wo[1] = Vi[wht_char(PAT, 4)]; Wo[2] = Vi[wht_char(PAT, 1)];
+                                Wo[3] = Vi[wht_char(PAT, 7)];
+                            }
+                        }
+                    };
                     auto mp_coset_begin = [&](const R *y, const R *dr) {
                         if constexpr (DIAG && MP) {
                             // unweighted slot sums (l, class) of the coset's first operation
@@ -731,7 +822,9 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             }
                             zre = cs; zim = sn;
                             if constexpr (ADIAG) {
-                                const R q = qd + xs(3) * qc[0] + xs(5) * qc[1] + xs(6) * qc[2];
+                                R q;
+                                if constexpr (WHT) q = qw[s & 3];
+                                else q = qd + xs(3) * qc[0] + xs(5) * qc[1] + xs(6) * qc[2];
                                 const R T = texp<R>(-q);
                                 zre *= T; zim *= T;
                             } else if constexpr (ANISO) {
@@ -771,6 +864,9 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                                 }
                                 fre = tv.x + anre; fim = tv.y + anim;
                             }
+                        } else if constexpr (DIAG && WHT) {
+                            fre = fwr[s & 3];
+                            fim = fwi[s & 3];
                         } else if constexpr (DIAG) {
                             // fsph rides in the class-0 sums (sign +1 for every operation)
                             if constexpr (F32) {
@@ -801,12 +897,17 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         }
                         const R ure = fre * zre - fim * zim;
                         const R uim = fre * zim + fim * zre;
-                        if (NSC > 0 && s == 0) {  // compile-time with a compiled operation count
+                        if constexpr (WHT) {
+                            // every sum over the coset's operations follows from these at its end (wht_end)
+                            ur4[s & 3] = ure;
+                            ui4[s & 3] = uim;
+                        } else if (NSC > 0 && s == 0) {  // compile-time with a compiled operation count
                             Ure = ure; Uim = uim;
                         } else {
                             Ure += ure; Uim += uim;
                         }
-                        if constexpr (XDIAG) {
+                        if constexpr (WHT) {
+                        } else if constexpr (XDIAG) {
                             // signed sums: x y z -> slots 0 1 2 (classes 1 2 4), xy xz yz -> 3 4 5 (3 5 6);
                             // the coset's first operation has every sign +1 (s is a compile-time index here)
                             const bool first = s % (CS > 0 ? CS : 1) == 0;
@@ -838,8 +939,13 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                                 const auto sg = [&](int c) -> R {
                                     if constexpr (F32) return G.f[s][c]; else return G.d[s][c];
                                 };
+                                if constexpr (WHT) {
+                                    wr4[s & 3] = wre;
+                                    wi4[s & 3] = wim;
+                                } else {
                                 We[0] += wre; We[1] += sg(3) * wre; We[2] += sg(6) * wre; We[3] += sg(5) * wre;
                                 Wo[0] += sg(2) * wim; Wo[1] += sg(4) * wim; Wo[2] += sg(1) * wim; Wo[3] += sg(7) * wim;
+                                }
                             } else {
                                 const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
                                 Ere += zre; Eim += zim;
@@ -866,17 +972,20 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             if constexpr (CS > 0) {
                                 if (s % CS == 0) {
                                     if (s > 0) {
+                                        wht_end();
                                         flush_slots(recs[s - CS].y, sTrm + (size_t)(lt * ht + hl) * 8);
                                         adp_coset_end();
                                     }
                                     class_sums(recs[s].y);
                                     mp_coset_begin(recs[s].y, sTrm + (size_t)(lt * ht + hl) * 8);
+                                    forward_wht();
                                     adp_coset_begin(recs[s]);
                                 }
                             }
                             term(s);
                         }
                         if constexpr (CS > 0) {
+                            wht_end();
                             flush_slots(recs[NSC - CS].y, sTrm + (size_t)(lt * ht + hl) * 8);
                             adp_coset_end();
                         }
@@ -996,27 +1105,29 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 }
 
 // one structure: block (tile, reflection chunk)
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true, bool INV = false>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true, bool INV = false,
+          int PAT = 0>
 __global__ void __launch_bounds__(kTileAtoms)
 sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 {
-    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD, INV>(S, C, L, G, blockIdx.x, blockIdx.y);
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD, INV, PAT>(S, C, L, G, blockIdx.x, blockIdx.y);
 }
 
 // the same with at least four blocks per SM: the tabulated model with up to
 // four compiled operations (HBM streaming: occupancy over registers).  The
 // other kernels keep the compiler's own register choice, which an explicit
 // minimum of one block would change.
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true, bool INV = false>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true, bool INV = false,
+          int PAT = 0>
 __global__ void __launch_bounds__(kTileAtoms, 4)
 sf_grad_kernel3_occ4(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
 {
-    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD, INV>(S, C, L, G, blockIdx.x, blockIdx.y);
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD, INV, PAT>(S, C, L, G, blockIdx.x, blockIdx.y);
 }
 
 // many structures of one kernel shape (and one sign table) in one launch: the
 // block's item is the last with block_begin <= blockIdx.x
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS, bool INV>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS, bool INV, int PAT = 0>
 __device__ __forceinline__ void sf_grad_batch_body(const SfBatch &B, const SignTable &G)
 {
     const int b = blockIdx.x;
@@ -1028,21 +1139,22 @@ __device__ __forceinline__ void sf_grad_batch_body(const SfBatch &B, const SignT
     }
     const SfBatchItem &it = B.item[lo];
     const int lb = b - B.block_begin[lo];
-    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, true, INV>(it.S, it.C, it.L, G, lb % it.n_tiles, lb / it.n_tiles);
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, true, INV, PAT>(it.S, it.C, it.L, G, lb % it.n_tiles,
+                                                               lb / it.n_tiles);
 }
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool INV = false>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool INV = false, int PAT = 0>
 __global__ void __launch_bounds__(kTileAtoms)
 sf_grad_batch3(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
 {
-    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS, INV>(B, G);
+    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS, INV, PAT>(B, G);
 }
 
-template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool INV = false>
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool INV = false, int PAT = 0>
 __global__ void __launch_bounds__(kTileAtoms, 4)
 sf_grad_batch3_occ4(const __grid_constant__ SfBatch B, const __grid_constant__ SignTable G)
 {
-    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS, INV>(B, G);
+    sf_grad_batch_body<R, MODEL, MP, ANISO, NSC, CS, INV, PAT>(B, G);
 }
 
 // kernels that take the four-block minimum: FP32 tabulated, form factors in registers

@@ -95,7 +95,11 @@ typedef struct dsf_ticket dsf_ticket;
  * engine's representation) or any operation list with centrosymmetric = 0
  * (e.g. all operations modulo centering: the generic AnyScatterer
  * representation).  Lattice centering enters as the per-reflection
- * multiplier of scattering_utilities::centeringSfMultipliers. */
+ * multiplier of scattering_utilities::centeringSfMultipliers.  With the
+ * inversion taken by the engine, anomalous dispersion enters as the
+ * reference's centrosymmetric engine takes it (F = U + c conj(U) with U the
+ * sum over the listed operations, HansenCoppens_SF_Engine3.cpp:1920-1935);
+ * the all-operations form sums f' + i f'' over every operation. */
 typedef struct {
     double cell[6];                   /* a b c [A], alpha beta gamma [deg] */
     int n_symops;

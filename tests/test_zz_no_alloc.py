@@ -93,7 +93,6 @@ CASES = [("iam_it92", "all"),                       # the generic engine's opera
 def test_noalloc_matches_allocating_entry_point(engine, name, rep, precision):
     torch = pytest.importorskip("torch")
     from discamb_gb300 import api
-    from oracle import oracle as O
     st, iam, d = _case(name)
     ref = api.IamCalculator(engine, st, iam, representation=rep).calculate(st.dtdf, precision=precision)
     sym, keep_sym = api.symmetry_desc(st, rep)
@@ -103,11 +102,13 @@ def test_noalloc_matches_allocating_entry_point(engine, name, rep, precision):
     n, m = st.n_atoms, st.n_hkl
     nadp = st.n_adp()
     tf, tg = TOL[precision]
-    # the reference's own result (fixture), else the oracle's
+    # and the reference's own result where the fixture holds one.  The shifted-inversion case has none: with
+    # the inversion taken by the engine, anomalous dispersion enters as the reference's centrosymmetric engine
+    # takes it (F = U + c conj(U), HansenCoppens_SF_Engine3.cpp:1920-1935), which differs from the sum over
+    # all operations by design; the allocating call with the same descriptor is its check
+    golds = [ref]
     if d is not None:
-        gold = dict(f=d["ref_f"], d_xyz=d["ref_d_xyz"], d_adp=ref_adp_list(st, d), d_occ=d["ref_d_occ"])
-    else:
-        gold = O.compute(st, model="iam", iam=iam, n_threads=2)
+        golds.append(dict(f=d["ref_f"], d_xyz=d["ref_d_xyz"], d_adp=ref_adp_list(st, d), d_occ=d["ref_d_occ"]))
     err = C.create_string_buffer(256)
     # outputs allocated before the first call: the second call must leave the device's free memory unchanged
     outs = []
@@ -138,7 +139,7 @@ def test_noalloc_matches_allocating_entry_point(engine, name, rep, precision):
         gaa = o["d_adp"].cpu().numpy()
         r = dict(f=fz, d_xyz=o["d_xyz"].cpu().numpy(), d_adp=[gaa[i, :nadp[i]] for i in range(n)],
                  d_occ=o["d_occ"].cpu().numpy())
-        for against in (ref, gold):
+        for against in golds:
             assert rel_f(r["f"], against["f"]) < tf, (call, rel_f(r["f"], against["f"]))
             for k in ("d_xyz", "d_adp", "d_occ"):
                 assert rel_norm(r[k], against[k]) < tg, (call, k, rel_norm(r[k], against[k]))
