@@ -641,6 +641,9 @@ def run_gpu(args):
         step_ms = [a.elapsed_time(b) for a, b in ev]
         return step_ms, kern, launches, wall
 
+    # the tile shape: the autotuner times a few candidates on this structure (set-up, outside the timed region)
+    tuned = calc.autotune(api.DSF_FP32_BULK, multipoles=mpd) if args.autotune else None
+    shape = calc.tile_shape(api.DSF_FP32_BULK, multipoles=mpd)
     with ClockSampler(device) as clk:
         ms32, kern32, launches32, wall32 = timed_device(api.DSF_FP32_BULK, args.steps, args.warmup)
     clocks = clk.summary()
@@ -724,6 +727,10 @@ def run_gpu(args):
         "gpu_launches": launches32,
         "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
         "wall_s_timed_region": wall32,
+        "tile_shape": {"blocks_per_sm": shape["blocks_per_sm"], "ht": shape["ht"] or "longest",
+                       "source": "autotuner (dsf_autotune over 8 candidates at set-up)" if shape["tuned"]
+                       else "rule (75 blocks per SM, longest sub-tile)",
+                       "tuned_ms": tuned["ms"] if tuned else None},
     }
     calc.close()
     eng.close()
@@ -761,6 +768,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the rule's tile shape instead of tuning it at set-up")
     ap.add_argument("--no-served", dest="served", action="store_false",
                     help="config2: skip the served stream (config3) attached to the line")
     ap.add_argument("--c4-crystals", type=int, default=256)

@@ -82,6 +82,10 @@ struct dsf_engine {
     // batched launches alternate between the call's stream and this one (under the batch launch lock)
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // tile shapes chosen by the autotuner, per shape key (tune_key): blocks per SM the reflection chunks
+    // aim at, and the sub-tile length (0: the longest the shared-memory budget allows)
+    std::map<std::string, std::pair<int, int> > tuned;
+    std::mutex tune_mtx;
 };
 
 namespace {
@@ -209,6 +213,7 @@ struct dsf_structure {
     int coset_size = 0;
     int inv_pairs = 0;  // generic models: operations n/2 .. n-1 are the images of 0 .. n/2-1 under -1 at the origin
     int debug_stall = 0;  // dsf_debug_stall_next_call: the next call's kernel waits run out (timeout test)
+    int tune_bps = 0, tune_ht = 0;  // the autotuner's candidate for this structure's next calls (0: none)
     int pending = 0;      // a dsf_submit call of this structure not yet completed by dsf_poll
     std::vector<int> sym_sign;   // [n_sym][3] Cartesian
     std::vector<int> sym_fsign;  // [n_sym][3] fractional h' components
@@ -577,8 +582,8 @@ void order_cosets_as_sign_group(dsf_structure *s)
 }
 
 // the sign-group pattern of a launch's sign table: cosets of four whose every operation gives every parity
-// class (harmonic and fractional) the sign of the pattern's character at its position, else 0
-int wht_pattern_of(const SignTable &G, int n_sym, int coset)
+// class (fractional, and for the HC model harmonic) the sign of the pattern's character at its position, else 0
+int wht_pattern_of(const SignTable &G, int n_sym, int coset, bool harmonics)
 {
     if (coset != 4 || n_sym % 4 != 0) return 0;
     for (const int pat : {kPatD2, kPatC2hB}) {
@@ -588,7 +593,7 @@ int wht_pattern_of(const SignTable &G, int n_sym, int coset)
             for (int c = 0; c < 8 && ok; c++) {
                 const int k = wht_char(pat, c);
                 const float want = (((k & 1) & (j & 1)) ^ (((k >> 1) & 1) & (j >> 1))) ? -1.0f : 1.0f;
-                ok = G.f[op][c] == want && G.xf[op][c] == want;
+                ok = (!harmonics || G.f[op][c] == want) && G.xf[op][c] == want;
             }
         }
         if (ok) return pat;
@@ -1946,7 +1951,7 @@ static void call_buffers(dsf_structure *s, bool fp64, CallBuffers &C, SfLaunch &
 // shared-memory budget (several blocks per SM), reflection chunks of about
 // `block_terms` atom x reflection pairs per block (at least four sub-tiles)
 static int kind_shape(dsf_structure *s, int kind, bool fp64, bool mp, double block_terms, SfLaunch &L, int &nt,
-                      int &n_chunks, size_t &smem)
+                      int &n_chunks, size_t &smem, int ht_cap = 0)
 {
     dsf_engine *e = s->eng;
     const int t0 = kind ? s->n_tiles_plain : 0, t1 = kind ? s->n_tiles : s->n_tiles_plain;
@@ -1961,6 +1966,7 @@ static int kind_shape(dsf_structure *s, int kind, bool fp64, bool mp, double blo
     // the staged FP32 table dominates the stage: a smaller budget keeps four blocks per SM
     if (table && !fp64) budget = std::min<size_t>(budget, 64 * 1024);
     while (ht > 4 && sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types, table) > budget) ht /= 2;
+    while (ht_cap >= 4 && ht > ht_cap) ht /= 2;
     smem = sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types, table);
     if (smem > e->max_smem) return fail(e, DSF_ERR_UNSUPPORTED, "shared-memory tile does not fit this device");
     L.ht = ht;
@@ -2006,10 +2012,47 @@ static int call_post(dsf_structure *s, int flags, const dsf_outputs *out, cudaSt
 // blocks of unequal tiles even out across the SMs, but at least 256 reflections (16 sub-tiles) per block so the
 // per-block set-up (atom loads, the final derivative commits) stays small -- unless that leaves fewer than four
 // blocks per SM (small structures)
-static int chunk_count(const dsf_engine *e, int ntk, int n_hkl)
+static int chunk_count(const dsf_engine *e, int ntk, int n_hkl, int blocks_per_sm = 75)
 {
     const int sm = std::max(1, e->n_sm), t = std::max(1, ntk);
-    return std::max(1, std::max(std::min(sm * 75 / t, n_hkl / 256), sm * 4 / t));
+    return std::max(1, std::max(std::min(sm * blocks_per_sm / t, n_hkl / 256), sm * 4 / t));
+}
+
+// ---------------------------------------------------------------------------
+// tile-shape autotuner: per shape key, the blocks per SM the reflection chunks
+// aim at and the sub-tile length, chosen by timing a few candidates
+// ---------------------------------------------------------------------------
+static int log2_bucket(double x) { return x > 1 ? (int)std::lround(2.0 * std::log2(x)) : 0; }
+
+// the shape a structure's call depends on: model, precision, multipole adjoint, derivative pass, operation
+// count, coset form, atoms and reflections in half-octaves, the device's SM count
+static std::string tune_key(const dsf_structure *s, bool fp64, bool mp, bool grad)
+{
+    char k[160];
+    std::snprintf(k, sizeof k, "m%d-p%d-mp%d-g%d-ns%d-cs%d-iv%d-a%d-h%d-sm%d", s->model, fp64 ? 64 : 32, mp ? 1 : 0,
+                  grad ? 1 : 0, s->n_sym, s->coset_size, s->inv_pairs, log2_bucket(s->n_atoms),
+                  log2_bucket(s->n_hkl), s->eng->n_sm);
+    return k;
+}
+
+// blocks per SM and sub-tile cap of a call: the autotuner's candidate under trial, else the tuned shape of the
+// key, else the rule (75 blocks per SM, the longest sub-tile)
+static void call_shape(dsf_structure *s, bool fp64, bool mp, bool grad, int &bps, int &ht)
+{
+    bps = 75;
+    ht = 0;
+    if (s->tune_bps > 0) {
+        bps = s->tune_bps;
+        ht = s->tune_ht;
+        return;
+    }
+    dsf_engine *e = s->eng;
+    std::lock_guard<std::mutex> lock(e->tune_mtx);
+    auto it = e->tuned.find(tune_key(s, fp64, mp, grad));
+    if (it != e->tuned.end()) {
+        bps = it->second.first;
+        ht = it->second.second;
+    }
 }
 
 // the inversion-pair kernels: FP32 generic models (tabulated, IAM) with a compiled operation count
@@ -2058,6 +2101,9 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         DSF_CUDA(cudaEventCreate(&s->ev_begin));
         DSF_CUDA(cudaEventCreate(&s->ev_end));
     }
+    const bool grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
+    int bps, ht_cap;
+    call_shape(s, fp64, mp, grad, bps, ht_cap);
     DSF_CUDA(cudaEventRecord(s->ev_begin, st));
     // one launch per ADP kind (tiles [0, n_tiles_plain) without anisotropic ADPs), reflection chunks of
     // chunk_count
@@ -2065,9 +2111,9 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         int nt, n_chunks;
         size_t smem;
         const int ntk = kind ? s->n_tiles - s->n_tiles_plain : s->n_tiles_plain;
-        const int n_chunks0 = chunk_count(e, ntk, s->n_hkl);
+        const int n_chunks0 = chunk_count(e, ntk, s->n_hkl, bps);
         const double block_terms = (double)kTileAtoms * ((s->n_hkl + n_chunks0 - 1) / n_chunks0);
-        if ((rc = kind_shape(s, kind, fp64, mp, block_terms, L, nt, n_chunks, smem))) return rc;
+        if ((rc = kind_shape(s, kind, fp64, mp, block_terms, L, nt, n_chunks, smem, ht_cap))) return rc;
         if (nt <= 0) continue;
         K3Args A;
         A.S = &s->dev;
@@ -2076,12 +2122,12 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         A.G = &G;
         A.n_sym = s->n_sym;
         A.coset = L.coset;
-        A.pattern = wht_pattern_of(G, s->n_sym, L.coset);
+        A.pattern = wht_pattern_of(G, s->n_sym, L.coset, s->model == MODEL_HC);
         A.n_tiles = nt;
         A.n_chunks = n_chunks;
         A.smem = smem;
         A.st = st;
-        A.grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
+        A.grad = grad;
         A.inv = inv_kernel(s, fp64);
         DSF_CUDA(launch_sf3(A, s->model, fp64, mp, kind == 1));
         launches++;
@@ -2089,6 +2135,129 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
     DSF_CUDA(cudaEventRecord(s->ev_end, st));
     if ((rc = call_post(s, flags, out, st, launches))) return rc;
     s->last_launches = launches;
+    return DSF_OK;
+}
+
+// Times the structure's call over a few tile shapes (reflection chunks aiming at 24, 48, 75 or 150 blocks per
+// SM; the longest sub-tile the shared-memory budget allows, or at most 8 reflections) with a zero dT/dF on scratch
+// buffers, and keeps the fastest for every later call of structures with the same shape key.  Any shape gives
+// the same sums (the cross-block sums in another order).
+int dsf_autotune(dsf_structure *s, int precision, int flags, int *blocks_per_sm, int *ht, double *best_ms)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    if (precision != DSF_FP64 && precision != DSF_FP32_BULK) return fail(e, DSF_ERR_ARGUMENT, "unknown precision");
+    if (s->n_hkl == 0) return fail(e, DSF_ERR_STATE, "no reflections to tune on");
+    cudaSetDevice(e->device);
+    const bool fp64 = precision == DSF_FP64;
+    const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
+    const bool grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
+    const size_t n = (size_t)s->n_atoms, m = (size_t)s->n_hkl;
+    const size_t doubles = 2 * m + 2 * m + n * (3 + 6 + 1) + (mp ? n * 28 : 0);
+    double *buf = nullptr;
+    DSF_CUDA(cudaMalloc(&buf, sizeof(double) * doubles));
+    DSF_CUDA(cudaMemsetAsync(buf, 0, sizeof(double) * doubles, e->stream));
+    dsf_outputs out{};
+    double *p = buf + 2 * m;  // buf[0, 2m): dT/dF = 0
+    out.f = p; p += 2 * m;
+    out.d_xyz = p; p += 3 * n;
+    out.d_adp = p; p += 6 * n;
+    out.d_occ = p; p += n;
+    if (mp) {
+        out.d_pval = p; p += n;
+        out.d_plm = p; p += 25 * n;
+        out.d_kappa = p; p += n;
+        out.d_kappa_prime = p;
+    }
+    int rc = DSF_OK;
+    auto timed = [&](int bps, int cap, double &ms) {
+        s->tune_bps = bps;
+        s->tune_ht = cap;
+        rc = dsf_calculate_device(s, precision, flags, buf, &out, e->stream);
+        s->tune_bps = s->tune_ht = 0;
+        if (rc) return false;
+        if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
+            rc = fail(e, DSF_ERR_CUDA, "autotune call failed");
+            return false;
+        }
+        ms = dsf_last_kernel_ms(s);
+        return ms >= 0;
+    };
+    double warm = 0, best = 1e300;
+    int best_bps = 75, best_cap = 0;
+    if (timed(75, 0, warm)) {
+        const int reps = warm < 20.0 ? 3 : 1;
+        for (const int bps : {24, 48, 75, 150})
+            for (const int cap : {0, 8}) {
+                double t = 1e300;
+                for (int r = 0; r < reps; r++) {
+                    double ms;
+                    if (!timed(bps, cap, ms)) break;
+                    t = std::min(t, ms);
+                }
+                if (rc) break;
+                if (t < best) {
+                    best = t;
+                    best_bps = bps;
+                    best_cap = cap;
+                }
+            }
+    }
+    cudaFree(buf);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> lock(e->tune_mtx);
+        e->tuned[tune_key(s, fp64, mp, grad)] = {best_bps, best_cap};
+    }
+    if (blocks_per_sm) *blocks_per_sm = best_bps;
+    if (ht) *ht = best_cap;
+    if (best_ms) *best_ms = best;
+    return DSF_OK;
+}
+
+// the tile shape the next call of s with these settings takes (tuned, or the rule's 75 blocks per SM and the
+// longest sub-tile, ht = 0); *tuned = 1 when it comes from the autotuner
+int dsf_tuning_lookup(dsf_structure *s, int precision, int flags, int *blocks_per_sm, int *ht, int *tuned)
+{
+    if (!s) return DSF_ERR_ARGUMENT;
+    dsf_engine *e = s->eng;
+    const bool fp64 = precision == DSF_FP64;
+    const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
+    const bool grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
+    std::lock_guard<std::mutex> lock(e->tune_mtx);
+    auto it = e->tuned.find(tune_key(s, fp64, mp, grad));
+    const bool hit = it != e->tuned.end();
+    if (blocks_per_sm) *blocks_per_sm = hit ? it->second.first : 75;
+    if (ht) *ht = hit ? it->second.second : 0;
+    if (tuned) *tuned = hit ? 1 : 0;
+    return DSF_OK;
+}
+
+// the tuned shapes as text, one "key blocks_per_sm ht" line each
+int dsf_tuning_save(dsf_engine *e, const char *path)
+{
+    if (!e || !path) return DSF_ERR_ARGUMENT;
+    FILE *f = std::fopen(path, "w");
+    if (!f) return fail(e, DSF_ERR_ARGUMENT, "cannot write the tuning file");
+    std::lock_guard<std::mutex> lock(e->tune_mtx);
+    for (const auto &kv : e->tuned) std::fprintf(f, "%s %d %d\n", kv.first.c_str(), kv.second.first, kv.second.second);
+    std::fclose(f);
+    return DSF_OK;
+}
+
+// adds the shapes of a file written by dsf_tuning_save (keys name the device's SM count, so shapes tuned on
+// another kind of device are never matched)
+int dsf_tuning_load(dsf_engine *e, const char *path)
+{
+    if (!e || !path) return DSF_ERR_ARGUMENT;
+    FILE *f = std::fopen(path, "r");
+    if (!f) return fail(e, DSF_ERR_ARGUMENT, "cannot read the tuning file");
+    char key[160];
+    int bps, ht;
+    std::lock_guard<std::mutex> lock(e->tune_mtx);
+    while (std::fscanf(f, "%159s %d %d", key, &bps, &ht) == 3)
+        if (bps > 0 && bps <= 4096 && ht >= 0 && ht <= kMaxHT) e->tuned[key] = {bps, ht};
+    std::fclose(f);
     return DSF_OK;
 }
 
@@ -2222,7 +2391,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
                 A.G = &G;
                 A.n_sym = s->n_sym;
                 A.coset = L.coset;
-                A.pattern = wht_pattern_of(G, s->n_sym, L.coset);
+                A.pattern = wht_pattern_of(G, s->n_sym, L.coset, s->model == MODEL_HC);
                 A.n_tiles = nt;
                 A.n_chunks = n_chunks;
                 A.smem = smem;
@@ -2300,7 +2469,7 @@ int dsf_calculate_batch_device(dsf_structure *const *structures, int n, int prec
             A.G = &g.G;
             A.n_sym = g.n_sym;
             A.coset = g.coset;
-            A.pattern = wht_pattern_of(g.G, g.n_sym, g.coset);
+            A.pattern = wht_pattern_of(g.G, g.n_sym, g.coset, g.model == MODEL_HC);
             A.inv = g.inv;
             A.blocks = blocks;
             A.smem = g.smem;
