@@ -514,25 +514,26 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     }
 
     // TAB_REG: form factors of the current and the next group of four reflections
-    float2 tab_cur[TAB_REG ? 4 * NR : 1], tab_next[TAB_REG ? 4 * NR : 1];
+    constexpr int kTabN = TAB_REG ? 4 * NR : 1;
+    float2 tab_a[kTabN], tab_b[kTabN];
     const float2 *tab_col = nullptr;
     if constexpr (TAB_REG) {
         // a tile's columns are contiguous (tiles do not straddle table_split)
         tab_col = S.table_f + (a + (a >= S.table_split ? S.table_shift : 0));
 #pragma unroll
-        for (int q = 0; q < 4 * NR; q++) tab_cur[q] = tab_next[q] = make_float2(0.f, 0.f);
+        for (int q = 0; q < 4 * NR; q++) tab_a[q] = tab_b[q] = make_float2(0.f, 0.f);
     }
     // rows hg .. hg + 3 (below n_hkl_pad for every group that starts before h_end)
-    auto tab_load = [&](int hg) {
+    auto tab_load = [&](float2 (&dst)[kTabN], int hg) {
         if constexpr (TAB_REG) {
             if (have && hg < h_end) {
 #pragma unroll
                 for (int q = 0; q < 4 * NR; q++)
-                    tab_next[q] = __ldcs(tab_col + ((size_t)hg * NR + q) * S.table_stride);
+                    dst[q] = __ldcs(tab_col + ((size_t)hg * NR + q) * S.table_stride);
             }
         }
     };
-    tab_load(h_begin);
+    tab_load(tab_a, h_begin);
 
     if (tid == 0 && !L.stall_first) issue(0, h_begin);
     uint32_t parity[2] = {0u, 0u};
@@ -568,12 +569,10 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 
         // reflections in groups of four: the partial F of a group is reduced across
         // the warp by one butterfly reduce-scatter of its eight values
-        for (int g0 = 0; g0 < ht; g0 += 4) {
-            if constexpr (TAB_REG) {
-#pragma unroll
-                for (int q = 0; q < 4 * NR; q++) tab_cur[q] = tab_next[q];
-                tab_load(h0 + g0 + 4);
-            }
+        // one group of four reflections; TAB_REG: its form factors in `cur` while the next group's load into
+        // `nxt` (two buffers taking turns, so no copy between groups)
+        auto group = [&](const int g0, float2 (&cur)[kTabN], float2 (&nxt)[kTabN]) {
+            if constexpr (TAB_REG) tab_load(nxt, h0 + g0 + 4);
             R Fv[8];
 #pragma unroll
             for (int q = 0; q < 8; q++) Fv[q] = R(0);
@@ -801,11 +800,15 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         const auto xs = [&](int c) -> R {
                             if constexpr (F32) return G.xf[s][c]; else return G.xd[s][c];
                         };
-                        if (INV && s >= NR / 2) {
+                        bool image = false;
+                        if constexpr (INV) image = s >= NR / 2;
+                        if (image) {
                             // the inversion image of operation s - n/2 (inversion at the origin): h' -> -h',
                             // the same translation sign-reversed, so the conjugate phase and the same T
-                            zre = zT_re[INV ? s - NR / 2 : 0];
-                            zim = -zT_im[INV ? s - NR / 2 : 0];
+                            if constexpr (INV) {
+                                zre = zT_re[s - NR / 2];
+                                zim = -zT_im[s - NR / 2];
+                            }
                         } else {
                             R cs, sn;
                             if constexpr (REC) {
@@ -845,7 +848,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             // the table holds n_hkl_pad rows (zero past the last reflection), columns in
                             // the engine's atom order (consecutive lanes read consecutive values)
                             if constexpr (TAB_REG) {
-                                const float2 tv = tab_cur[j * NR + s];
+                                const float2 tv = cur[j * NR + s];
                                 fre = tv.x + anre; fim = tv.y + anim;
                             } else if constexpr (F32) {
                                 const float2 tv = reinterpret_cast<const float2 *>(st + SL.tab)[
@@ -1053,20 +1056,35 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                 R *dst = reinterpret_cast<R *>(&sF[warp * ht + g0 + (idx >> 1)]);
                 dst[idx & 1] = v1;
             }
+            };
+        if constexpr (TAB_REG) {
+            int g0 = 0;
+            for (; g0 + 8 <= ht; g0 += 8) {
+            group(g0, tab_a, tab_b);
+            group(g0 + 4, tab_b, tab_a);
+            }
+            if (g0 < ht) {  // an odd group count (sub-tiles of four reflections)
+            group(g0, tab_a, tab_b);
+#pragma unroll
+            for (int q = 0; q < kTabN; q++) tab_a[q] = tab_b[q];
+            }
+        } else {
+#pragma unroll 1
+            for (int g0 = 0; g0 < ht; g0 += 4) group(g0, tab_a, tab_b);
         }
         // fold the partial sums into the Kahan totals (each thread its own column;
         // isotropic tiles use one ADP channel of six)
         if (GRAD && ((k + 1) % fold == 0 || h0 + ht >= h_end)) {
 #pragma unroll
             for (int q = 0; q < NT; q++) {
-                if (!ANISO && q > CH_ADP && q < CH_OCC) continue;
-                R sum = sTot[q * kTileAtoms + tid], comp = sCmp[q * kTileAtoms + tid];
-                const R yv = part[q] - comp;
-                const R tv = sum + yv;
-                comp = (tv - sum) - yv;
-                sTot[q * kTileAtoms + tid] = tv;
-                sCmp[q * kTileAtoms + tid] = comp;
-                part[q] = R(0);
+            if (!ANISO && q > CH_ADP && q < CH_OCC) continue;
+            R sum = sTot[q * kTileAtoms + tid], comp = sCmp[q * kTileAtoms + tid];
+            const R yv = part[q] - comp;
+            const R tv = sum + yv;
+            comp = (tv - sum) - yv;
+            sTot[q * kTileAtoms + tid] = tv;
+            sCmp[q * kTileAtoms + tid] = comp;
+            part[q] = R(0);
             }
         }
         __syncthreads();
@@ -1074,9 +1092,9 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             R sre = 0, sim = 0;
 #pragma unroll
             for (int wp = 0; wp < kWarps; wp++) {
-                const R2 v = sF[wp * ht + i];
-                sre += v.x;
-                sim += v.y;
+            const R2 v = sF[wp * ht + i];
+            sre += v.x;
+            sim += v.y;
             }
             atomicAdd(&C.f_acc[h0 + i].x, (double)sre);
             atomicAdd(&C.f_acc[h0 + i].y, (double)sim);
