@@ -66,7 +66,7 @@ WORKLOADS = {
                                  "hkl log-uniform 1k-300k, P1/P-1/P21/P21c/P212121/C2c, HC l<=4, aniso U, "
                                  "dF/d(xyz,U,occ)"),
     "config2": dict(seed=2, multipoles=True, flops=195, fp64_steps=1, fp64_warmup=0, cpu_frac=0.002,
-                    traffic_key="sf_grad_kernel3<float,HC,MP,ANISO,8,CS4>@config2",
+                    traffic_key="sf_grad_kernel3<float,HC,MP,ANISO,8,CS4,PAT_D2>@config2",
                     desc="config2: HC multipoles l<=4, 50000 atoms (300 types), P43212, all hkl d>=1.2A, aniso U "
                          "(H iso), dF/d(xyz,U,occ,Pv,Plm,kappa,kappa')"),
 }

@@ -515,6 +515,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 
     // TAB_REG: form factors of the current and the next group of four reflections
     constexpr int kTabN = TAB_REG ? 4 * NR : 1;
+    constexpr int kTabPrefetchGroups = 4;  // L2 prefetch distance of the register-loaded table (groups of four)
     float2 tab_a[kTabN], tab_b[kTabN];
     const float2 *tab_col = nullptr;
     if constexpr (TAB_REG) {
@@ -533,7 +534,24 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             }
         }
     };
-    tab_load(tab_a, h_begin);
+    // L2 prefetch of the table rows kTabPrefetchGroups groups of four reflections ahead of the register loads: the
+    // tile's columns of every (reflection, operation) row (one bulk prefetch per row by lanes of warp 0), so the
+    // per-thread loads one group ahead find them in L2 instead of waiting on HBM (the registers hold only one
+    // group in flight)
+    auto tab_prefetch_l2 = [&](int hg) {
+        if constexpr (TAB_REG) {
+            const int q = lane;
+            if (warp == 0 && q < 4 * NR && hg + q / NR < h_end) {
+                const int col0 = a_begin + (a_begin >= S.table_split ? S.table_shift : 0);
+                const uint32_t bytes = (uint32_t)((sizeof(float2) * (a_end - a_begin) + 15) & ~(size_t)15);
+                const float2 *row = S.table_f + ((size_t)hg * NR + q) * S.table_stride + col0;
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(row), "r"(bytes) : "memory");
+            }
+        }
+    };
+    tab_load(tab_b, h_begin);
+#pragma unroll
+    for (int gp = 1; gp <= kTabPrefetchGroups; gp++) tab_prefetch_l2(h_begin + 4 * gp);
 
     if (tid == 0 && !L.stall_first) issue(0, h_begin);
     uint32_t parity[2] = {0u, 0u};
@@ -1056,17 +1074,17 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                 R *dst = reinterpret_cast<R *>(&sF[warp * ht + g0 + (idx >> 1)]);
                 dst[idx & 1] = v1;
             }
-            };
+        };
         if constexpr (TAB_REG) {
-            int g0 = 0;
-            for (; g0 + 8 <= ht; g0 += 8) {
-            group(g0, tab_a, tab_b);
-            group(g0 + 4, tab_b, tab_a);
-            }
-            if (g0 < ht) {  // an odd group count (sub-tiles of four reflections)
-            group(g0, tab_a, tab_b);
+            // the group's form factors (loaded one group ahead) move to `tab_a`; `group` loads the next group's
+            // into `tab_b`.  (Two buffers taking turns without the copy spill the anisotropic kernels under the
+            // four-block register cap.)
+#pragma unroll 1
+            for (int g0 = 0; g0 < ht; g0 += 4) {
 #pragma unroll
-            for (int q = 0; q < kTabN; q++) tab_a[q] = tab_b[q];
+                for (int q = 0; q < kTabN; q++) tab_a[q] = tab_b[q];
+                tab_prefetch_l2(h0 + g0 + 4 * (1 + kTabPrefetchGroups));
+                group(g0, tab_a, tab_b);
             }
         } else {
 #pragma unroll 1
