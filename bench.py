@@ -389,10 +389,53 @@ def run_config3(args):
         "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
         "wall_s_timed_region": t_end - t0,
     }
-    print(json.dumps(line))
     srv.close()
+    if args.c3_burst > 0:
+        line["burst"] = config3_burst(args, eng, api, serve, sts, terms, factory)
+    print(json.dumps(line))
     eng.close()
     return 0
+
+
+def config3_burst(args, eng, api, serve, sts, terms, factory):
+    """The served stream's scheduler under pressure: the five cycles of the
+    first `--c3-burst` structures submitted at once (all clients arrive
+    together) to a server whose device-memory budget (`--c3-burst-hbm-gb`)
+    holds only part of them, so requests batch up to 48 per round and idle
+    structures are evicted to admit the next."""
+    n_st = min(args.c3_burst, len(sts))
+    budget = int(args.c3_burst_hbm_gb * (1 << 30))
+    run_batch = serve.batch_executor(eng, precision=api.DSF_FP32_BULK)
+    srv = serve.SfServer(run_batch, budget, max_batch=48)
+    est = [serve.estimate_device_bytes(st.n_atoms, st.n_hkl, len(st.sg.subset_rot), len(st.types))
+           for st in sts[:n_st]]
+    for i in range(n_st):
+        srv.add_structure(i, lambda st=sts[i]: factory(st), est[i])
+    rng = np.random.default_rng(44)
+    cycles = [[_perturbed_cycle(sts[i], rng) for _ in range(5)] for i in range(n_st)]
+    srv.start()
+    t0 = time.perf_counter()
+    reqs = []
+    for c in range(5):
+        for i in range(n_st):
+            xyz, adp, occ = cycles[i][c]
+            reqs.append(srv.submit(serve.Request(key=i, xyz=xyz, adp=adp, occupancy=occ, dtdf=sts[i].dtdf)))
+    for q in reqs:
+        q.done.wait()
+    span = time.perf_counter() - t0
+    srv.stop()
+    lat = np.array([q.latency for q in reqs]) * 1e3
+    out = {"structures": n_st, "requests": len(reqs), "hbm_budget_gb": args.c3_burst_hbm_gb,
+           "sum_of_structure_bytes_gb": sum(est) / (1 << 30),
+           "value": 5 * sum(terms[:n_st]) / span, "unit": "terms/s", "span_ms": span * 1e3,
+           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max())},
+           "mean_batch": float(np.mean(srv.batch_sizes)) if srv.batch_sizes else 0.0,
+           "max_batch": max(srv.batch_sizes) if srv.batch_sizes else 0, "rounds": srv.rounds,
+           "admissions": srv.admissions, "evictions": srv.evictions,
+           "errors": sum(1 for q in reqs if q.error)}
+    srv.close()
+    return out
 
 
 def run_config3_reference(args, sts, terms):
@@ -728,7 +771,8 @@ def run_gpu(args, served=None):
         "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
         "wall_s_timed_region": wall32,
         "tile_shape": {"blocks_per_sm": shape["blocks_per_sm"], "ht": shape["ht"] or "longest",
-                       "source": "autotuner (dsf_autotune over 8 candidates at set-up)" if shape["tuned"]
+                       "register_cap_blocks_per_sm": shape["occupancy"] or "compiler's",
+                       "source": "autotuner (dsf_autotune at set-up)" if shape["tuned"]
                        else "rule (75 blocks per SM, longest sub-tile)",
                        "tuned_ms": tuned["ms"] if tuned else None},
     }
@@ -753,7 +797,7 @@ def served_stream(args):
         rec = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
     except Exception as exc:  # the headline stands without it; say why
         return {"error": f"config3 run failed: {exc}"}
-    keep = ("value", "unit", "ms_per_step", "latency_ms", "served", "e2e", "clocks", "gpu_launches")
+    keep = ("value", "unit", "ms_per_step", "latency_ms", "served", "e2e", "clocks", "gpu_launches", "burst")
     out = {k: rec.get(k) for k in keep}
     out["workload"] = rec.get("config", {}).get("workload")
     out["requests"] = rec.get("config", {}).get("requests")
@@ -778,6 +822,9 @@ def main():
     ap.add_argument("--c3-structures", type=int, default=400)
     ap.add_argument("--c3-rate", type=float, default=200.0)
     ap.add_argument("--c3-hbm-gb", type=float, default=160.0)
+    ap.add_argument("--c3-burst", type=int, default=80,
+                    help="config3: structures of the burst phase (all cycles at once, small budget); 0 = none")
+    ap.add_argument("--c3-burst-hbm-gb", type=float, default=6.0)
     ap.add_argument("--cpu-sample", type=float, default=0.25)
     ap.add_argument("--reference-sample", type=float, default=0.1)
     args = ap.parse_args()

@@ -130,8 +130,10 @@ def library():
         L.dsf_last_launch_count.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.argtypes = [C.c_void_p]
         L.dsf_last_kernel_ms.restype = C.c_double
-        L.dsf_autotune.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_int), _P(C.c_int), _P(C.c_double)]
-        L.dsf_tuning_lookup.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_int), _P(C.c_int), _P(C.c_int)]
+        L.dsf_autotune.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_int), _P(C.c_int), _P(C.c_int),
+                                   _P(C.c_double)]
+        L.dsf_tuning_lookup.argtypes = [C.c_void_p, C.c_int, C.c_int, _P(C.c_int), _P(C.c_int), _P(C.c_int),
+                                        _P(C.c_int)]
         L.dsf_tuning_save.argtypes = [C.c_void_p, C.c_char_p]
         L.dsf_tuning_load.argtypes = [C.c_void_p, C.c_char_p]
     return _lib
@@ -546,20 +548,22 @@ class _Calculator:
     def autotune(self, precision=DSF_FP32_BULK, derivatives=("xyz", "adp", "occ"), multipoles=False):
         """dsf_autotune: times this structure's call over a few tile shapes and
         keeps the fastest for every later call of structures of the same shape
-        key.  Returns dict(blocks_per_sm, ht, ms) of the chosen shape (ht 0:
-        the longest shared-memory sub-tile)."""
-        bps, ht, ms = C.c_int(0), C.c_int(0), C.c_double(0)
+        key.  Returns dict(blocks_per_sm, ht, occupancy, ms) of the chosen
+        shape (ht 0: the longest shared-memory sub-tile; occupancy 3: the
+        register-capped form, 0: the compiler's registers)."""
+        bps, ht, occ, ms = C.c_int(0), C.c_int(0), C.c_int(0), C.c_double(0)
         self.engine.check(self.lib.dsf_autotune(self.h, int(precision), _flags(derivatives, multipoles), C.byref(bps),
-                                                C.byref(ht), C.byref(ms)), "autotune")
-        return dict(blocks_per_sm=bps.value, ht=ht.value, ms=ms.value)
+                                                C.byref(ht), C.byref(occ), C.byref(ms)), "autotune")
+        return dict(blocks_per_sm=bps.value, ht=ht.value, occupancy=occ.value, ms=ms.value)
 
     def tile_shape(self, precision=DSF_FP32_BULK, derivatives=("xyz", "adp", "occ"), multipoles=False):
         """dsf_tuning_lookup: the tile shape the next call takes and whether it
         is a tuned one."""
-        bps, ht, tuned = C.c_int(0), C.c_int(0), C.c_int(0)
+        bps, ht, occ, tuned = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
         self.engine.check(self.lib.dsf_tuning_lookup(self.h, int(precision), _flags(derivatives, multipoles),
-                                                     C.byref(bps), C.byref(ht), C.byref(tuned)), "tile_shape")
-        return dict(blocks_per_sm=bps.value, ht=ht.value, tuned=bool(tuned.value))
+                                                     C.byref(bps), C.byref(ht), C.byref(occ), C.byref(tuned)),
+                          "tile_shape")
+        return dict(blocks_per_sm=bps.value, ht=ht.value, occupancy=occ.value, tuned=bool(tuned.value))
 
     def calculate_device(self, dtdf_ptr, outputs, precision=DSF_FP32_BULK, derivatives=("xyz", "adp", "occ"),
                          multipoles=False, stream=0):

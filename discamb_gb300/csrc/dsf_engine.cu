@@ -19,6 +19,7 @@
 #include "dsf_launch_v3.cuh"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -84,7 +85,7 @@ struct dsf_engine {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // tile shapes chosen by the autotuner, per shape key (tune_key): blocks per SM the reflection chunks
     // aim at, and the sub-tile length (0: the longest the shared-memory budget allows)
-    std::map<std::string, std::pair<int, int> > tuned;
+    std::map<std::string, std::array<int, 3> > tuned;  // blocks per SM, sub-tile cap, register-capped form
     std::mutex tune_mtx;
 };
 
@@ -213,7 +214,7 @@ struct dsf_structure {
     int coset_size = 0;
     int inv_pairs = 0;  // generic models: operations n/2 .. n-1 are the images of 0 .. n/2-1 under -1 at the origin
     int debug_stall = 0;  // dsf_debug_stall_next_call: the next call's kernel waits run out (timeout test)
-    int tune_bps = 0, tune_ht = 0;  // the autotuner's candidate for this structure's next calls (0: none)
+    int tune_bps = 0, tune_ht = 0, tune_occ3 = 0;  // the autotuner's candidate for the next calls (bps 0: none)
     int pending = 0;      // a dsf_submit call of this structure not yet completed by dsf_poll
     std::vector<int> sym_sign;   // [n_sym][3] Cartesian
     std::vector<int> sym_fsign;  // [n_sym][3] fractional h' components
@@ -2035,23 +2036,26 @@ static std::string tune_key(const dsf_structure *s, bool fp64, bool mp, bool gra
     return k;
 }
 
-// blocks per SM and sub-tile cap of a call: the autotuner's candidate under trial, else the tuned shape of the
-// key, else the rule (75 blocks per SM, the longest sub-tile)
-static void call_shape(dsf_structure *s, bool fp64, bool mp, bool grad, int &bps, int &ht)
+// blocks per SM, sub-tile cap and register-capped form of a call: the autotuner's candidate under trial, else the
+// tuned shape of the key, else the rule (75 blocks per SM, the longest sub-tile, the compiler's registers)
+static void call_shape(dsf_structure *s, bool fp64, bool mp, bool grad, int &bps, int &ht, int &occ3)
 {
     bps = 75;
     ht = 0;
+    occ3 = 0;
     if (s->tune_bps > 0) {
         bps = s->tune_bps;
         ht = s->tune_ht;
+        occ3 = s->tune_occ3;
         return;
     }
     dsf_engine *e = s->eng;
     std::lock_guard<std::mutex> lock(e->tune_mtx);
     auto it = e->tuned.find(tune_key(s, fp64, mp, grad));
     if (it != e->tuned.end()) {
-        bps = it->second.first;
-        ht = it->second.second;
+        bps = it->second[0];
+        ht = it->second[1];
+        occ3 = it->second[2];
     }
 }
 
@@ -2102,8 +2106,8 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         DSF_CUDA(cudaEventCreate(&s->ev_end));
     }
     const bool grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
-    int bps, ht_cap;
-    call_shape(s, fp64, mp, grad, bps, ht_cap);
+    int bps, ht_cap, occ3;
+    call_shape(s, fp64, mp, grad, bps, ht_cap, occ3);
     DSF_CUDA(cudaEventRecord(s->ev_begin, st));
     // one launch per ADP kind (tiles [0, n_tiles_plain) without anisotropic ADPs), reflection chunks of
     // chunk_count
@@ -2129,6 +2133,7 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         A.st = st;
         A.grad = grad;
         A.inv = inv_kernel(s, fp64);
+        A.occ3 = occ3 != 0;
         DSF_CUDA(launch_sf3(A, s->model, fp64, mp, kind == 1));
         launches++;
     }
@@ -2142,7 +2147,8 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
 // SM; the longest sub-tile the shared-memory budget allows, or at most 8 reflections) with a zero dT/dF on scratch
 // buffers, and keeps the fastest for every later call of structures with the same shape key.  Any shape gives
 // the same sums (the cross-block sums in another order).
-int dsf_autotune(dsf_structure *s, int precision, int flags, int *blocks_per_sm, int *ht, double *best_ms)
+int dsf_autotune(dsf_structure *s, int precision, int flags, int *blocks_per_sm, int *ht, int *occupancy,
+                 double *best_ms)
 {
     if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
@@ -2170,11 +2176,12 @@ int dsf_autotune(dsf_structure *s, int precision, int flags, int *blocks_per_sm,
         out.d_kappa_prime = p;
     }
     int rc = DSF_OK;
-    auto timed = [&](int bps, int cap, double &ms) {
+    auto timed = [&](int bps, int cap, int occ3, double &ms) {
         s->tune_bps = bps;
         s->tune_ht = cap;
+        s->tune_occ3 = occ3;
         rc = dsf_calculate_device(s, precision, flags, buf, &out, e->stream);
-        s->tune_bps = s->tune_ht = 0;
+        s->tune_bps = s->tune_ht = s->tune_occ3 = 0;
         if (rc) return false;
         if (cudaStreamSynchronize(e->stream) != cudaSuccess) {
             rc = fail(e, DSF_ERR_CUDA, "autotune call failed");
@@ -2184,40 +2191,46 @@ int dsf_autotune(dsf_structure *s, int precision, int flags, int *blocks_per_sm,
         return ms >= 0;
     };
     double warm = 0, best = 1e300;
-    int best_bps = 75, best_cap = 0;
-    if (timed(75, 0, warm)) {
+    int best_bps = 75, best_cap = 0, best_occ3 = 0;
+    // the register-capped form exists for the FP32 multipole-adjoint kernels
+    const int n_occ = (s->model == MODEL_HC && mp && !fp64) ? 2 : 1;
+    if (timed(75, 0, 0, warm)) {
         const int reps = warm < 20.0 ? 3 : 1;
-        for (const int bps : {24, 48, 75, 150})
-            for (const int cap : {0, 8}) {
-                double t = 1e300;
-                for (int r = 0; r < reps; r++) {
-                    double ms;
-                    if (!timed(bps, cap, ms)) break;
-                    t = std::min(t, ms);
+        for (int occ3 = 0; occ3 < n_occ && !rc; occ3++)
+            for (const int bps : {24, 48, 75, 150})
+                for (const int cap : {0, 8}) {
+                    double t = 1e300;
+                    for (int r = 0; r < reps; r++) {
+                        double ms;
+                        if (!timed(bps, cap, occ3, ms)) break;
+                        t = std::min(t, ms);
+                    }
+                    if (rc) break;
+                    if (t < best) {
+                        best = t;
+                        best_bps = bps;
+                        best_cap = cap;
+                        best_occ3 = occ3;
+                    }
                 }
-                if (rc) break;
-                if (t < best) {
-                    best = t;
-                    best_bps = bps;
-                    best_cap = cap;
-                }
-            }
     }
     cudaFree(buf);
     if (rc) return rc;
     {
         std::lock_guard<std::mutex> lock(e->tune_mtx);
-        e->tuned[tune_key(s, fp64, mp, grad)] = {best_bps, best_cap};
+        e->tuned[tune_key(s, fp64, mp, grad)] = {best_bps, best_cap, best_occ3};
     }
     if (blocks_per_sm) *blocks_per_sm = best_bps;
     if (ht) *ht = best_cap;
+    if (occupancy) *occupancy = best_occ3 ? 3 : 0;
     if (best_ms) *best_ms = best;
     return DSF_OK;
 }
 
 // the tile shape the next call of s with these settings takes (tuned, or the rule's 75 blocks per SM and the
 // longest sub-tile, ht = 0); *tuned = 1 when it comes from the autotuner
-int dsf_tuning_lookup(dsf_structure *s, int precision, int flags, int *blocks_per_sm, int *ht, int *tuned)
+int dsf_tuning_lookup(dsf_structure *s, int precision, int flags, int *blocks_per_sm, int *ht, int *occupancy,
+                      int *tuned)
 {
     if (!s) return DSF_ERR_ARGUMENT;
     dsf_engine *e = s->eng;
@@ -2227,8 +2240,9 @@ int dsf_tuning_lookup(dsf_structure *s, int precision, int flags, int *blocks_pe
     std::lock_guard<std::mutex> lock(e->tune_mtx);
     auto it = e->tuned.find(tune_key(s, fp64, mp, grad));
     const bool hit = it != e->tuned.end();
-    if (blocks_per_sm) *blocks_per_sm = hit ? it->second.first : 75;
-    if (ht) *ht = hit ? it->second.second : 0;
+    if (blocks_per_sm) *blocks_per_sm = hit ? it->second[0] : 75;
+    if (ht) *ht = hit ? it->second[1] : 0;
+    if (occupancy) *occupancy = (hit && it->second[2]) ? 3 : 0;
     if (tuned) *tuned = hit ? 1 : 0;
     return DSF_OK;
 }
@@ -2240,7 +2254,8 @@ int dsf_tuning_save(dsf_engine *e, const char *path)
     FILE *f = std::fopen(path, "w");
     if (!f) return fail(e, DSF_ERR_ARGUMENT, "cannot write the tuning file");
     std::lock_guard<std::mutex> lock(e->tune_mtx);
-    for (const auto &kv : e->tuned) std::fprintf(f, "%s %d %d\n", kv.first.c_str(), kv.second.first, kv.second.second);
+    for (const auto &kv : e->tuned)
+        std::fprintf(f, "%s %d %d %d\n", kv.first.c_str(), kv.second[0], kv.second[1], kv.second[2]);
     std::fclose(f);
     return DSF_OK;
 }
@@ -2253,10 +2268,10 @@ int dsf_tuning_load(dsf_engine *e, const char *path)
     FILE *f = std::fopen(path, "r");
     if (!f) return fail(e, DSF_ERR_ARGUMENT, "cannot read the tuning file");
     char key[160];
-    int bps, ht;
+    int bps, ht, occ3;
     std::lock_guard<std::mutex> lock(e->tune_mtx);
-    while (std::fscanf(f, "%159s %d %d", key, &bps, &ht) == 3)
-        if (bps > 0 && bps <= 4096 && ht >= 0 && ht <= kMaxHT) e->tuned[key] = {bps, ht};
+    while (std::fscanf(f, "%159s %d %d %d", key, &bps, &ht, &occ3) == 4)
+        if (bps > 0 && bps <= 4096 && ht >= 0 && ht <= kMaxHT && (occ3 == 0 || occ3 == 1)) e->tuned[key] = {bps, ht, occ3};
     std::fclose(f);
     return DSF_OK;
 }

@@ -21,6 +21,7 @@ struct K3Args {
     bool grad = true;  // false: structure factors only (single-structure FP32 kernels without the adjoint)
     bool inv = false;  // operations as n/2 plus their images under an inversion at the origin (generic models)
     int pattern = 0;   // cosets of four in the order of a known sign group (kPatD2, kPatC2hB), else 0
+    bool occ3 = false; // the register-capped form (three blocks per SM) where it is compiled (occ3_kernel)
     int n_tiles = 0, n_chunks = 0, blocks = 0;
     size_t smem = 0;
     cudaStream_t st = nullptr;
@@ -35,11 +36,19 @@ cudaError_t launch_with(K k, dim3 grid, size_t smem, cudaStream_t st, const Args
     return cudaGetLastError();
 }
 
+// kernels with a register-capped form of three blocks per SM: FP32 HC multipole adjoint, sign-group cosets
+template <bool BATCH, typename R, int MODEL, bool MP, bool GRAD, int PAT>
+constexpr bool occ3_kernel() { return !BATCH && sizeof(R) == 4 && MODEL == MODEL_HC && MP && GRAD && PAT != 0; }
+
 template <bool BATCH, typename R, int MODEL, bool MP, bool ANISO, bool GRAD, bool INV, int NSC, int CS = 0,
           int PAT = 0>
 cudaError_t launch_k3(const K3Args &A)
 {
     constexpr bool OCC4 = occ4_kernel<R, MODEL, NSC>();
+    if constexpr (occ3_kernel<BATCH, R, MODEL, MP, GRAD, PAT>())
+        if (A.occ3)
+            return launch_with(sf_grad_kernel3_occ3<R, MODEL, MP, ANISO, NSC, CS, true, INV, PAT>,
+                               dim3(A.n_tiles, A.n_chunks), A.smem, A.st, *A.S, *A.C, *A.L, *A.G);
     const dim3 grid = BATCH ? dim3(A.blocks) : dim3(A.n_tiles, A.n_chunks);
     static_assert(GRAD || !BATCH, "structure-factor-only kernels: single structures");
     if constexpr (!GRAD && OCC4)

@@ -1149,6 +1149,17 @@ sf_grad_kernel3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
     sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD, INV, PAT>(S, C, L, G, blockIdx.x, blockIdx.y);
 }
 
+// the same with at least three blocks per SM: a register cap (168) for the FP32 multipole-adjoint kernels, which
+// the compiler otherwise gives about 220 registers (two blocks per SM); the autotuner times both and keeps the
+// faster (it trades a few spills for half again as many warps)
+template <typename R, int MODEL, bool MP, bool ANISO, int NSC, int CS = 0, bool GRAD = true, bool INV = false,
+          int PAT = 0>
+__global__ void __launch_bounds__(kTileAtoms, 3)
+sf_grad_kernel3_occ3(DevStructure S, CallBuffers C, SfLaunch L, SignTable G)
+{
+    sf_grad_body<R, MODEL, MP, ANISO, NSC, CS, GRAD, INV, PAT>(S, C, L, G, blockIdx.x, blockIdx.y);
+}
+
 // the same with at least four blocks per SM: the tabulated model with up to
 // four compiled operations (HBM streaming: occupancy over registers).  The
 // other kernels keep the compiler's own register choice, which an explicit

@@ -282,17 +282,18 @@ int dsf_calculate_batch_atoms(dsf_structure *const *structures, int n, int preci
  * No reference counterpart (the reference's threads take fixed contiguous shares of the reflections,
  * scattering_utilities::splitHklLines, src/Scattering/scattering_utilities.cpp:463-517).  dsf_autotune times
  * the structure's call (these precision and derivative flags) over a few tile shapes -- reflection chunks aiming
- * at 24, 48, 75 or 150 blocks per SM, the longest shared-memory sub-tile or at most 8 reflections -- on a zero
- * dT/dF in scratch buffers it allocates and frees, and keeps the fastest for every later call of structures
- * with the same shape key (model, precision, multipole adjoint, derivative pass, operation count, coset form,
- * atoms and reflections in half-octaves, SM count).  Results do not depend on the shape beyond the order of
- * the cross-block sums.  Synchronous.  dsf_tuning_lookup: the shape the next call would take (ht 0: the longest
- * sub-tile; *tuned 0: the rule, 75 blocks per SM).  dsf_tuning_save / dsf_tuning_load: the engine's tuned
- * shapes to and from a text file. */
+ * at 24, 48, 75 or 150 blocks per SM, the longest shared-memory sub-tile or at most 8 reflections, and for the
+ * FP32 multipole-adjoint kernels the compiler's registers or a cap for three blocks per SM -- on a zero dT/dF
+ * in scratch buffers it allocates and frees, and keeps the fastest for every later call of structures with the
+ * same shape key (model, precision, multipole adjoint, derivative pass, operation count, coset form, atoms and
+ * reflections in half-octaves, SM count).  Results do not depend on the shape beyond the order of the
+ * cross-block sums.  Synchronous.  dsf_tuning_lookup: the shape the next call would take (ht 0: the longest
+ * sub-tile; occupancy 3: the register-capped form, 0: the compiler's registers; *tuned 0: the rule, 75 blocks
+ * per SM).  dsf_tuning_save / dsf_tuning_load: the engine's tuned shapes to and from a text file. */
 int dsf_autotune(dsf_structure *s, int precision, int derivative_flags, int *blocks_per_sm, int *ht,
-                 double *best_ms);
+                 int *occupancy, double *best_ms);
 int dsf_tuning_lookup(dsf_structure *s, int precision, int derivative_flags, int *blocks_per_sm, int *ht,
-                      int *tuned);
+                      int *occupancy, int *tuned);
 int dsf_tuning_save(dsf_engine *e, const char *path);
 int dsf_tuning_load(dsf_engine *e, const char *path);
 
