@@ -55,7 +55,7 @@ import numpy as np  # noqa: E402
 #            kappa' 14, Plm 55, p 6) = 195
 WORKLOADS = {
     "config1": dict(seed=1, multipoles=False, flops=94, fp64_steps=3, fp64_warmup=1, cpu_frac=0.25,
-                    traffic_key="sf_grad_kernel3<float,HC,0,ISO,4,CS4>@config1",
+                    traffic_key="sf_grad_kernel3<float,HC,0,ISO,4,CS4,PAT_D2>@config1",
                     desc="config1: HC multipoles l<=4, 5000 atoms (150 types), P212121, 54704 hkl d>=1.5A, iso B, "
                          "dF/d(xyz,B,occ)"),
     "config4": dict(seed=4, desc="config4: 256 crystals, P21/c, tabulated complex64 form factors per (atom, h'), "

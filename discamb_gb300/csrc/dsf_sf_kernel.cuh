@@ -545,7 +545,9 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                 const int col0 = a_begin + (a_begin >= S.table_split ? S.table_shift : 0);
                 const uint32_t bytes = (uint32_t)((sizeof(float2) * (a_end - a_begin) + 15) & ~(size_t)15);
                 const float2 *row = S.table_f + ((size_t)hg * NR + q) * S.table_stride + col0;
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(row), "r"(bytes) : "memory");
+                // no memory clobber: a prefetch changes nothing the program reads, and a clobber would keep the
+                // compiler from holding shared-memory values in registers across it
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(row), "r"(bytes));
             }
         }
     };
