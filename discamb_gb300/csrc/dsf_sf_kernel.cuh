@@ -515,7 +515,6 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
 
     // TAB_REG: form factors of the current and the next group of four reflections
     constexpr int kTabN = TAB_REG ? 4 * NR : 1;
-    constexpr int kTabPrefetchGroups = 4;  // L2 prefetch distance of the register-loaded table (groups of four)
     float2 tab_a[kTabN], tab_b[kTabN];
     const float2 *tab_col = nullptr;
     if constexpr (TAB_REG) {
@@ -534,26 +533,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             }
         }
     };
-    // L2 prefetch of the table rows kTabPrefetchGroups groups of four reflections ahead of the register loads: the
-    // tile's columns of every (reflection, operation) row (one bulk prefetch per row by lanes of warp 0), so the
-    // per-thread loads one group ahead find them in L2 instead of waiting on HBM (the registers hold only one
-    // group in flight)
-    auto tab_prefetch_l2 = [&](int hg) {
-        if constexpr (TAB_REG) {
-            const int q = lane;
-            if (warp == 0 && q < 4 * NR && hg + q / NR < h_end) {
-                const int col0 = a_begin + (a_begin >= S.table_split ? S.table_shift : 0);
-                const uint32_t bytes = (uint32_t)((sizeof(float2) * (a_end - a_begin) + 15) & ~(size_t)15);
-                const float2 *row = S.table_f + ((size_t)hg * NR + q) * S.table_stride + col0;
-                // no memory clobber: a prefetch changes nothing the program reads, and a clobber would keep the
-                // compiler from holding shared-memory values in registers across it
-                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(row), "r"(bytes));
-            }
-        }
-    };
     tab_load(tab_b, h_begin);
-#pragma unroll
-    for (int gp = 1; gp <= kTabPrefetchGroups; gp++) tab_prefetch_l2(h_begin + 4 * gp);
 
     if (tid == 0 && !L.stall_first) issue(0, h_begin);
     uint32_t parity[2] = {0u, 0u};
@@ -1085,7 +1065,6 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             for (int g0 = 0; g0 < ht; g0 += 4) {
 #pragma unroll
                 for (int q = 0; q < kTabN; q++) tab_a[q] = tab_b[q];
-                tab_prefetch_l2(h0 + g0 + 4 * (1 + kTabPrefetchGroups));
                 group(g0, tab_a, tab_b);
             }
         } else {
