@@ -518,7 +518,8 @@ def run_config4(args):
     clocks = clk.summary()
     launches = calcs[0].last_launch_count()
     ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
-    # FP64 form of the same batch (per-structure launches)
+    # FP64 form of the same batch (per-structure launches); the FP32 results of the last timed step against it
+    r32 = [{k: v.clone() for k, v in o.items()} for o in outs]
     ev64 = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     eng.calculate_batch_device(calcs, ptrs, optrs, precision=api.DSF_FP64, stream=sptr)
     ev64[0].record(stream)
@@ -526,6 +527,15 @@ def run_config4(args):
     ev64[1].record(stream)
     torch.cuda.synchronize(dev)
     ms64 = ev64[0].elapsed_time(ev64[1])
+    err32 = {"f": float(sum((a["f"] - b["f"]).norm(dim=1).sum() for a, b in zip(r32, outs)) /
+                        sum(b["f"].norm(dim=1).sum() for b in outs))}
+    err_max = {}
+    for k in ("d_xyz", "d_adp", "d_occ"):
+        dg = torch.cat([(a[k] - b[k]).flatten() for a, b in zip(r32, outs)])
+        g64 = torch.cat([b[k].flatten() for b in outs])
+        err32[k] = float(dg.norm() / g64.norm())
+        err_max[k] = float(dg.abs().max() / g64.abs().max())
+    del r32
     # end to end: host dT/dF in, host F and derivatives out, one submission
     hd = [st.dtdf for st in sts]
     for _ in range(2):
@@ -560,7 +570,11 @@ def run_config4(args):
         "config": {"workload": WORKLOADS["config4"]["desc"], "crystals": len(sts), "terms_per_step": terms,
                    "table_bytes": table_bytes, "setup_s": t_setup,
                    "l2": "inputs larger than L2 (tables); 256 MB flush between steps"},
-        "fp64": {"value": terms / (ms64 * 1e-3), "ms_per_step": ms64, "fp32_over_fp64": ms64 / ms},
+        "fp64": {"value": terms / (ms64 * 1e-3), "ms_per_step": ms64, "fp32_over_fp64": ms64 / ms,
+                 "fp32_error": {**err32, "measure": "sum|dF|/sum|F| over every crystal's reflections; derivatives "
+                                                   "per class |dg|/|g| over every crystal's atoms, FP32-bulk "
+                                                   "against this FP64 run"},
+                 "fp32_error_max": {**err_max, "measure": "per derivative class max|dg| / max|g|"}},
         "e2e": {"value": terms / (e2e_ms * 1e-3), "unit": "terms/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": sum(16 * st.n_hkl for st in sts),
                 "d2h_bytes_per_step": sum(16 * st.n_hkl + 80 * st.n_atoms for st in sts)},

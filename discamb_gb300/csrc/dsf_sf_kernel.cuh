@@ -252,6 +252,28 @@ __device__ __forceinline__ void wht4(const R (&u)[4], R (&W)[4])
     W[3] = t1 - t3;
 }
 
+// two transforms at once (the real and imaginary parts of a complex quantity, or two real ones): in FP32 as
+// packed pairs (one add.f32x2 or fma.f32x2 per butterfly leg instead of two scalar adds; a - b as fma(b, -1, a),
+// rounded once like the subtraction, so the results equal the scalar form's)
+template <typename R>
+__device__ __forceinline__ void wht4x2(const R (&a)[4], const R (&b)[4], R (&A)[4], R (&B)[4])
+{
+    if constexpr (sizeof(R) == 4) {
+        const float2 m1 = make_float2(-1.f, -1.f);
+        const float2 u0 = make_float2(a[0], b[0]), u1 = make_float2(a[1], b[1]);
+        const float2 u2 = make_float2(a[2], b[2]), u3 = make_float2(a[3], b[3]);
+        const float2 t0 = __fadd2_rn(u0, u1), t1 = __ffma2_rn(u1, m1, u0);
+        const float2 t2 = __fadd2_rn(u2, u3), t3 = __ffma2_rn(u3, m1, u2);
+        const float2 w0 = __fadd2_rn(t0, t2), w1 = __fadd2_rn(t1, t3);
+        const float2 w2 = __ffma2_rn(t2, m1, t0), w3 = __ffma2_rn(t3, m1, t1);
+        A[0] = w0.x; A[1] = w1.x; A[2] = w2.x; A[3] = w3.x;
+        B[0] = w0.y; B[1] = w1.y; B[2] = w2.y; B[3] = w3.y;
+    } else {
+        wht4(a, A);
+        wht4(b, B);
+    }
+}
+
 template <typename R>
 struct StageLayout {
     size_t rs, tr, trm, gw, h2, cont, tab, bytes;
@@ -614,6 +636,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     // (classes 3 5 6) and plain U
                     R hr[3] = {0, 0, 0}, m6r[ADIAG ? 6 : 1], qd = 0, qc[3] = {0, 0, 0}, qw[WHT && ADIAG ? 4 : 1];
                     R Sre[NSG], Sim[NSG], Ucre = 0, Ucim = 0;
+                    R gUc = 0;  // WHT: Re(g U), contracted per coset
 #pragma unroll
                     for (int q = 0; q < (ADIAG ? 6 : 1); q++) m6r[q] = R(0);
 #pragma unroll
@@ -641,11 +664,13 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         }
                     };
                     auto adp_coset_end = [&]() {
-                        if constexpr (XDIAG) {
+                        if constexpr (WHT) {
+                            // contracted in wht_end
+                        } else if constexpr (XDIAG) {
 #pragma unroll
                             for (int c = 0; c < 3; c++) { Xre[c] += hr[c] * Sre[c]; Xim[c] += hr[c] * Sim[c]; }
                         }
-                        if constexpr (ADIAG) {
+                        if constexpr (ADIAG && !WHT) {
 #pragma unroll
                             for (int q = 0; q < 3; q++) { Are[q] -= m6r[q] * Ucre; Aim[q] -= m6r[q] * Ucim; }
 #pragma unroll
@@ -667,8 +692,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                                 Ep[wht_char(PAT, ec[q])] += Ec[q];
                                 Op[wht_char(PAT, oc[q])] += Oc[q];
                             }
-                            wht4(Ep, fwr);
-                            wht4(Op, t);
+                            wht4x2(Ep, Op, fwr, t);
 #pragma unroll
                             for (int q = 0; q < 4; q++) fwi[q] = fsim + t[q];
                         }
@@ -686,21 +710,34 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     auto wht_end = [&]() {
                         if constexpr (WHT) {
                             R Wr[4], Wi[4];
-                            wht4(ur4, Wr);
-                            wht4(ui4, Wi);
+                            wht4x2(ur4, ui4, Wr, Wi);
                             Ure += Wr[0];
                             Uim += Wi[0];
                             constexpr int cls[6] = {1, 2, 4, 3, 5, 6};
+                            if constexpr (GRAD) {
+                                // the position and ADP adjoints contracted with g here, once per coset, from
+                                // the characters their classes take: -h'_c Im(g S_c) and -m6_q Re(g S_q)
+                                // (the diagonal q with S = U of the coset); Re(g U) summed over the cosets
+                                const R gw0 = gre * Wr[0] - gim * Wi[0];
+                                gUc += gw0;
 #pragma unroll
-                            for (int q = 0; q < NSG; q++) {
-                                Sre[q] = Wr[wht_char(PAT, cls[q])];
-                                Sim[q] = Wi[wht_char(PAT, cls[q])];
+                                for (int c = 0; c < 3; c++) {
+                                    const int k = wht_char(PAT, cls[c]);
+                                    part[CH_XYZ + c] -= hr[c] * (gre * Wi[k] + gim * Wr[k]);
+                                }
+                                if constexpr (ADIAG) {
+#pragma unroll
+                                    for (int q = 0; q < 3; q++) part[CH_ADP + q] -= m6r[q] * gw0;
+#pragma unroll
+                                    for (int q = 3; q < 6; q++) {
+                                        const int k = wht_char(PAT, cls[q]);
+                                        part[CH_ADP + q] -= m6r[q] * (gre * Wr[k] - gim * Wi[k]);
+                                    }
+                                }
                             }
-                            if constexpr (ADIAG) { Ucre = Wr[0]; Ucim = Wi[0]; }
                             if constexpr (MP && DIAG) {
                                 R Vr[4], Vi[4];
-                                wht4(wr4, Vr);
-                                wht4(wi4, Vi);
+                                wht4x2(wr4, wi4, Vr, Vi);
                                 We[0] = Vr[0]; We[1] = Vr[wht_char(PAT, 3)]; We[2] = Vr[wht_char(PAT, 6)];
                                 We[3] = Vr[wht_char(PAT, 5)];
                                 Wo[0] = Vi[wht_char(PAT, 2)]; Wo[1] = Vi[wht_char(PAT, 4)]; Wo[2] = Vi[wht_char(PAT, 1)];
@@ -848,8 +885,8 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             // the table holds n_hkl_pad rows (zero past the last reflection), columns in
                             // the engine's atom order (consecutive lanes read consecutive values)
                             if constexpr (TAB_REG) {
-                                const float2 tv = cur[j * NR + s];
-                                fre = tv.x + anre; fim = tv.y + anim;
+                                const float2 tv = __fadd2_rn(cur[j * NR + s], make_float2(anre, anim));
+                                fre = tv.x; fim = tv.y;
                             } else if constexpr (F32) {
                                 const float2 tv = reinterpret_cast<const float2 *>(st + SL.tab)[
                                     (size_t)(hl * nS + s) * kTileAtoms + tid];
@@ -1007,16 +1044,18 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         Fv[2 * j] = wT * Ure;
                         Fv[2 * j + 1] = wT * Uim;
                     }
-                    const R gU = gre * Ure - gim * Uim;  // Re(g T U)
+                    R gU;  // Re(g T U)
+                    if constexpr (WHT) gU = gUc; else gU = gre * Ure - gim * Uim;
                     part[CH_OCC] += gU;
-                    if constexpr (ANISO) {
+                    if constexpr (!ANISO) {
+                        part[CH_ADP] -= sH2[hl] * gU;
+                    } else if constexpr (!WHT) {
 #pragma unroll
                         for (int q = 0; q < 6; q++) part[CH_ADP + q] += gre * Are[q] - gim * Aim[q];
-                    } else {
-                        part[CH_ADP] -= sH2[hl] * gU;
                     }
+                    if constexpr (!WHT)
 #pragma unroll
-                    for (int q = 0; q < 3; q++) part[CH_XYZ + q] -= gre * Xim[q] + gim * Xre[q];  // -Im(g T X)
+                        for (int q = 0; q < 3; q++) part[CH_XYZ + q] -= gre * Xim[q] + gim * Xre[q];  // -Im(g T X)
                     if constexpr (MP && !DIAG) {
                         const R *dr = sTrm + (size_t)(lt * ht + hl) * 8;
                         const R gE = gre * Ere - gim * Eim;
