@@ -77,7 +77,7 @@ struct DevStructure {
     const int4 *hkl;             // [n_hkl] (h,k,l,0)
     const double *h2;            // |h_cart|^2
     const float *h2f;
-    const float2 *table_f;       // tabulated model: [n_hkl_pad][n_sym][table_stride]
+    const float2 *table_f;       // tabulated model: [n_hkl_pad][table_stride][n_sym] (+16 bytes of slack)
     const double2 *table_d;
     int table_stride;            // columns per (reflection, operation) row: even
     int table_split, table_shift;  // column of sorted atom a: a + (a >= split ? shift : 0) (even tile starts)

@@ -1495,7 +1495,8 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
     table_columns(s);
     const int nA = s->n_atoms, nS = s->n_sym, stride = s->table_stride;
     const size_t row = (size_t)nS * stride;  // complex values per reflection
-    std::vector<float> tf(2 * row * n_pad, 0.0f);
+    // [n_pad][stride][nS] plus 16 bytes of slack (the staged kernels read whole 16-byte units)
+    std::vector<float> tf(2 * row * n_pad + 4, 0.0f);
     std::vector<double> td(table_fp32 ? 0 : 2 * row * n_pad, 0.0);
     for (int i = 0; i < n_hkl; i++)
         for (int op = 0; op < nS; op++)
@@ -1503,7 +1504,7 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
                 const int a = table_column_atom(c, s->table_split, s->table_shift, nA);
                 if (a < 0) continue;
                 const size_t j = 2 * (((size_t)order[i] * nS + op) * nA + s->perm[a]);
-                const size_t k = 2 * (row * i + (size_t)op * stride + c);
+                const size_t k = 2 * (row * i + (size_t)c * nS + op);
                 tf[k] = (float)table[j];
                 tf[k + 1] = (float)table[j + 1];
                 if (!table_fp32) {
@@ -1523,15 +1524,15 @@ int dsf_structure_create_tabulated(dsf_engine *e, const dsf_symmetry *sym, const
 
 // gathers a caller's [n_hkl][n_sym][n_atoms] complex table (complex64 or
 // complex128, the caller's reflection and atom order) into the engine's
-// line-ordered, padded complex64 table with columns in the engine's atom
-// order; rows past n_hkl are zero
+// line-ordered, padded complex64 table [n_pad][stride][n_sym] with columns in
+// the engine's atom order; rows past n_hkl are zero
 __global__ void table_gather_kernel(int n_pad, int n_hkl, int n_sym, int n_atoms, int stride, int split, int shift,
                                     const int *order, const int *perm, const void *src, int src_fp64, float2 *dst)
 {
     const size_t row = (size_t)n_sym * stride, total = (size_t)n_pad * row;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const size_t r = i / row, q = i - r * row;
-        const int op = (int)(q / stride), c = (int)(q - (size_t)op * stride);
+        const int c = (int)(q / n_sym), op = (int)(q - (size_t)c * n_sym);
         const int a = table_column_atom(c, split, shift, n_atoms);
         float2 v = make_float2(0.f, 0.f);
         if (r < (size_t)n_hkl && a >= 0) {
@@ -1585,11 +1586,12 @@ int dsf_structure_create_tabulated_device(dsf_engine *e, const dsf_symmetry *sym
     if ((rc = upload(e, d_order, order.data(), order.size()))) return bail(rc);
     table_columns(s);
     const size_t row = (size_t)s->n_sym * s->table_stride;
-    cudaError_t ce = s->d_table_f.alloc(sizeof(float2) * row * n_pad);
+    cudaError_t ce = s->d_table_f.alloc(sizeof(float2) * (row * n_pad + 2));  // 16 bytes of slack
     if (ce != cudaSuccess) {
         d_order.release();
         return bail(fail(e, DSF_ERR_MEMORY, "table allocation failed"));
     }
+    cudaMemsetAsync(s->d_table_f.as<float2>() + row * n_pad, 0, 2 * sizeof(float2), e->setup);
     table_gather_kernel<<<std::max(1, e->n_sm) * 8, 256, 0, e->setup>>>(
         n_pad, n_hkl, s->n_sym, s->n_atoms, s->table_stride, s->table_split, s->table_shift, d_order.as<int>(),
         s->d_perm.as<int>(), table_device, table_fp64, s->d_table_f.as<float2>());

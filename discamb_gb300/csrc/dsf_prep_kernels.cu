@@ -74,6 +74,12 @@ __global__ void rs_prep_kernel(DevStructure S, int n_hkl_pad, RsRec<R> *out)
                 harmonic_polys<double>(cx * inv, cy * inv, cz * inv, v);
                 for (int q = 0; q < 25; q++) rec.y[q] = R(v[q] * kDensityNorm[q]);
             }
+        } else {
+            // the ADP quadratic form's monomials of h' (the coset kernels read them instead of forming them per
+            // atom), rounded as the kernel's own products in R would be
+            const R a = rec.hf[0], b = rec.hf[1], c = rec.hf[2];
+            rec.y[0] = a * a; rec.y[1] = b * b; rec.y[2] = c * c;
+            rec.y[3] = R(2) * a * b; rec.y[4] = R(2) * a * c; rec.y[5] = R(2) * b * c;
         }
     }
     out[i] = rec;

@@ -49,7 +49,7 @@ template <typename R>
 struct __align__(16) RsRec {
     int4 hi;   // h'0, h'1, h'2, fixed-point phase offset of h.t
     R hf[4];   // h' as reals, h.t (FP64 form)
-    R y[28];   // 25 harmonics, padded
+    R y[28];   // HC: 25 harmonics, padded; other models: h'0^2, h'1^2, h'2^2, 2h'0h'1, 2h'0h'2, 2h'1h'2
 };
 
 // sin and cos of 2 pi (P 2^-32 + lo) for a phase P in 2^32 fixed point (the
@@ -81,11 +81,19 @@ __device__ __forceinline__ void sincos_fixed(uint32_t P, float lo, float *sn, fl
 }
 
 // temperature factor from the exponent of the ADP quadratic form: FP64 exp;
-// FP32 exp2 (the FP32 ADPs are stored multiplied by log2 e)
+// FP32 2^x (the FP32 ADPs are stored multiplied by log2 e) by the hardware
+// approximation ex2.approx.ftz.f32 alone (relative error about 2^-22, below
+// the FP32 rounding of the terms it scales; x <= 0 here, and a result below
+// 2^-126 flushes to zero, which moves its term by less than that)
 template <typename R>
 __device__ __forceinline__ R texp(R x);
 template <>
-__device__ __forceinline__ float texp<float>(float x) { return exp2f(x); }
+__device__ __forceinline__ float texp<float>(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 template <>
 __device__ __forceinline__ double texp<double>(double x) { return exp(x); }
 
@@ -274,6 +282,31 @@ __device__ __forceinline__ void wht4x2(const R (&a)[4], const R (&b)[4], R (&A)[
     }
 }
 
+// one table row of a column: its NR operation values (complex64, contiguous, 16 x NR-byte aligned), streamed
+// past L1 (read once): 256-bit loads for four operations
+template <int NR>
+__device__ __forceinline__ void ld_table_row(const float2 *p, float2 *d)
+{
+    if constexpr (NR % 4 == 0) {
+#pragma unroll
+        for (int k = 0; k < NR / 4; k++) {
+            float v[8];
+            asm("ld.global.cs.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+                : "l"(p + 4 * k));
+#pragma unroll
+            for (int q = 0; q < 4; q++) d[4 * k + q] = make_float2(v[2 * q], v[2 * q + 1]);
+        }
+    } else if constexpr (NR == 2) {
+        const float4 v = __ldcs(reinterpret_cast<const float4 *>(p));
+        d[0] = make_float2(v.x, v.y);
+        d[1] = make_float2(v.z, v.w);
+    } else {
+#pragma unroll
+        for (int q = 0; q < NR; q++) d[q] = __ldcs(p + q);
+    }
+}
+
 template <typename R>
 struct StageLayout {
     size_t rs, tr, trm, gw, h2, cont, tab, bytes;
@@ -340,6 +373,10 @@ struct PhaseOps<double> {
 // form, every kAnchorF32 reflections so the FP32 rounding of the step cannot
 // build up.
 constexpr int kAnchorF32 = 8;
+// the tabulated kernels (little arithmetic per term, so an anchor's exact phases weigh more) re-anchor at
+// line and sub-tile starts only (every 16 reflections at most): config 4's FP32 error against FP64 went
+// 1.6e-7 -> 2.2e-7 (F and each derivative class) for 1.3% of the step
+constexpr int kAnchorTableF32 = 16;
 
 // GRAD = false: structure factors only (the reference's calculateStructureFactors, which runs its engine with
 // every derivative switched off, HansenCoppensStructureFactorCalculator.cpp:305-326): the derivative sums are
@@ -447,20 +484,19 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
         unsigned char *st = stage0 + buf * SL.bytes;
         const uint32_t rs_bytes = (uint32_t)(sizeof(RsRec<R>) * ht * nS);
         const uint32_t tr_bytes = (uint32_t)(sizeof(R) * 8 * ht);
-        // the tile's columns of the table: 16-byte aligned (even first column, even row stride)
+        // the tile's columns of one table row (each column its nS operation values): 16-byte aligned (even
+        // first column, even row stride), rounded up to 16 bytes (the table has 16 bytes of slack at its end)
         const int tab_col0 = a_begin + (a_begin >= S.table_split ? S.table_shift : 0);
-        const uint32_t tab_bytes = (uint32_t)((sizeof(float2) * (a_end - a_begin) + 15) & ~(size_t)15);
+        const uint32_t tab_bytes = (uint32_t)((sizeof(float2) * (size_t)nS * (a_end - a_begin) + 15) & ~(size_t)15);
         const uint32_t bytes = rs_bytes + (uint32_t)(2 * sizeof(R) * ht) + (uint32_t)(sizeof(R) * ht) +
                                (uint32_t)(sizeof(int) * ht) + (TABLE ? 0u : tr_bytes * nT * (MP ? 2u : 1u)) +
-                               (TAB_SMEM ? tab_bytes * (uint32_t)(ht * nS) : 0u);
+                               (TAB_SMEM ? tab_bytes * (uint32_t)ht : 0u);
         fence_proxy_async();
         mbar_expect_tx(&bar[buf], bytes);
         if constexpr (TAB_SMEM) {
-            for (int q = 0; q < ht * nS; q++) {
-                const size_t row = (size_t)(h0 + q / nS) * nS + (q % nS);
-                bulk_copy(st + SL.tab + sizeof(float2) * kTileAtoms * (size_t)q,
-                          S.table_f + row * S.table_stride + tab_col0, tab_bytes, &bar[buf]);
-            }
+            for (int q = 0; q < ht; q++)
+                bulk_copy(st + SL.tab + sizeof(float2) * kTileAtoms * (size_t)(q * nS),
+                          S.table_f + ((size_t)(h0 + q) * S.table_stride + tab_col0) * nS, tab_bytes, &bar[buf]);
         }
         bulk_copy(st + SL.rs, rs_g + (size_t)h0 * nS, rs_bytes, &bar[buf]);
         if constexpr (!TABLE) {
@@ -540,18 +576,19 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
     float2 tab_a[kTabN], tab_b[kTabN];
     const float2 *tab_col = nullptr;
     if constexpr (TAB_REG) {
-        // a tile's columns are contiguous (tiles do not straddle table_split)
-        tab_col = S.table_f + (a + (a >= S.table_split ? S.table_shift : 0));
+        // a tile's columns are contiguous (tiles do not straddle table_split); row 0 of this atom's column
+        tab_col = S.table_f + (size_t)(a + (a >= S.table_split ? S.table_shift : 0)) * NR;
 #pragma unroll
         for (int q = 0; q < 4 * NR; q++) tab_a[q] = tab_b[q] = make_float2(0.f, 0.f);
     }
-    // rows hg .. hg + 3 (below n_hkl_pad for every group that starts before h_end)
+    // rows hg .. hg + 3 (below n_hkl_pad for every group that starts before h_end): per row the column's NR
+    // operation values, contiguous (one 32-byte load per four operations)
     auto tab_load = [&](float2 (&dst)[kTabN], int hg) {
         if constexpr (TAB_REG) {
             if (have && hg < h_end) {
+                const size_t rstep = (size_t)S.table_stride * NR;
 #pragma unroll
-                for (int q = 0; q < 4 * NR; q++)
-                    dst[q] = __ldcs(tab_col + ((size_t)hg * NR + q) * S.table_stride);
+                for (int j = 0; j < 4; j++) ld_table_row<NR>(tab_col + (size_t)(hg + j) * rstep, &dst[j * NR]);
             }
         }
     };
@@ -601,7 +638,8 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             // reflection j of the group; its partial F goes to Fv[2j], Fv[2j + 1]
             auto reflection = [&](const int j) {
                 const int hl = g0 + j;
-                const bool anchor = !REC || sCont[hl] == 0 || hl == 0 || (F32 && (hl % kAnchorF32) == 0);
+                const bool anchor = !REC || sCont[hl] == 0 || hl == 0 ||
+                                    (F32 && (hl % (TABLE ? kAnchorTableF32 : kAnchorF32)) == 0);
                 if (active) {
                     const R2 g = sG[hl];
                     R fsre = anre, fsim = anim, r0 = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0;
@@ -648,8 +686,16 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             for (int q = 0; q < NSG; q++) { Sre[q] = R(0); Sim[q] = R(0); }
                         }
                         if constexpr (ADIAG) {
-                            m6r[0] = hr[0] * hr[0]; m6r[1] = hr[1] * hr[1]; m6r[2] = hr[2] * hr[2];
-                            m6r[3] = R(2) * hr[0] * hr[1]; m6r[4] = R(2) * hr[0] * hr[2]; m6r[5] = R(2) * hr[1] * hr[2];
+                            if constexpr (HC) {
+                                m6r[0] = hr[0] * hr[0]; m6r[1] = hr[1] * hr[1]; m6r[2] = hr[2] * hr[2];
+                                m6r[3] = R(2) * hr[0] * hr[1]; m6r[4] = R(2) * hr[0] * hr[2];
+                                m6r[5] = R(2) * hr[1] * hr[2];
+                            } else {
+                                // the same six products, from the record (rs_prep_kernel; the other models
+                                // have no harmonics there)
+#pragma unroll
+                                for (int q = 0; q < 6; q++) m6r[q] = rec.y[q];
+                            }
                             qd = adp[0] * m6r[0] + adp[1] * m6r[1] + adp[2] * m6r[2];
                             qc[0] = adp[3] * m6r[3]; qc[1] = adp[4] * m6r[4]; qc[2] = adp[5] * m6r[5];
                             Ucre = R(0); Ucim = R(0);
@@ -824,7 +870,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         }
                     };
                     // INV: e^{i theta} T of the first half of the operations, for their inversion images
-                    R zT_re[INV ? NR / 2 : 1], zT_im[INV ? NR / 2 : 1];
+                    R zT_re[INV ? NR / 2 : 1] = {}, zT_im[INV ? NR / 2 : 1] = {};  // each set before its image reads it
                     auto term = [&](int s) {
                         const RsRec<R> &rec = recs[s];
                         const R h0f = rec.hf[0], h1f = rec.hf[1], h2f = rec.hf[2];
@@ -882,18 +928,19 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                         R A0 = 0, A1 = 0, A2 = 0, A3 = 0, A4 = 0;
                         const R *y = rec.y;
                         if constexpr (TABLE) {
-                            // the table holds n_hkl_pad rows (zero past the last reflection), columns in
-                            // the engine's atom order (consecutive lanes read consecutive values)
+                            // the table holds n_hkl_pad rows (zero past the last reflection), columns in the
+                            // engine's atom order, each column's operation values contiguous (consecutive lanes
+                            // read consecutive columns)
                             if constexpr (TAB_REG) {
                                 const float2 tv = __fadd2_rn(cur[j * NR + s], make_float2(anre, anim));
                                 fre = tv.x; fim = tv.y;
                             } else if constexpr (F32) {
                                 const float2 tv = reinterpret_cast<const float2 *>(st + SL.tab)[
-                                    (size_t)(hl * nS + s) * kTileAtoms + tid];
+                                    ((size_t)hl * kTileAtoms + tid) * nS + s];
                                 fre = tv.x + anre; fim = tv.y + anim;
                             } else {
                                 const int col = a + (a >= S.table_split ? S.table_shift : 0);
-                                const size_t ti = ((size_t)(h0 + hl) * nS + s) * S.table_stride + (have ? col : 0);
+                                const size_t ti = ((size_t)(h0 + hl) * S.table_stride + (have ? col : 0)) * nS + s;
                                 // an FP32-only table is read widened
                                 double2 tv;
                                 if (S.table_d) {
