@@ -371,12 +371,12 @@ struct PhaseOps<double> {
 // src/Scattering/scattering_utilities.cpp:575-627); the exact phase is
 // re-anchored at every line start, at every sub-tile start and, in the FP32
 // form, every kAnchorF32 reflections so the FP32 rounding of the step cannot
-// build up.
-constexpr int kAnchorF32 = 8;
-// the tabulated kernels (little arithmetic per term, so an anchor's exact phases weigh more) re-anchor at
-// line and sub-tile starts only (every 16 reflections at most): on a 256-crystal P2_1/c tabulated batch the
-// FP32 error against FP64 went 1.6e-7 -> 2.2e-7 (F and each derivative class) for 1.3% of the time
-constexpr int kAnchorTableF32 = 16;
+// build up.  With 16 (sub-tiles hold at most 16 reflections: an anchor at
+// every line and sub-tile start) the FP32 error against FP64 measured
+// 3.6e-7 (F) on the 5,000-atom P2_1 2_1 2_1 and 50,000-atom P4_3 2_1 2
+// structures and 2.2e-7 on a 256-crystal P2_1/c tabulated batch, against
+// 3.1-3.2e-7 and 1.6e-7 with 8, for 2.4-3.4% of the time.
+constexpr int kAnchorF32 = 16;
 
 // GRAD = false: structure factors only (the reference's calculateStructureFactors, which runs its engine with
 // every derivative switched off, HansenCoppensStructureFactorCalculator.cpp:305-326): the derivative sums are
@@ -639,7 +639,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
             auto reflection = [&](const int j) {
                 const int hl = g0 + j;
                 const bool anchor = !REC || sCont[hl] == 0 || hl == 0 ||
-                                    (F32 && (hl % (TABLE ? kAnchorTableF32 : kAnchorF32)) == 0);
+                                    (F32 && (hl % kAnchorF32) == 0);
                 if (active) {
                     const R2 g = sG[hl];
                     R fsre = anre, fsim = anim, r0 = 0, r1 = 0, r2 = 0, r3 = 0, r4 = 0;
