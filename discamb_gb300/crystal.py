@@ -247,6 +247,7 @@ _F_VECTORS = [("0", "1/2", "1/2"), ("1/2", "0", "1/2"), ("1/2", "1/2", "0")]
 _P3 = ["x,y,z", "-y,x-y,z", "-x+y,-x,z"]
 _P3_INV = ["-x,-y,-z", "y,-x+y,-z", "x-y,x,-z"]
 SPACE_GROUPS.update({
+    "P3": list(_P3),
     # rhombohedral centering on hexagonal axes, obverse and reverse settings
     "R-3": _with_centering(_P3 + _P3_INV, _R_OBVERSE),
     "R3(reverse)": _with_centering(_P3, _R_REVERSE),

@@ -248,6 +248,11 @@ __host__ __device__ constexpr int wht_char(int pat, int c)
     return parity3(c & pat & 7) + 2 * parity3(c & (pat >> 3) & 7);
 }
 
+// the additive identity for sums that start empty: x + (-0) = x for every x, so the compiler drops the first
+// addition (x + (+0) differs from x for x = -0, and is kept)
+template <typename R>
+constexpr R kZero = R(-0.0);
+
 // W[k] = sum_s chi_k(s) u[s] for the coset order [e, a, b, ab] (the transform is its own inverse up to 1/4,
 // and symmetric: the same butterfly gives each operation's combination of the character sums)
 template <typename R>
@@ -662,7 +667,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     R Tiso = R(1);
                     if (!ANISO && has_adp) Tiso = texp<R>(-adp[0] * sH2[hl]);
                     const R gre = g.x * Tiso, gim = g.y * Tiso;  // adjoint weight with the isotropic factor
-                    R Ure = 0, Uim = 0;
+                    R Ure = kZero<R>, Uim = kZero<R>;
                     R Xre[3] = {0, 0, 0}, Xim[3] = {0, 0, 0};
                     R Are[ANISO ? 6 : 1], Aim[ANISO ? 6 : 1];
 #pragma unroll
@@ -674,7 +679,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     // (classes 3 5 6) and plain U
                     R hr[3] = {0, 0, 0}, m6r[ADIAG ? 6 : 1], qd = 0, qc[3] = {0, 0, 0}, qw[WHT && ADIAG ? 4 : 1];
                     R Sre[NSG], Sim[NSG], Ucre = 0, Ucim = 0;
-                    R gUc = 0;  // WHT: Re(g U), contracted per coset
+                    R gUc = kZero<R>;  // WHT: Re(g U), contracted per coset
 #pragma unroll
                     for (int q = 0; q < (ADIAG ? 6 : 1); q++) m6r[q] = R(0);
 #pragma unroll
@@ -701,7 +706,7 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                             Ucre = R(0); Ucim = R(0);
                             if constexpr (WHT) {
                                 // each operation's quadratic form: qd + the cross terms xy xz yz with its signs
-                                R Qp[4] = {qd, 0, 0, 0};
+                                R Qp[4] = {qd, kZero<R>, kZero<R>, kZero<R>};
                                 Qp[wht_char(PAT, 3)] += qc[0];
                                 Qp[wht_char(PAT, 5)] += qc[1];
                                 Qp[wht_char(PAT, 6)] += qc[2];
@@ -732,7 +737,8 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
                     auto forward_wht = [&]() {
                         if constexpr (WHT && DIAG) {
                             constexpr int ec[4] = {0, 3, 6, 5}, oc[4] = {2, 4, 1, 7};
-                            R Ep[4] = {0, 0, 0, 0}, Op[4] = {0, 0, 0, 0}, t[4];
+                            R Ep[4] = {kZero<R>, kZero<R>, kZero<R>, kZero<R>}, t[4];
+                            R Op[4] = {kZero<R>, kZero<R>, kZero<R>, kZero<R>};
 #pragma unroll
                             for (int q = 0; q < 4; q++) {
                                 Ep[wht_char(PAT, ec[q])] += Ec[q];

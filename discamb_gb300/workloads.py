@@ -232,7 +232,7 @@ def small_case(sg_symbol="P21/c", n_atoms=6, stol_max=0.5, seed=7, cell_kind=Non
     if cell_kind is None:
         cell_kind = {"P1": "triclinic", "P-1": "triclinic", "P-1(shift)": "triclinic",
                      "P21": "monoclinic", "P21/c": "monoclinic", "C2/c": "monoclinic",
-                     "I2/m-like": "monoclinic", "R-3": "hexagonal",
+                     "I2/m-like": "monoclinic", "R-3": "hexagonal", "P3": "hexagonal",
                      "R3(reverse)": "hexagonal"}.get(sg_symbol, "orthorhombic")
     cell = random_cell(rng, cell_kind)
     if sg_symbol in ("P43212", "P41"):
