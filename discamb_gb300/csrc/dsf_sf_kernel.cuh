@@ -82,8 +82,8 @@ __device__ __forceinline__ void sincos_fixed(uint32_t P, float lo, float *sn, fl
 
 // temperature factor from the exponent of the ADP quadratic form: FP64 exp;
 // FP32 2^x (the FP32 ADPs are stored multiplied by log2 e) by the hardware
-// approximation ex2.approx.ftz.f32 alone (relative error about 2^-22, below
-// the FP32 rounding of the terms it scales; x <= 0 here, and a result below
+// approximation ex2.approx.ftz.f32 alone (a few FP32 ulps: the FP32-bulk
+// errors against FP64 did not change with it; x <= 0 here, and a result below
 // 2^-126 flushes to zero, which moves its term by less than that)
 template <typename R>
 __device__ __forceinline__ R texp(R x);
