@@ -235,6 +235,15 @@ def table(st, keys, values):
     return _pack(out, st, ms.value)
 
 
+def tsc_read_seconds(path):
+    """The reference's .tsc reader alone (tsc_io::read_tsc) on a file: (scatterers, rows, seconds of the read)."""
+    na, nr, sec = C.c_int(0), C.c_int(0), C.c_double(0.0)
+    rc = lib().ref_tsc_read(C.c_char_p(os.fsencode(path)), C.byref(na), C.byref(nr), C.byref(sec))
+    if rc != 0:
+        raise RuntimeError("reference tsc reader raised an exception: " + _err())
+    return na.value, nr.value, sec.value
+
+
 def tsc(st, path):
     """The tabulated path reading a .tsc file with the reference's own reader
     (tsc_io::read_tsc), columns = the structure's atoms in order."""

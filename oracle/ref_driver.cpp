@@ -413,6 +413,29 @@ int ref_table_sf(const double *cell, const char *ops, const char *labels, int n_
     }
 }
 
+// The reference's .tsc reader alone (tsc_io::read_tsc, src/IO/tsc_io.cpp:60-125), timed around the call:
+// the scatterer and row counts and the seconds the read took (for the reader comparison in oracle/tsc_speed.py).
+int ref_tsc_read(const char *path, int *n_atoms, int *n_rows, double *seconds)
+{
+    try {
+        vector<string> names;
+        vector<Vector3i> keys;
+        vector<vector<complex<double> > > ff;
+        const auto t0 = std::chrono::steady_clock::now();
+        tsc_io::read_tsc(path, names, keys, ff);
+        *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        *n_atoms = (int)names.size();
+        *n_rows = (int)keys.size();
+        return 0;
+    } catch (const std::exception &ex) {
+        g_last_error = ex.what();
+        return 1;
+    } catch (...) {
+        g_last_error = "unknown exception";
+        return 1;
+    }
+}
+
 // The tabulated path from a .tsc file read by the reference's own reader
 // (tsc_io::read_tsc, src/IO/tsc_io.cpp:60-125), then as ref_table_sf
 // (TscFileBasedSfCalculator, src/Scattering/TscFileBasedSfCalculator.cpp:17-123).
