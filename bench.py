@@ -176,7 +176,7 @@ def fp32_peak_tflops(device):
     return out.value
 
 
-def cpu_baseline(st, sample_frac, threads, multipoles=False):
+def cpu_baseline(st, sample_frac, threads, multipoles=False, electron_f000=None):
     """The reference engine's algorithm on the host cores: the oracle's
     line-ordered restatement of its loop (recurrences along reflection lines,
     one contiguous share of the ordered reflections per thread, as the
@@ -192,7 +192,8 @@ def cpu_baseline(st, sample_frac, threads, multipoles=False):
     from oracle import oracle as O
 
     def timed(m):
-        r = O.compute(st, hkl_subset=np.arange(m), n_threads=threads, multipoles=multipoles, loop="lines")
+        r = O.compute(st, hkl_subset=np.arange(m), n_threads=threads, multipoles=multipoles, loop="lines",
+                      electron_f000=electron_f000)
         return r["c_seconds"]
 
     m = max(2, int(st.n_hkl * sample_frac))
@@ -650,6 +651,11 @@ def run_gpu(args, served=None):
     mpd = wl["multipoles"]
     eng = api.Engine(device)
     calc = api.HcCalculator(eng, st)
+    # electron scattering (Mott-Bethe), folded into the radial tables; f_e(0) per wavefunction only enters F(000),
+    # which no benchmark reflection set holds
+    f000 = [float(w.atomic_number) for w in st.wfns] if args.electron else None
+    if args.electron:
+        calc.set_electron(True, f000)
     n_hkl, n = st.n_hkl, st.n_atoms
     terms = st.terms()
     dev = torch.device("cuda", device)
@@ -753,7 +759,8 @@ def run_gpu(args, served=None):
         return 0
     achieved = wl["flops"] * terms / (k32 * 1e-3) * 1e-12
     peak = fp32_peak_tflops(device)
-    cpu_v, cpu_dt, cpu_m, cpu_pr, cpu_su = cpu_baseline(st, wl["cpu_frac"], os.cpu_count() or 1, multipoles=mpd)
+    cpu_v, cpu_dt, cpu_m, cpu_pr, cpu_su = cpu_baseline(st, wl["cpu_frac"], os.cpu_count() or 1, multipoles=mpd,
+                                                        electron_f000=f000)
     mp = measured_peaks()
     line = {
         "metric": "atom*symop*hkl terms/s (SF+grad)", "value": value, "unit": "terms/s", "n_gpus": world,
@@ -761,7 +768,8 @@ def run_gpu(args, served=None):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk (integer phase reduction, f64 accumulation)",
         "data": "synthetic (seeded)",
         "config": {"workload": wl["desc"], "terms_per_step": terms, "l2": "flushed (256 MB write) between timed steps",
-                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+                   "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                   "scattering": "electron (Mott-Bethe)" if args.electron else "X-ray"},
         "fp64": {"value": world * terms64 / (step64 * 1e-3), "ms_per_step": step64,
                  "kernel_ms": statistics.mean(kern64),
                  "fp32_over_fp64": (terms / step32) / (terms64 / step64),
@@ -798,6 +806,108 @@ def run_gpu(args, served=None):
     return 0
 
 
+def run_taam(args):
+    """Config 1's structure with the TAAM split: hydrogen atoms on the IAM
+    model (seeded four-Gaussian form factors), the rest on HC, through the
+    combined calculator (CombinedStructureFactorCalculator's split: F summed,
+    every atom's derivatives from its own part, the parts in one batched
+    submission).  Host-buffer calls of the combined calculator, timed beside
+    the same call with every atom on HC; FP32-bulk against FP64; the CPU port
+    of both parts on a sample of the reflections."""
+    import torch
+    from discamb_gb300 import api, build, workloads as W
+    from oracle import oracle as O
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(0)
+    build.build()
+    wl = WORKLOADS["config1"]
+    st = W.config1(seed=wl["seed"])
+    z = np.array([st.wfns[w].atomic_number for w in st.atom_wfn])
+    h_idx = np.flatnonzero(z == 1)
+    hc_idx = np.flatnonzero(z != 1)
+    rng = np.random.default_rng(11)
+    a = np.zeros((1, 5))
+    b = np.zeros((1, 5))
+    a[0, :4] = rng.uniform(0.05, 0.5, 4)
+    b[0, :4] = rng.uniform(2.0, 50.0, 4)
+    iam = dict(ngauss=np.array([4], dtype=np.int32), a=a, b=b, c=np.array([0.002]))
+    eng = api.Engine(0)
+
+    def make_iam(sub):
+        sub.atom_type = np.zeros(sub.n_atoms, dtype=np.int64)  # one IAM type: hydrogen
+        return api.IamCalculator(eng, sub, iam)
+
+    comb = api.CombinedCalculator(eng, st, [(lambda sub: api.HcCalculator(eng, sub), hc_idx), (make_iam, h_idx)])
+    hc_all = api.HcCalculator(eng, st)
+    terms = st.terms()
+
+    def timed(call, steps):
+        for _ in range(args.warmup):
+            call()
+        out = []
+        for _ in range(steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            call()
+            out.append(time.perf_counter() - t0)
+        return statistics.mean(out) * 1e3
+
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        ms = timed(lambda: comb.calculate(st.dtdf, precision=api.DSF_FP32_BULK), args.steps)
+        wall = time.perf_counter() - t0
+    clocks = clk.summary()
+    launches = sum(c.last_launch_count() for c, _ in comb.parts)
+    ms_hc = timed(lambda: hc_all.calculate(st.dtdf, precision=api.DSF_FP32_BULK), args.steps)
+    r32 = comb.calculate(st.dtdf, precision=api.DSF_FP32_BULK)
+    t0 = time.perf_counter()
+    r64 = comb.calculate(st.dtdf, precision=api.DSF_FP64)
+    ms64 = (time.perf_counter() - t0) * 1e3
+    err = {"f": float(np.abs(r32["f"] - r64["f"]).sum() / np.abs(r64["f"]).sum())}
+    for k in ("d_xyz", "d_adp", "d_occ"):
+        g32 = np.concatenate([np.ravel(v) for v in r32[k]])
+        g64 = np.concatenate([np.ravel(v) for v in r64[k]])
+        err[k] = float(np.linalg.norm(g32 - g64) / np.linalg.norm(g64))
+    # CPU: the port of both parts on the first 5% of the reflections (line-ordered HC engine, generic IAM engine)
+    m = max(2, int(st.n_hkl * 0.05))
+    threads = os.cpu_count() or 1
+    s_hc, s_h = st.subset(hc_idx), st.subset(h_idx)
+    s_h.atom_type = np.zeros(s_h.n_atoms, dtype=np.int64)
+    t_cpu = O.compute(s_hc, hkl_subset=np.arange(m), n_threads=threads, loop="lines")["c_seconds"]
+    t_cpu += O.compute(s_h, model="iam", iam=iam, hkl_subset=np.arange(m), n_threads=threads)["c_seconds"]
+    cpu_v = terms * m / st.n_hkl / t_cpu
+    line = {
+        "metric": "atom*symop*hkl terms/s (SF+grad)", "value": terms / (ms * 1e-3), "unit": "terms/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 bulk (integer phase reduction, f64 accumulation)",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl["desc"] + "; TAAM split: " + f"{len(hc_idx)} atoms HC, {len(h_idx)} H atoms IAM "
+                                            "(seeded 4-Gaussian f0), combined calculator",
+                   "terms_per_step": terms, "timed": "host-buffer calls of the combined calculator (dT/dF in, "
+                                                     "F and derivatives out)"},
+        "hc_only_ms_per_step": ms_hc,
+        "fp64": {"ms_per_step": ms64, "fp32_over_fp64": ms64 / ms,
+                 "fp32_error": {**err, "measure": "sum|dF|/sum|F|; derivatives per class |dg|/|g|, FP32-bulk "
+                                                 "against FP64 over every reflection"}},
+        "e2e": {"value": terms / (ms * 1e-3), "unit": "terms/s", "ms_per_step": ms,
+                "h2d_bytes_per_step": 2 * 16 * st.n_hkl,
+                "d2h_bytes_per_step": 2 * 16 * st.n_hkl + 80 * st.n_atoms},
+        "cpu_baseline": {"value": cpu_v, "unit": "terms/s", "cores": threads, "kind": "port",
+                         "sample": f"both parts on the first {m} reflections ({t_cpu:.1f} s, C time only)"},
+        "gpu_launches": launches,
+        "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"], "reasons": clocks["reasons"]},
+        "wall_s_timed_region": wall,
+    }
+    print(json.dumps(line))
+    hc_all.close()
+    for c, _ in comb.parts:
+        c.close()
+    eng.close()
+    return 0
+
+
 def served_stream(args):
     """The served mixed stream (config 3: 2,000 requests, Poisson arrivals at
     200 req/s) run in a child process of its own before this process touches
@@ -828,6 +938,10 @@ def main():
     ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="keep the rule's tile shape instead of tuning it at set-up")
+    ap.add_argument("--electron", action="store_true",
+                    help="config1/config2: electron scattering (Mott-Bethe) instead of X-ray")
+    ap.add_argument("--taam", action="store_true",
+                    help="config1: the TAAM split (H atoms on IAM, the rest on HC) through the combined calculator")
     ap.add_argument("--no-served", dest="served", action="store_false",
                     help="config2: skip the served stream (config3) attached to the line")
     ap.add_argument("--c4-crystals", type=int, default=256)
@@ -850,6 +964,8 @@ def main():
         return run_config3(args)
     if args.impl == "reference":
         return run_reference(args)
+    if args.taam:
+        return run_taam(args)
     served = None
     if args.workload == "config2" and args.served and dist_env()[1] == 1:
         served = served_stream(args)
