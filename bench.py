@@ -22,10 +22,15 @@ form is timed beside it (``fp64``) over the whole reflection set, and the
 FP32-bulk error is stated against it over every reflection.  L2 (129 MB)
 is flushed by writing a 256 MB buffer between timed steps (outside the
 timed events).  With config 2 the served stream (config 3: p50/p99
-latency, requests/s) runs afterwards in a child process and is attached
-as ``served_stream``.
+latency, requests/s) runs first in a child process of its own and is
+attached as ``served_stream``.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload configN]
+                    [--electron] [--taam]
+
+``--electron`` (configs 1, 2): electron scattering (Mott-Bethe) instead of
+X-rays.  ``--taam`` (config 1): the hydrogen atoms on the IAM model and the
+rest on HC through the combined calculator, host-buffer calls.
 
 ``--impl reference``: the reference engine's CPU algorithm timed on the
 host cores (the reference sources are absent on the GPU host, so the
