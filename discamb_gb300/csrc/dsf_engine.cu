@@ -1283,7 +1283,12 @@ int dsf_engine_create(int device, dsf_engine **out)
     e->device = device;
     cudaError_t ce = cudaSetDevice(device);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking);
-    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->setup, cudaStreamNonBlocking);
+    // structure set-up (uploads, table builds) on the greatest stream priority: its kernels take SMs ahead of the
+    // pending blocks of calculations running on other streams, so a new structure's first call does not wait
+    // behind them
+    int prio_low = 0, prio_high = 0;
+    if (ce == cudaSuccess) ce = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithPriority(&e->setup, cudaStreamNonBlocking, prio_high);
     if (ce != cudaSuccess) {
         delete e;
         return DSF_ERR_CUDA;
