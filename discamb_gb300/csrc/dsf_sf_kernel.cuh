@@ -632,9 +632,8 @@ __device__ __forceinline__ void sf_grad_body(const DevStructure &S, const CallBu
         const int *sCont = reinterpret_cast<const int *>(st + SL.cont);
 
         // reflections in groups of four: the partial F of a group is reduced across
-        // the warp by one butterfly reduce-scatter of its eight values
-        // one group of four reflections; TAB_REG: its form factors in `cur` while the next group's load into
-        // `nxt` (two buffers taking turns, so no copy between groups)
+        // the warp by one butterfly reduce-scatter of its eight values.  TAB_REG: the
+        // group's form factors in `cur` while the next group's load into `nxt`
         auto group = [&](const int g0, float2 (&cur)[kTabN], float2 (&nxt)[kTabN]) {
             if constexpr (TAB_REG) tab_load(nxt, h0 + g0 + 4);
             R Fv[8];
