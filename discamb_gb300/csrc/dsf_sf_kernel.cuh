@@ -315,7 +315,7 @@ __device__ __forceinline__ void ld_table_row(const float2 *p, float2 *d)
 template <typename R>
 struct StageLayout {
     size_t rs, tr, trm, gw, h2, cont, tab, bytes;
-    // tab: FP32 tabulated model, the tile's form factors [ht][ns][kTileAtoms] (complex64)
+    // tab: FP32 tabulated model, the tile's form factors [ht][kTileAtoms][ns] (complex64)
     __host__ __device__ StageLayout(int ht, int ns, int max_types, bool mp, bool table = false)
     {
         tab = 0;
