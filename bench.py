@@ -9,8 +9,9 @@ multipoles to l = 4 on 300 shared types; F plus the full derivative set
 dT/d(xyz, U, occupancy, P_val, P_lm, kappa, kappa') from a complex N(0,1)
 dT/dF.  Seeded synthetic data (no dataset exists).  ``--workload config1``
 (5,000 atoms, P2_1 2_1 2_1, 54,704 reflections, isotropic B, dF/d(xyz, B,
-occ)), ``config3`` (the served stream) and ``config4`` (a batch of
-tabulated crystals) run the other configurations.
+occ)), ``config0`` (32 atoms in P2_1/c: a small molecule, latency-bound),
+``config3`` (the served stream) and ``config4`` (a batch of tabulated
+crystals) run the other configurations.
 
 One step = one SF + derivative pass over that reflection set.  Metric:
 atom x symop x hkl terms per second (symops = point-group order without
@@ -58,7 +59,11 @@ import numpy as np  # noqa: E402
 #   config1: phase 6 + multipole forward 60 + 1 + f*e*T 8 + accumulate 4 + adjoint 6 + xyz 6 + B 2 + occ 1 = 94
 #   config2: forward 91 (with the aniso exponent 12) + full adjoint 104 (xyz 6, U 12, occ 1, Pv 6, kappa 4,
 #            kappa' 14, Plm 55, p 6) = 195
+#   config0: forward 91 (as config2) + adjoint xyz 6, U 12, occ 1 = 110
 WORKLOADS = {
+    "config0": dict(seed=0, multipoles=False, flops=110, fp64_steps=5, fp64_warmup=2, cpu_frac=1.0, traffic_key=None,
+                    desc="config0: HC multipoles l<=4, 32 atoms (12 C, 12 H, 4 N, 4 O), P21/c, all hkl with "
+                         "sin(theta)/lambda<=0.8, aniso U (H iso), dF/d(xyz,U,occ); the small-molecule case"),
     "config1": dict(seed=1, multipoles=False, flops=94, fp64_steps=3, fp64_warmup=1, cpu_frac=0.25,
                     traffic_key="sf_grad_kernel3<float,HC,0,ISO,4,CS4,PAT_D2>@config1",
                     desc="config1: HC multipoles l<=4, 5000 atoms (150 types), P212121, 54704 hkl d>=1.5A, iso B, "

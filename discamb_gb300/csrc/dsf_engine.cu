@@ -1959,7 +1959,7 @@ static void call_buffers(dsf_structure *s, bool fp64, CallBuffers &C, SfLaunch &
 // shared-memory budget (several blocks per SM), reflection chunks of about
 // `block_terms` atom x reflection pairs per block (at least four sub-tiles)
 static int kind_shape(dsf_structure *s, int kind, bool fp64, bool mp, double block_terms, SfLaunch &L, int &nt,
-                      int &n_chunks, size_t &smem, int ht_cap = 0)
+                      int &n_chunks, size_t &smem, int ht_cap = 0, bool short_chunks = false)
 {
     dsf_engine *e = s->eng;
     const int t0 = kind ? s->n_tiles_plain : 0, t1 = kind ? s->n_tiles : s->n_tiles_plain;
@@ -1977,8 +1977,14 @@ static int kind_shape(dsf_structure *s, int kind, bool fp64, bool mp, double blo
     while (ht_cap >= 4 && ht > ht_cap) ht /= 2;
     smem = sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types, table);
     if (smem > e->max_smem) return fail(e, DSF_ERR_UNSUPPORTED, "shared-memory tile does not fit this device");
-    L.ht = ht;
     int chunk = (int)std::min<double>(s->n_hkl, std::max(1.0, block_terms / kTileAtoms));
+    // short_chunks (a single structure's launch): a small problem whose reflection chunks would be shorter than
+    // four sub-tiles takes shorter sub-tiles instead (down to 4 reflections), so its grid still spreads over the
+    // SMs; larger problems are unchanged
+    if (short_chunks)
+        while (ht > 4 && chunk < 4 * ht) ht /= 2;
+    smem = sf3_smem_bytes(fp64, mp, ht, s->n_sym, L.max_types, table);
+    L.ht = ht;
     chunk = std::max(chunk, 4 * ht);
     chunk = (chunk + ht - 1) / ht * ht;
     L.hkl_chunk = chunk;
@@ -2124,7 +2130,7 @@ int dsf_calculate_device(dsf_structure *s, int precision, int flags, const doubl
         const int ntk = kind ? s->n_tiles - s->n_tiles_plain : s->n_tiles_plain;
         const int n_chunks0 = chunk_count(e, ntk, s->n_hkl, bps);
         const double block_terms = (double)kTileAtoms * ((s->n_hkl + n_chunks0 - 1) / n_chunks0);
-        if ((rc = kind_shape(s, kind, fp64, mp, block_terms, L, nt, n_chunks, smem, ht_cap))) return rc;
+        if ((rc = kind_shape(s, kind, fp64, mp, block_terms, L, nt, n_chunks, smem, ht_cap, true))) return rc;
         if (nt <= 0) continue;
         K3Args A;
         A.S = &s->dev;
