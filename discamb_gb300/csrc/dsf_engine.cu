@@ -391,6 +391,33 @@ __global__ void grad_epilogue_kernel(GradParams P, const double *g_acc, const in
                           d_kappa, d_kappa_p);
 }
 
+// a single structure's call in two small launches around the structure-factor kernels: before them the adjoint
+// weights and the zeroed F and derivative accumulators (in place of a weight kernel and two memsets), after them
+// F and the derivatives in the caller's conventions and order (in place of two epilogue kernels)
+__global__ void call_pre_kernel(int n_hkl, int n_g, const double2 *dtdf, const double *mult, const double2 *cinv,
+                                int centro, double2 *gw_d, float2 *gw_f, const int *perm, double2 *facc, double *gacc)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_hkl) {
+        gw_one(i, dtdf, mult, cinv, centro, gw_d, gw_f, perm);
+        facc[i] = make_double2(0.0, 0.0);
+    }
+    if (i < n_g) gacc[i] = 0.0;
+}
+
+__global__ void call_post_kernel(int n_hkl, const double2 *facc, const double *mult, const double2 *cinv, int centro,
+                                 double *f_out, const int *hperm, int grad, GradParams P, const double *g_acc,
+                                 const int *perm, const int *adpk, const double *w, const double *mult_w,
+                                 const double *dmat, const int *plm_lmax, double *d_xyz, double *d_adp,
+                                 double *d_occ, double *d_pval, double *d_plm, double *d_kappa, double *d_kappa_p)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_hkl) f_epilogue_one(i, facc, mult, cinv, centro, f_out, hperm);
+    if (grad && i < P.n_atoms)
+        grad_epilogue_one(i, P, g_acc, perm, adpk, w, mult_w, dmat, plm_lmax, d_xyz, d_adp, d_occ, d_pval, d_plm,
+                          d_kappa, d_kappa_p);
+}
+
 // multipole-parameter derivatives summed over the atoms of each type (atoms of
 // one type share P_val, P_lm in their local frames, kappa, kappa'); inputs and
 // outputs in the caller's (original) atom order
@@ -1907,14 +1934,13 @@ static int call_check(dsf_structure *s, int precision, int flags, const double *
 static int call_pre(dsf_structure *s, const double *dtdf_device, cudaStream_t st)
 {
     dsf_engine *e = s->eng;
-    const int n_hkl = s->n_hkl;
-    gw_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, reinterpret_cast<const double2 *>(dtdf_device),
-                                                   s->d_hmult.as<double>(), s->d_cinv.as<double2>(), s->centro_mode,
-                                                   s->d_gw_d.as<double2>(), s->d_gw_f.as<float2>(),
-                                                   s->d_hperm.as<int>());
+    const int n_hkl = s->n_hkl, n_g = kNch * s->n_atoms, n = std::max(n_hkl, n_g);
+    call_pre_kernel<<<(n + 255) / 256, 256, 0, st>>>(n_hkl, n_g, reinterpret_cast<const double2 *>(dtdf_device),
+                                                     s->d_hmult.as<double>(), s->d_cinv.as<double2>(),
+                                                     s->centro_mode, s->d_gw_d.as<double2>(),
+                                                     s->d_gw_f.as<float2>(), s->d_hperm.as<int>(),
+                                                     s->d_facc.as<double2>(), s->d_gacc.as<double>());
     DSF_CUDA(cudaGetLastError());
-    DSF_CUDA(cudaMemsetAsync(s->d_facc.p, 0, 16 * (size_t)n_hkl, st));
-    DSF_CUDA(cudaMemsetAsync(s->d_gacc.p, 0, sizeof(double) * kNch * (size_t)s->n_atoms, st));
     return DSF_OK;
 }
 
@@ -1997,28 +2023,25 @@ static int call_post(dsf_structure *s, int flags, const dsf_outputs *out, cudaSt
     dsf_engine *e = s->eng;
     const int n_hkl = s->n_hkl, n = s->n_atoms;
     const bool mp = (flags & DSF_D_MULTIPOLE) && s->model == MODEL_HC;
-    f_epilogue_kernel<<<(n_hkl + 255) / 256, 256, 0, st>>>(n_hkl, s->d_facc.as<double2>(), s->d_hmult.as<double>(),
-                                                           s->d_cinv.as<double2>(), s->centro_mode, out->f,
-                                                           s->d_hperm.as<int>());
+    const bool grad = (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) != 0;
+    GradParams P;
+    P.n_atoms = n;
+    P.xyz_conv = s->xyz_conv;
+    std::copy(s->Minv, s->Minv + 9, P.Minv);
+    std::copy(s->A6, s->A6 + 36, P.A6);
+    P.want_xyz = (flags & DSF_D_XYZ) != 0;
+    P.want_adp = (flags & DSF_D_ADP) != 0;
+    P.want_occ = (flags & DSF_D_OCC) != 0;
+    P.want_mp = mp;
+    const int m = grad ? std::max(n_hkl, n) : n_hkl;
+    call_post_kernel<<<(m + 127) / 128, 128, 0, st>>>(
+        n_hkl, s->d_facc.as<double2>(), s->d_hmult.as<double>(), s->d_cinv.as<double2>(), s->centro_mode, out->f,
+        s->d_hperm.as<int>(), grad ? 1 : 0, P, s->d_gacc.as<double>(), s->d_perm.as<int>(),
+        s->d_atom_adpk.as<int>(), s->d_w_d.as<double>(), s->d_multw.as<double>(), s->d_dmat.as<double>(),
+        s->d_plm_lmax.as<int>(), out->d_xyz, out->d_adp, out->d_occ, out->d_pval, out->d_plm, out->d_kappa,
+        out->d_kappa_prime);
     launches++;
     DSF_CUDA(cudaGetLastError());
-    if (flags & (DSF_D_XYZ | DSF_D_ADP | DSF_D_OCC | DSF_D_MULTIPOLE)) {
-        GradParams P;
-        P.n_atoms = n;
-        P.xyz_conv = s->xyz_conv;
-        std::copy(s->Minv, s->Minv + 9, P.Minv);
-        std::copy(s->A6, s->A6 + 36, P.A6);
-        P.want_xyz = (flags & DSF_D_XYZ) != 0;
-        P.want_adp = (flags & DSF_D_ADP) != 0;
-        P.want_occ = (flags & DSF_D_OCC) != 0;
-        P.want_mp = mp;
-        grad_epilogue_kernel<<<(n + 127) / 128, 128, 0, st>>>(
-            P, s->d_gacc.as<double>(), s->d_perm.as<int>(), s->d_atom_adpk.as<int>(), s->d_w_d.as<double>(),
-            s->d_multw.as<double>(), s->d_dmat.as<double>(), s->d_plm_lmax.as<int>(), out->d_xyz, out->d_adp, out->d_occ, out->d_pval,
-            out->d_plm, out->d_kappa, out->d_kappa_prime);
-        launches++;
-        DSF_CUDA(cudaGetLastError());
-    }
     return DSF_OK;
 }
 
