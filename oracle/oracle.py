@@ -217,11 +217,13 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     pos = (m @ st.xyz.T).T if st.xyz_convention == "fractional" else st.xyz
     nadp = st.n_adp()
     adp = np.zeros((n, 6))
-    for i, a in enumerate(st.adp):
-        if len(a) == 6:
-            adp[i] = convert_adp(cell, a, st.adp_convention, "U_cart") * 2 * math.pi ** 2
-        elif len(a) == 1:
-            adp[i, 0] = a[0] * 2 * math.pi ** 2
+    i6 = np.flatnonzero(nadp == 6)
+    i1 = np.flatnonzero(nadp == 1)
+    if len(i6):  # the same conversion for every anisotropic atom, as one batched matrix product
+        adp[i6] = convert_adp(cell, np.array([st.adp[i] for i in i6], dtype=np.float64), st.adp_convention,
+                              "U_cart") * 2 * math.pi ** 2
+    if len(i1):
+        adp[i1, 0] = np.array([st.adp[i][0] for i in i1], dtype=np.float64) * 2 * math.pi ** 2
     pr.n_atoms = n
     pr.atom_wfn = keep.i(st.atom_wfn)
     pr.atom_type = keep.i(st.atom_type)
@@ -298,9 +300,8 @@ def compute(st, model="hc", n_threads=None, derivatives=("xyz", "adp", "occ"), m
     if st.xyz_convention == "fractional":
         d_xyz = convert_xyz_gradient(cell, d_xyz, "cartesian", "fractional")
     d_adp = out["d_adp"].reshape(n, 6).copy()
-    for i in range(n):
-        if nadp[i] == 6:
-            d_adp[i] = convert_adp_gradient(cell, d_adp[i], "U_cart", st.adp_convention)
+    if len(i6):
+        d_adp[i6] = convert_adp_gradient(cell, d_adp[i6], "U_cart", st.adp_convention)
     # c_seconds: the C computation alone (the algorithm's own time, without this wrapper's array set-up)
     res_d = dict(f=f, d_xyz=d_xyz, d_adp=[d_adp[i, :nadp[i]] for i in range(n)], d_occ=out["d_occ"], c_seconds=t_c)
     if multipoles:
